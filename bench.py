@@ -1,0 +1,377 @@
+"""Benchmark of the render hot path on GB300.
+
+Headline workload (one step = one nearest-hit pass of the ray-cast kernel over
+one batch): a displaced icosphere of subdivision 6 (81,920 triangles, value
+noise seed 7) in a 10-triangle box room, 4,194,304 rays with origins uniform
+in the room and directions uniform on the sphere (seed 7), FP32, hit index
+and t bit-exact against the oracle. Metric: Mrays/s.
+
+Also reported (extra keys): frame time p50/p99 and Mrays/s of the 1280x736,
+1 spp, 5-bounce interactive frame of the room-and-sphere scene.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Under torchrun (N > 1) every rank runs the same workload on its own GPU
+(replicas: rays are independent, there is no collective on the data path);
+value = rays of all ranks / max-over-ranks time.
+"""
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N_RAYS = 4194304
+METRIC = "Mrays/s (nearest-hit rays per second)"
+WORKLOAD = "ray-cast isolation: displaced icosphere subdiv 6 (81,920 tris, seed 7) in a 10-tri box room, " \
+           "4,194,304 rays uniform in the room / on S^2 (seed 7)"
+
+
+def _peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def _traffic(kernel_key):
+    try:
+        with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
+            return json.load(f).get(kernel_key)
+    except Exception:
+        return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons while the timed region runs."""
+
+    FIELDS = "clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown," \
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown," \
+             "clocks_event_reasons.sw_power_cap"
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+            time.sleep(0.3)
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            time.sleep(0.2)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx = max(mx, float(parts[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[3:7]):
+                if v.lower() in ("active", "1", "0x1"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def build_c1():
+    import convector_gb300 as cg
+    from convector_gb300 import scenes
+    text, mats = scenes.displaced_icosphere()
+    bvh = cg.Bvh.from_meshes([cg.Mesh.parse(text, mats)])
+    o, d = scenes.random_rays(N_RAYS, seed=7)
+    return bvh, o, d
+
+
+def build_c0():
+    import convector_gb300 as cg
+    from convector_gb300 import scenes
+    text, mats = scenes.room_sphere()
+    bvh = cg.Bvh.from_meshes([cg.Mesh.parse(text, mats)])
+    return bvh
+
+
+def cpu_sample_rays_per_s(osc, o, d, target_s=12.0, max_rays=1 << 20):
+    """Times the oracle's packet traversal (all host cores) on a bounded sample."""
+    threads = os.cpu_count() or 1
+    n = 8192
+    t0 = time.perf_counter()
+    osc.intersect(o[:n], d[:n], nthreads=threads)
+    est = (time.perf_counter() - t0) / n
+    n = int(min(max_rays, max(8192, target_s / max(est, 1e-9))))
+    n -= n % 8
+    t0 = time.perf_counter()
+    osc.intersect(o[:n], d[:n], nthreads=threads)
+    dt = time.perf_counter() - t0
+    return n / dt, threads, n, dt
+
+
+def run_reference(args):
+    """The reference's CPU path on the host cores: the oracle's C++ restatement
+    of the reference AVX packet traversal (the Rust original cannot be built)."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    from oracle import oracle as orc
+    bvh, o, d = build_c1()
+    osc = orc.OracleScene.from_bvh(bvh)
+    threads = os.cpu_count() or 1
+    sample = 1 << 16
+    for s in range(args.warmup):
+        lo = (s * sample) % (N_RAYS - sample)
+        osc.intersect(o[lo:lo + sample], d[lo:lo + sample], nthreads=threads)
+    times = []
+    for s in range(args.steps):
+        lo = ((args.warmup + s) * sample) % (N_RAYS - sample)
+        t0 = time.perf_counter()
+        osc.intersect(o[lo:lo + sample], d[lo:lo + sample], nthreads=threads)
+        times.append(time.perf_counter() - t0)
+    total = sum(times)
+    value = sample * args.steps / total / 1e6
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "Mrays/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "sample_rays_per_step": sample, "traversal": "reference 8-ray packets"},
+        "cpu_baseline": {"value": value, "unit": "Mrays/s", "cores": threads, "kind": "port",
+                         "sample": "%d rays per step of the same workload, %d steps" % (sample, args.steps)},
+        "e2e": {"value": value, "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def run_ours(args):
+    import torch
+    import torch.distributed as dist
+
+    import convector_gb300 as cg
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl")
+    cg.lib(build=True)
+
+    bvh, o, d = build_c1()
+    scene = cg.Scene(bvh)
+    n = o.shape[0]
+    rays = torch.from_numpy(np.concatenate([o.T, d.T]).copy()).cuda()
+    t_out = torch.empty(n, dtype=torch.float32, device="cuda")
+    tri_out = torch.empty(n, dtype=torch.int32, device="cuda")
+    cnt = torch.empty(2 * n, dtype=torch.int32, device="cuda")
+    stream = torch.cuda.current_stream().cuda_stream
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")  # larger than the 129 MB L2
+
+    # Algorithmic bytes per launch (counters from one untimed pass per variant).
+    algo = {}
+    for trav in (0, 1):
+        scene.intersect_nearest_device(rays, t_out, tri_out, traversal=trav, counters=cnt, stream=stream)
+        torch.cuda.synchronize()
+        c = cnt.cpu().numpy().view(np.uint32).astype(np.int64)
+        na, nt = c[:n], c[n:]
+        if trav == 0:  # packet counters repeat on the 8 lanes: node and triangle data once per packet
+            b = int((32 * na[::8] + 36 * nt[::8]).sum()) + 32 * n
+        else:
+            b = int((32 * na + 36 * nt).sum()) + 32 * n
+        algo[trav] = {"bytes": b, "boxes_per_ray": float(na.mean()), "tris_per_ray": float(nt.mean())}
+
+    def step(trav):
+        scene.intersect_nearest_device(rays, t_out, tri_out, traversal=trav, stream=stream)
+
+    # Pick the faster traversal variant on a short untimed trial.
+    trial = {}
+    for trav in (0, 1):
+        for _ in range(2):
+            step(trav)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(3):
+            step(trav)
+        e1.record()
+        torch.cuda.synchronize()
+        trial[trav] = e0.elapsed_time(e1) / 3
+    trav = min(trial, key=trial.get)
+
+    for _ in range(args.warmup):
+        flush.zero_()
+        step(trav)
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    with ClockSampler(local) as clocks:
+        torch.cuda.synchronize()
+        wall0 = time.perf_counter()
+        for e0, e1 in evs:
+            flush.zero_()  # L2 flush between timed iterations, outside the timed span
+            e0.record()
+            step(trav)
+            e1.record()
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - wall0
+    step_ms = [e0.elapsed_time(e1) for e0, e1 in evs]
+    total_ms = sum(step_ms)
+    if world > 1:
+        tt = torch.tensor([total_ms], device="cuda", dtype=torch.float64)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        total_ms = float(tt.item())
+        dist.barrier()
+    ms_per_step = total_ms / args.steps
+    value = world * n * args.steps / (total_ms * 1e-3) / 1e6
+
+    # End to end through the C-ABI with host buffers: copies in and out every step.
+    pin = [torch.from_numpy(np.ascontiguousarray(a)).pin_memory() for a in
+           (o[:, 0], o[:, 1], o[:, 2], d[:, 0], d[:, 1], d[:, 2])]
+    t_host = torch.empty(n, dtype=torch.float32).pin_memory()
+    tri_host = torch.empty(n, dtype=torch.int32).pin_memory()
+    L = cg.lib()
+    import ctypes
+    ptrs = [ctypes.c_void_p(p.data_ptr()) for p in pin]
+
+    def e2e_call():
+        st = L.cvx_intersect_nearest(scene._h, *ptrs, n, 1.0e5, trav, ctypes.c_void_p(t_host.data_ptr()),
+                                     ctypes.c_void_p(tri_host.data_ptr()))
+        if st:
+            cg._check(st)
+
+    for _ in range(max(1, args.warmup)):
+        e2e_call()
+    if world > 1:
+        dist.barrier()
+    e2e_steps = max(3, min(args.steps, 20))
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        e2e_call()
+    e2e_s = time.perf_counter() - t0
+    if world > 1:
+        tt = torch.tensor([e2e_s], device="cuda", dtype=torch.float64)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        e2e_s = float(tt.item())
+    e2e_value = world * n * e2e_steps / e2e_s / 1e6
+
+    render = None
+    if rank == 0 and not args.no_render:
+        render = bench_render(cg, torch)
+
+    if rank == 0:
+        peak, peak_kind = _peaks()
+        bytes_launch = algo[trav]["bytes"]
+        achieved = bytes_launch / (ms_per_step * 1e-3) / 1e9
+        kname = "k_intersect_packet" if trav == 0 else "k_intersect_single"
+        cpu = None
+        if world == 1:
+            from oracle import oracle as orc
+            osc = orc.OracleScene.from_bvh(bvh)
+            rps, cores, sample, dt = cpu_sample_rays_per_s(osc, o, d)
+            cpu = {"value": rps / 1e6, "unit": "Mrays/s", "cores": cores, "kind": "port",
+                   "sample": "%d rays of the same workload (%.1f s), reference 8-ray packet traversal" % (sample, dt)}
+        line = {
+            "metric": METRIC, "value": value, "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "rays_per_step": n, "triangles": int(bvh.triangles.shape[0]),
+                       "traversal": "packet8" if trav == 0 else "single", "trial_ms": trial,
+                       "l2": "flushed between timed steps (256 MB write)", "parallelism": "replicas"},
+            "e2e": {"value": e2e_value, "unit": "Mrays/s", "h2d_bytes_per_step": 24 * n, "d2h_bytes_per_step": 8 * n},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                         "peak_kind": peak_kind, "traffic": _traffic(kname),
+                         "algorithmic_bytes_per_launch": bytes_launch,
+                         "boxes_per_ray": algo[trav]["boxes_per_ray"], "tris_per_ray": algo[trav]["tris_per_ray"],
+                         "kernel": kname},
+            "cpu_baseline": cpu,
+            "clocks": clocks.summary(),
+            "gpu_launches": args.steps,
+            "wall_s_timed": wall,
+            "step_ms_p50": statistics.median(step_ms),
+            "render": render,
+        }
+        print(json.dumps(line))
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def bench_render(cg, torch):
+    """1280x736, 1 spp, 5 bounces on the room-and-sphere scene: frame p50/p99."""
+    from convector_gb300 import scenes
+    bvh = build_c0()
+    scene = cg.Scene(bvh)
+    scenes.default_camera(scene.camera)
+    out = {}
+    for name, order, frames in (("per_group", cg.RNG_GROUP, 30), ("patch_exact", cg.RNG_PATCH, 10)):
+        best = None
+        for trav in (cg.TRAVERSE_PACKET, cg.TRAVERSE_SINGLE):
+            r = cg.Renderer(scene, 1280, 736, rng_order=order, traversal=trav)
+            for f in range(3):
+                r.render_frame_u8(f, gbuffer=False)
+            ms, rays = [], 0
+            for f in range(frames):
+                r.render_frame_u8(42 + f, gbuffer=False)
+                nr, m = r.stats()
+                ms.append(m)
+                rays += nr
+            res = {"traversal": "packet8" if trav == 0 else "single", "frame_ms_p50": float(np.percentile(ms, 50)),
+                   "frame_ms_p99": float(np.percentile(ms, 99)), "mrays_per_s": rays / (sum(ms) * 1e-3) / 1e6,
+                   "rays_per_frame": rays / frames}
+            if best is None or res["frame_ms_p50"] < best["frame_ms_p50"]:
+                best = res
+        out[name] = best
+    return out
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-render", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

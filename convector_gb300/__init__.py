@@ -1,0 +1,377 @@
+"""GB300 render hot path of ruuda/convector.
+
+Python mirror of the reference's Rust API for the render path, over the C-ABI
+in include/convector_gpu.h (libconvector_gpu.so):
+
+    SMaterial               material.rs:74-136   32-bit material encoding
+    Mesh.load_with_materials wavefront.rs:83-152  OBJ loading
+    Bvh.from_meshes / build bvh.rs:488-568       binned tree-SAH build
+    Scene.from_meshes       scene.rs:114-129     scene + camera
+    Camera                  scene.rs:20-100
+    Renderer                renderer.rs:120-410  frames, accumulation, resolve
+
+There is no CPU fallback: every render and query runs the CUDA kernels, and
+a missing or unbuilt extension raises.
+"""
+
+import ctypes
+import math
+import os
+
+import numpy as np
+
+from . import _build
+
+__all__ = ["SMaterial", "Mesh", "Bvh", "Scene", "Camera", "Renderer", "RenderConfig", "CvxError", "lib",
+           "TRIANGLE_DTYPE_WORDS", "NODE_DTYPE_WORDS"]
+
+TRIANGLE_DTYPE_WORDS = 16  # cvx_triangle: v0 v1 v2 (9 f32), uv0..2 (6 f32), material (u32)
+NODE_DTYPE_WORDS = 8       # cvx_bvh_node: origin far_ (6 f32), index, len (u32)
+
+TRAVERSE_PACKET, TRAVERSE_SINGLE = 0, 1
+RNG_PATCH, RNG_GROUP = 0, 1
+MODE_MEGAKERNEL, MODE_WAVEFRONT = 0, 1
+
+_LIB = None
+
+
+class CvxError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__("convector_gpu error %d: %s" % (status, msg))
+        self.status = status
+
+
+class _Camera(ctypes.Structure):
+    _fields_ = [("position", ctypes.c_float * 3), ("position_delta", ctypes.c_float * 3),
+                ("orientation", ctypes.c_float * 4), ("orientation_delta", ctypes.c_float * 4),
+                ("screen_distance", ctypes.c_float)]
+
+
+class RenderConfig(ctypes.Structure):
+    _fields_ = [("rng_order", ctypes.c_uint32), ("traversal", ctypes.c_uint32), ("mode", ctypes.c_uint32),
+                ("block_size", ctypes.c_uint32), ("use_graph", ctypes.c_uint32)]
+
+
+def lib(build=False):
+    """Loads libconvector_gpu.so (building it first when `build` is true)."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    path = _build.build() if build else _build.LIB
+    if not os.path.exists(path):
+        raise RuntimeError("libconvector_gpu.so is not built: run __graft_entry__.build() or "
+                           "python -m convector_gb300._build")
+    L = ctypes.CDLL(path)
+    P, U32, I32, F32, SZ = ctypes.c_void_p, ctypes.c_uint32, ctypes.c_int32, ctypes.c_float, ctypes.c_size_t
+    sig = {
+        "cvx_last_error": (I32, [ctypes.c_char_p, SZ]),
+        "cvx_mesh_load_obj": (I32, [ctypes.c_char_p, P, P, U32, P]),
+        "cvx_mesh_parse_obj": (I32, [ctypes.c_char_p, SZ, P, P, U32, P]),
+        "cvx_mesh_num_triangles": (U32, [P]),
+        "cvx_mesh_destroy": (None, [P]),
+        "cvx_bvh_from_meshes": (I32, [P, U32, P]),
+        "cvx_bvh_build": (I32, [P, U32, P]),
+        "cvx_bvh_num_nodes": (U32, [P]),
+        "cvx_bvh_num_triangles": (U32, [P]),
+        "cvx_bvh_copy_nodes": (None, [P, P]),
+        "cvx_bvh_copy_triangles": (None, [P, P]),
+        "cvx_bvh_copy_source_index": (None, [P, P]),
+        "cvx_bvh_stats": (None, [P, P, P, P]),
+        "cvx_bvh_destroy": (None, [P]),
+        "cvx_camera_default": (None, [P]),
+        "cvx_camera_set_rotation": (None, [P, F32, F32]),
+        "cvx_camera_set_fov": (None, [P, F32]),
+        "cvx_scene_create": (I32, [P, U32, P, U32, P]),
+        "cvx_scene_from_bvh": (I32, [P, P]),
+        "cvx_scene_num_direct_samples": (U32, [P]),
+        "cvx_scene_set_light_pick": (I32, [P, U32]),
+        "cvx_scene_destroy": (None, [P]),
+        "cvx_intersect_nearest": (I32, [P, P, P, P, P, P, P, U32, F32, U32, P, P]),
+        "cvx_intersect_nearest_device": (I32, [P, P, U32, F32, U32, P, P, P, P]),
+        "cvx_renderer_create": (I32, [P, U32, U32, P, P]),
+        "cvx_renderer_destroy": (None, [P]),
+        "cvx_renderer_set_camera": (I32, [P, P]),
+        "cvx_render_frame_u8": (I32, [P, U32, P, P]),
+        "cvx_accumulate_frame_f32": (I32, [P, U32, P]),
+        "cvx_resolve_u8": (I32, [P, U32, P]),
+        "cvx_read_accumulator": (I32, [P, P]),
+        "cvx_clear_accumulator": (I32, [P]),
+        "cvx_read_frame_f32": (I32, [P, P]),
+        "cvx_renderer_stats": (I32, [P, P, P]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+    _LIB = L
+    return L
+
+
+def _check(status):
+    if status != 0:
+        buf = ctypes.create_string_buffer(1024)
+        lib().cvx_last_error(buf, 1024)
+        raise CvxError(status, buf.value.decode(errors="replace"))
+
+
+def _ptr(a):
+    return None if a is None else ctypes.c_void_p(a.ctypes.data)
+
+
+class SMaterial:
+    """The reference's 32-bit material (material.rs:10-31, 84-136)."""
+
+    @staticmethod
+    def sky():
+        return 0xC0000000
+
+    @staticmethod
+    def diffuse(r, g, b):
+        def q(c):  # `(c * 255.0) as u32` on f32
+            v = float(np.float32(c) * np.float32(255.0))
+            return 0 if not v > 0 else min(int(v), 0xFFFFFFFF)
+        return ((q(b) << 16) | (q(g) << 8) | q(r)) & 0xFFFFFFFF
+
+    @staticmethod
+    def white():
+        return SMaterial.diffuse(1.0, 1.0, 1.0)
+
+    @staticmethod
+    def glass():
+        return 0x60000000
+
+    @staticmethod
+    def with_glossiness(mat, glossiness):
+        assert 0 <= glossiness <= 6
+        return ((mat & 0b11100011_11111111_11111111_11111111) | (glossiness << 26)) & 0xFFFFFFFF
+
+    @staticmethod
+    def with_texture(mat, texture_index):
+        assert 0 <= texture_index <= 3
+        return ((mat & 0b11111100_11111111_11111111_11111111) | (texture_index << 24)) & 0xFFFFFFFF
+
+    @staticmethod
+    def is_direct_sample(mat):
+        return (mat >> 30) & 1 == 1
+
+
+def _material_arrays(materials):
+    materials = materials or {}
+    names = list(materials.keys())
+    arr_names = (ctypes.c_char_p * max(1, len(names)))(*[n.encode() for n in names])
+    arr_vals = np.array([materials[n] for n in names] or [0], dtype=np.uint32)
+    return arr_names, arr_vals, len(names)
+
+
+class Mesh:
+    """A loaded OBJ mesh (wavefront.rs:24-28)."""
+
+    def __init__(self, handle):
+        self._h = ctypes.c_void_p(handle)
+
+    @staticmethod
+    def load(path):
+        return Mesh.load_with_materials(path, {})
+
+    @staticmethod
+    def load_with_materials(path, materials):
+        names, vals, n = _material_arrays(materials)
+        out = ctypes.c_void_p()
+        _check(lib().cvx_mesh_load_obj(os.fsencode(path), names, _ptr(vals), n, ctypes.byref(out)))
+        return Mesh(out.value)
+
+    @staticmethod
+    def parse(text, materials=None):
+        data = text.encode() if isinstance(text, str) else bytes(text)
+        names, vals, n = _material_arrays(materials)
+        out = ctypes.c_void_p()
+        _check(lib().cvx_mesh_parse_obj(data, len(data), names, _ptr(vals), n, ctypes.byref(out)))
+        return Mesh(out.value)
+
+    @property
+    def num_triangles(self):
+        return lib().cvx_mesh_num_triangles(self._h)
+
+    def __del__(self):
+        if getattr(self, "_h", None) and self._h.value and _LIB is not None:
+            _LIB.cvx_mesh_destroy(self._h)
+            self._h = None
+
+
+class Bvh:
+    """A built BVH in the reference's node and triangle order (bvh.rs:33-42)."""
+
+    def __init__(self, handle):
+        L = lib()
+        self._h = ctypes.c_void_p(handle)
+        nn, nt = L.cvx_bvh_num_nodes(self._h), L.cvx_bvh_num_triangles(self._h)
+        self.nodes = np.zeros((nn, NODE_DTYPE_WORDS), dtype=np.uint32)
+        self.triangles = np.zeros((nt, TRIANGLE_DTYPE_WORDS), dtype=np.uint32)
+        self.source_index = np.zeros(nt, dtype=np.uint32)
+        L.cvx_bvh_copy_nodes(self._h, _ptr(self.nodes))
+        L.cvx_bvh_copy_triangles(self._h, _ptr(self.triangles))
+        L.cvx_bvh_copy_source_index(self._h, _ptr(self.source_index))
+        a, b, d = ctypes.c_float(), ctypes.c_float(), ctypes.c_uint32()
+        L.cvx_bvh_stats(self._h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(d))
+        self.avg_tris_per_leaf, self.avg_area_ratio, self.depth = a.value, b.value, d.value
+
+    @staticmethod
+    def from_meshes(meshes):
+        arr = (ctypes.c_void_p * len(meshes))(*[m._h.value for m in meshes])
+        out = ctypes.c_void_p()
+        _check(lib().cvx_bvh_from_meshes(arr, len(meshes), ctypes.byref(out)))
+        return Bvh(out.value)
+
+    @staticmethod
+    def build(triangles):
+        tris = np.ascontiguousarray(triangles).view(np.uint32).reshape(-1, TRIANGLE_DTYPE_WORDS)
+        out = ctypes.c_void_p()
+        _check(lib().cvx_bvh_build(_ptr(tris), tris.shape[0], ctypes.byref(out)))
+        return Bvh(out.value)
+
+    @property
+    def triangles_f32(self):
+        return self.triangles.view(np.float32)
+
+    @property
+    def nodes_f32(self):
+        return self.nodes.view(np.float32)
+
+    @property
+    def direct_sample(self):
+        """Indices of direct-sample triangles in BVH order (scene.rs:117-122)."""
+        return np.nonzero((self.triangles[:, 15] >> 30) & 1)[0].astype(np.uint32)
+
+    def __del__(self):
+        if getattr(self, "_h", None) and self._h.value and _LIB is not None:
+            _LIB.cvx_bvh_destroy(self._h)
+            self._h = None
+
+
+class Camera:
+    """scene.rs:20-100; the setters compute on the host in f32 like the reference."""
+
+    def __init__(self):
+        self._c = _Camera()
+        lib().cvx_camera_default(ctypes.byref(self._c))
+
+    def set_position(self, position, delta=(0.0, 0.0, 0.0)):
+        self._c.position[:] = [float(np.float32(v)) for v in position]
+        self._c.position_delta[:] = [float(np.float32(v)) for v in delta]
+
+    def set_orientation(self, orientation, delta=(0.0, 0.0, 0.0, 0.0)):
+        self._c.orientation[:] = [float(np.float32(v)) for v in orientation]
+        self._c.orientation_delta[:] = [float(np.float32(v)) for v in delta]
+
+    def set_rotation(self, radians, delta=0.0):
+        lib().cvx_camera_set_rotation(ctypes.byref(self._c), radians, delta)
+
+    def set_fov(self, fov):
+        lib().cvx_camera_set_fov(ctypes.byref(self._c), fov)
+
+    def as_array(self):
+        """pos[3], pos_delta[3], q[4], dq[4], screen_distance as float32."""
+        c = self._c
+        return np.array(list(c.position) + list(c.position_delta) + list(c.orientation)
+                        + list(c.orientation_delta) + [c.screen_distance], dtype=np.float32)
+
+
+class Scene:
+    """A scene resident on the GPU (scene.rs:102-129)."""
+
+    def __init__(self, bvh, light_pick=1):
+        self.bvh = bvh
+        self.camera = Camera()
+        out = ctypes.c_void_p()
+        _check(lib().cvx_scene_create(_ptr(bvh.triangles), bvh.triangles.shape[0], _ptr(bvh.nodes),
+                                      bvh.nodes.shape[0], ctypes.byref(out)))
+        self._h = out
+        if light_pick != 1:
+            _check(lib().cvx_scene_set_light_pick(self._h, light_pick))
+
+    @staticmethod
+    def from_meshes(meshes, light_pick=1):
+        return Scene(Bvh.from_meshes(meshes), light_pick=light_pick)
+
+    def direct_sample_num(self):
+        return lib().cvx_scene_num_direct_samples(self._h)
+
+    def intersect_nearest(self, origins, directions, far=1.0e5, traversal=TRAVERSE_PACKET):
+        """Bvh::intersect_nearest over rays (n x 3 arrays); returns (t, triangle index in BVH order)."""
+        o = np.ascontiguousarray(origins, dtype=np.float32)
+        d = np.ascontiguousarray(directions, dtype=np.float32)
+        n = o.shape[0]
+        cols = [np.ascontiguousarray(o[:, k]) for k in range(3)] + [np.ascontiguousarray(d[:, k]) for k in range(3)]
+        t = np.empty(n, dtype=np.float32)
+        tri = np.empty(n, dtype=np.int32)
+        _check(lib().cvx_intersect_nearest(self._h, *[_ptr(c) for c in cols], n, far, traversal, _ptr(t), _ptr(tri)))
+        return t, tri
+
+    def intersect_nearest_device(self, rays_soa, t_out, tri_out, far=1.0e5, traversal=TRAVERSE_PACKET,
+                                 counters=None, stream=None):
+        """Device form over torch CUDA tensors: rays_soa is a (6, n) float32 tensor."""
+        n = rays_soa.shape[1]
+        _check(lib().cvx_intersect_nearest_device(
+            self._h, ctypes.c_void_p(rays_soa.data_ptr()), n, far, traversal, ctypes.c_void_p(t_out.data_ptr()),
+            ctypes.c_void_p(tri_out.data_ptr()), None if counters is None else ctypes.c_void_p(counters.data_ptr()),
+            None if stream is None else ctypes.c_void_p(stream)))
+
+    def __del__(self):
+        if getattr(self, "_h", None) and self._h.value and _LIB is not None:
+            _LIB.cvx_scene_destroy(self._h)
+            self._h = None
+
+
+class Renderer:
+    """renderer.rs:120-410 as whole-frame GPU calls."""
+
+    def __init__(self, scene, width, height, rng_order=RNG_GROUP, traversal=TRAVERSE_PACKET,
+                 mode=MODE_MEGAKERNEL, block_size=0, use_graph=0):
+        self.scene, self.width, self.height = scene, width, height
+        self.config = RenderConfig(rng_order, traversal, mode, block_size, use_graph)
+        out = ctypes.c_void_p()
+        _check(lib().cvx_renderer_create(scene._h, width, height, ctypes.byref(self.config), ctypes.byref(out)))
+        self._h = out
+        self.set_camera(scene.camera)
+
+    def set_camera(self, camera):
+        _check(lib().cvx_renderer_set_camera(self._h, ctypes.byref(camera._c)))
+
+    def render_frame_u8(self, frame_number, gbuffer=True):
+        rgba = np.empty((self.height, self.width), dtype=np.uint32)
+        gb = np.empty((self.height, self.width), dtype=np.uint32) if gbuffer else None
+        _check(lib().cvx_render_frame_u8(self._h, frame_number, _ptr(rgba), _ptr(gb)))
+        return rgba, gb
+
+    def accumulate_frame_f32(self, frame_number, gbuffer=False):
+        gb = np.empty((self.height, self.width), dtype=np.uint32) if gbuffer else None
+        _check(lib().cvx_accumulate_frame_f32(self._h, frame_number, _ptr(gb)))
+        return gb
+
+    def resolve_u8(self, num_samples):
+        rgba = np.empty((self.height, self.width), dtype=np.uint32)
+        _check(lib().cvx_resolve_u8(self._h, num_samples, _ptr(rgba)))
+        return rgba
+
+    def read_accumulator(self):
+        out = np.empty((self.height, self.width, 3), dtype=np.float32)
+        _check(lib().cvx_read_accumulator(self._h, _ptr(out)))
+        return out
+
+    def clear_accumulator(self):
+        _check(lib().cvx_clear_accumulator(self._h))
+
+    def read_frame_f32(self):
+        out = np.empty((self.height, self.width, 3), dtype=np.float32)
+        _check(lib().cvx_read_frame_f32(self._h, _ptr(out)))
+        return out
+
+    def stats(self):
+        rays, ms = ctypes.c_uint64(), ctypes.c_float()
+        _check(lib().cvx_renderer_stats(self._h, ctypes.byref(rays), ctypes.byref(ms)))
+        return rays.value, ms.value
+
+    def __del__(self):
+        if getattr(self, "_h", None) and self._h.value and _LIB is not None:
+            _LIB.cvx_renderer_destroy(self._h)
+            self._h = None

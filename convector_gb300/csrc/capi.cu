@@ -1,0 +1,414 @@
+// The device half of the C-ABI (include/convector_gpu.h): scene upload,
+// nearest-hit queries and frame rendering.
+#include <cuda_runtime.h>
+
+#include <cstring>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "internal.h"
+#include "kernels.h"
+#include "x86_approx_tables.h"
+
+using namespace cvx;
+
+namespace {
+
+const uint32_t kRcp32[2048] = CVX_RCP_TABLE_INIT;
+const uint32_t kRsqrt32[2048] = CVX_RSQRT_TABLE_INIT;
+
+std::mutex g_init_mu;
+std::vector<bool> g_tables_ready;
+
+int32_t cuda_fail(cudaError_t e, const char* what) {
+    return set_error(CVX_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define CK(call, what)                                \
+    do {                                              \
+        cudaError_t e_ = (call);                      \
+        if (e_ != cudaSuccess) return cuda_fail(e_, what); \
+    } while (0)
+
+// Uploads the approximation tables once per device.
+int32_t ensure_device(int* dev_out) {
+    int n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess || n == 0) return set_error(CVX_ERR_CUDA, "no CUDA device available");
+    int dev = 0;
+    CK(cudaGetDevice(&dev), "cudaGetDevice");
+    std::lock_guard<std::mutex> lk(g_init_mu);
+    if ((int)g_tables_ready.size() < n) g_tables_ready.resize(n, false);
+    if (!g_tables_ready[dev]) {
+        uint16_t r[2048], s[2048];
+        for (int i = 0; i < 2048; i++) {
+            r[i] = (uint16_t)(kRcp32[i] >> 11);
+            s[i] = (uint16_t)(kRsqrt32[i] >> 11);
+        }
+        CK(upload_tables(r, s), "upload approximation tables");
+        g_tables_ready[dev] = true;
+    }
+    *dev_out = dev;
+    return CVX_OK;
+}
+
+template <class T>
+int32_t dalloc(T** p, size_t count, const char* what) {
+    *p = nullptr;
+    if (count == 0) count = 1;
+    cudaError_t e = cudaMalloc((void**)p, count * sizeof(T));
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return set_error(e == cudaErrorMemoryAllocation ? CVX_ERR_CAPACITY : CVX_ERR_CUDA,
+                         std::string("cudaMalloc ") + what + ": " + cudaGetErrorString(e));
+    }
+    return CVX_OK;
+}
+
+}  // namespace
+
+struct cvx_scene {
+    int device = 0;
+    float4* d_nodes = nullptr;
+    float4* d_geom = nullptr;
+    TriShade* d_shade = nullptr;
+    float4* d_lights = nullptr;
+    uint32_t* d_err = nullptr;
+    uint32_t n_nodes = 0, n_tris = 0, n_lights = 0, depth = 0;
+    uint32_t general_pick = 1;
+    // scratch for the host-buffer query
+    float* d_rays = nullptr;
+    float* d_t = nullptr;
+    int32_t* d_tri = nullptr;
+    size_t scratch_n = 0;
+    cudaStream_t stream = nullptr;
+
+    DeviceScene view() const {
+        DeviceScene s;
+        s.nodes = d_nodes;
+        s.geom = d_geom;
+        s.shade = d_shade;
+        s.lights = d_lights;
+        s.n_nodes = n_nodes;
+        s.n_tris = n_tris;
+        s.n_lights = n_lights;
+        s.general_pick = general_pick;
+        return s;
+    }
+    ~cvx_scene() {
+        cudaFree(d_nodes);
+        cudaFree(d_geom);
+        cudaFree(d_shade);
+        cudaFree(d_lights);
+        cudaFree(d_err);
+        cudaFree(d_rays);
+        cudaFree(d_t);
+        cudaFree(d_tri);
+        if (stream) cudaStreamDestroy(stream);
+    }
+};
+
+struct cvx_renderer {
+    cvx_scene* scene = nullptr;
+    uint32_t w = 0, h = 0;
+    cvx_render_config cfg{};
+    DeviceCamera cam{};
+    uint32_t* d_rgba = nullptr;
+    uint32_t* d_gbuf = nullptr;
+    float* d_color = nullptr;
+    float* d_accum = nullptr;
+    unsigned long long* d_rays = nullptr;
+    uint32_t* d_err = nullptr;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    uint64_t last_rays = 0;
+    float last_ms = 0.0f;
+    ~cvx_renderer() {
+        cudaFree(d_rgba);
+        cudaFree(d_gbuf);
+        cudaFree(d_color);
+        cudaFree(d_accum);
+        cudaFree(d_rays);
+        cudaFree(d_err);
+        if (e0) cudaEventDestroy(e0);
+        if (e1) cudaEventDestroy(e1);
+        if (stream) cudaStreamDestroy(stream);
+    }
+};
+
+// Checks the tree and returns its depth (roots at depth 1).
+static int32_t validate_tree(const cvx_bvh_node* nodes, uint32_t n_nodes, uint32_t n_tris, uint32_t* depth_out) {
+    if (n_nodes < 2 || (n_nodes & 1u)) return set_error(CVX_ERR_INVALID, "node count must be even and at least 2");
+    std::vector<std::pair<uint32_t, uint32_t>> stack{{0u, 1u}, {1u, 1u}};
+    uint32_t depth = 0;
+    size_t visited = 0;
+    while (!stack.empty()) {
+        auto [i, dep] = stack.back();
+        stack.pop_back();
+        if (++visited > n_nodes) return set_error(CVX_ERR_INVALID, "BVH nodes form a cycle");
+        depth = dep > depth ? dep : depth;
+        const cvx_bvh_node& nd = nodes[i];
+        if (nd.len == 0) {
+            if ((nd.index & 1u) || nd.index + 1 >= n_nodes || nd.index < 2)
+                return set_error(CVX_ERR_INVALID, "internal node child index out of range");
+            stack.push_back({nd.index, dep + 1});
+            stack.push_back({nd.index + 1, dep + 1});
+        } else if ((uint64_t)nd.index + nd.len > n_tris) {
+            return set_error(CVX_ERR_INVALID, "leaf triangle range out of range");
+        }
+    }
+    *depth_out = depth;
+    return CVX_OK;
+}
+
+extern "C" {
+
+int32_t cvx_scene_create(const cvx_triangle* tris, uint32_t n_tris, const cvx_bvh_node* nodes, uint32_t n_nodes,
+                         cvx_scene** out) {
+    if (!tris || !nodes || !out || n_tris == 0) return set_error(CVX_ERR_INVALID, "null argument or empty scene");
+    uint32_t depth = 0;
+    int32_t st = validate_tree(nodes, n_nodes, n_tris, &depth);
+    if (st) return st;
+    if (depth + 2 > (uint32_t)kStackDepth)
+        return set_error(CVX_ERR_INVALID, "BVH deeper than the device traversal stack (" +
+                                              std::to_string(depth) + " levels)");
+    std::vector<uint32_t> ds;
+    for (uint32_t i = 0; i < n_tris; i++) {
+        if (((tris[i].material >> 26) & 7u) > 5u)
+            return set_error(CVX_ERR_INVALID, "glossiness index above 5 (material.rs:497-512 has six entries)");
+        if ((tris[i].material >> 30) & 1u) ds.push_back(i);  // scene.rs:117-122
+    }
+    int dev = 0;
+    st = ensure_device(&dev);
+    if (st) return st;
+    std::unique_ptr<cvx_scene> s(new cvx_scene());
+    s->device = dev;
+    s->n_nodes = n_nodes;
+    s->n_tris = n_tris;
+    s->n_lights = (uint32_t)ds.size();
+    s->depth = depth;
+    CK(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking), "cudaStreamCreate");
+    if ((st = dalloc(&s->d_nodes, (size_t)n_nodes * 2, "nodes"))) return st;
+    if ((st = dalloc(&s->d_geom, (size_t)n_tris * 3, "triangles"))) return st;
+    if ((st = dalloc(&s->d_shade, n_tris, "shading data"))) return st;
+    if ((st = dalloc(&s->d_lights, (size_t)s->n_lights * 5, "lights"))) return st;
+    if ((st = dalloc(&s->d_err, 1, "status"))) return st;
+    // Node pairs: q0 = lo0 hi0.x | q1 = hi0.yz lo1.xy | q2 = lo1.z hi1 | q3 = index/len x2
+    std::vector<float4> pairs((size_t)n_nodes / 2 * 4);
+    for (uint32_t p = 0; p < n_nodes / 2; p++) {
+        const cvx_bvh_node& a = nodes[2 * p];
+        const cvx_bvh_node& b = nodes[2 * p + 1];
+        float4* q = &pairs[4 * (size_t)p];
+        q[0] = make_float4(a.origin[0], a.origin[1], a.origin[2], a.far_[0]);
+        q[1] = make_float4(a.far_[1], a.far_[2], b.origin[0], b.origin[1]);
+        q[2] = make_float4(b.origin[2], b.far_[0], b.far_[1], b.far_[2]);
+        uint32_t w[4] = {a.index, a.len, b.index, b.len};
+        std::memcpy(&q[3], w, 16);
+    }
+    CK(cudaMemcpyAsync(s->d_nodes, pairs.data(), pairs.size() * sizeof(float4), cudaMemcpyHostToDevice, s->stream),
+       "upload nodes");
+    cvx_triangle* d_src = nullptr;
+    uint32_t* d_ds = nullptr;
+    if ((st = dalloc(&d_src, n_tris, "staging"))) return st;
+    if ((st = dalloc(&d_ds, ds.size(), "staging"))) {
+        cudaFree(d_src);
+        return st;
+    }
+    cudaError_t e = cudaMemcpyAsync(d_src, tris, (size_t)n_tris * sizeof(cvx_triangle), cudaMemcpyHostToDevice,
+                                    s->stream);
+    if (e == cudaSuccess && !ds.empty())
+        e = cudaMemcpyAsync(d_ds, ds.data(), ds.size() * 4, cudaMemcpyHostToDevice, s->stream);
+    if (e == cudaSuccess) e = launch_prep_geom(d_src, n_tris, s->d_geom, s->d_shade, s->stream);
+    if (e == cudaSuccess && !ds.empty()) e = launch_prep_lights(d_src, d_ds, s->n_lights, s->d_lights, s->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+    cudaFree(d_src);
+    cudaFree(d_ds);
+    if (e != cudaSuccess) return cuda_fail(e, "scene upload");
+    *out = s.release();
+    return CVX_OK;
+}
+
+int32_t cvx_scene_from_bvh(const cvx_bvh* bvh, cvx_scene** out) {
+    if (!bvh) return set_error(CVX_ERR_INVALID, "null bvh");
+    return cvx_scene_create(bvh->triangles.data(), (uint32_t)bvh->triangles.size(), bvh->nodes.data(),
+                            (uint32_t)bvh->nodes.size(), out);
+}
+
+uint32_t cvx_scene_num_direct_samples(const cvx_scene* s) { return s ? s->n_lights : 0u; }
+
+int32_t cvx_scene_set_light_pick(cvx_scene* s, uint32_t light_pick) {
+    if (!s) return set_error(CVX_ERR_INVALID, "null scene");
+    if (light_pick == 0 && s->n_lights != 8)
+        return set_error(CVX_ERR_INVALID, "the reference light pick (bits >> 29) needs exactly 8 direct-sample triangles");
+    s->general_pick = light_pick ? 1u : 0u;
+    return CVX_OK;
+}
+
+void cvx_scene_destroy(cvx_scene* s) { delete s; }
+
+int32_t cvx_intersect_nearest_device(cvx_scene* s, const float* rays, uint32_t n, float far_dist, uint32_t traversal,
+                                     float* t_out, int32_t* tri_out, uint32_t* counters, void* stream) {
+    if (!s || (!rays && n) || (!t_out && n) || (!tri_out && n)) return set_error(CVX_ERR_INVALID, "null argument");
+    if (traversal > 1) return set_error(CVX_ERR_INVALID, "unknown traversal variant");
+    if (n == 0) return CVX_OK;
+    cudaStream_t st = (cudaStream_t)stream;
+    CK(launch_intersect(s->view(), rays, n, far_dist, traversal == CVX_TRAVERSE_PACKET, t_out, tri_out, counters,
+                        s->d_err, 0, 0, st),
+       "intersect launch");
+    return CVX_OK;
+}
+
+int32_t cvx_intersect_nearest(cvx_scene* s, const float* ox, const float* oy, const float* oz, const float* dx,
+                              const float* dy, const float* dz, uint32_t n, float far_dist, uint32_t traversal,
+                              float* t_out, int32_t* tri_out) {
+    if (!s) return set_error(CVX_ERR_INVALID, "null scene");
+    if (n == 0) return CVX_OK;
+    if (!ox || !oy || !oz || !dx || !dy || !dz || !t_out || !tri_out) return set_error(CVX_ERR_INVALID, "null buffer");
+    if (traversal > 1) return set_error(CVX_ERR_INVALID, "unknown traversal variant");
+    int32_t st = 0;
+    if (s->scratch_n < n) {
+        cudaFree(s->d_rays);
+        cudaFree(s->d_t);
+        cudaFree(s->d_tri);
+        s->d_rays = nullptr;
+        s->d_t = nullptr;
+        s->d_tri = nullptr;
+        s->scratch_n = 0;
+        if ((st = dalloc(&s->d_rays, (size_t)n * 6, "ray buffer"))) return st;
+        if ((st = dalloc(&s->d_t, n, "hit buffer"))) return st;
+        if ((st = dalloc(&s->d_tri, n, "hit buffer"))) return st;
+        s->scratch_n = n;
+    }
+    const float* src[6] = {ox, oy, oz, dx, dy, dz};
+    for (int k = 0; k < 6; k++)
+        CK(cudaMemcpyAsync(s->d_rays + (size_t)k * n, src[k], (size_t)n * 4, cudaMemcpyHostToDevice, s->stream),
+           "copy rays");
+    CK(cudaMemsetAsync(s->d_err, 0, 4, s->stream), "reset status");
+    CK(launch_intersect(s->view(), s->d_rays, n, far_dist, traversal == CVX_TRAVERSE_PACKET, s->d_t, s->d_tri,
+                        nullptr, s->d_err, 0, 0, s->stream),
+       "intersect launch");
+    CK(cudaMemcpyAsync(t_out, s->d_t, (size_t)n * 4, cudaMemcpyDeviceToHost, s->stream), "copy distances");
+    CK(cudaMemcpyAsync(tri_out, s->d_tri, (size_t)n * 4, cudaMemcpyDeviceToHost, s->stream), "copy indices");
+    uint32_t err = 0;
+    CK(cudaMemcpyAsync(&err, s->d_err, 4, cudaMemcpyDeviceToHost, s->stream), "copy status");
+    CK(cudaStreamSynchronize(s->stream), "intersect");
+    if (err) return set_error(CVX_ERR_DEVICE, "traversal stack overflow reported by the kernel");
+    return CVX_OK;
+}
+
+int32_t cvx_renderer_create(cvx_scene* scene, uint32_t w, uint32_t h, const cvx_render_config* cfg,
+                            cvx_renderer** out) {
+    if (!scene || !out) return set_error(CVX_ERR_INVALID, "null argument");
+    if (w == 0 || h == 0 || w > 16384 || h > 16384) return set_error(CVX_ERR_INVALID, "frame size out of range");
+    if (scene->n_lights == 0)
+        return set_error(CVX_ERR_INVALID, "rendering needs at least one direct-sample triangle (scene.rs:143-161)");
+    cvx_render_config c{};
+    if (cfg) c = *cfg;
+    if (c.rng_order > 1 || c.traversal > 1 || c.mode > 1 || (c.block_size % 32) || c.block_size > 1024)
+        return set_error(CVX_ERR_INVALID, "bad render configuration");
+    std::unique_ptr<cvx_renderer> r(new cvx_renderer());
+    r->scene = scene;
+    r->w = w;
+    r->h = h;
+    r->cfg = c;
+    cvx_camera cam;
+    cvx_camera_default(&cam);
+    std::memcpy(&r->cam, &cam, sizeof cam);
+    size_t npx = (size_t)w * h;
+    int32_t st = 0;
+    if ((st = dalloc(&r->d_rgba, npx, "colour buffer"))) return st;
+    if ((st = dalloc(&r->d_gbuf, npx, "gbuffer"))) return st;
+    if ((st = dalloc(&r->d_color, npx * 3, "frame buffer"))) return st;
+    if ((st = dalloc(&r->d_accum, npx * 3, "accumulator"))) return st;
+    if ((st = dalloc(&r->d_rays, 1, "counters"))) return st;
+    if ((st = dalloc(&r->d_err, 1, "status"))) return st;
+    CK(cudaStreamCreateWithFlags(&r->stream, cudaStreamNonBlocking), "cudaStreamCreate");
+    CK(cudaEventCreate(&r->e0), "cudaEventCreate");
+    CK(cudaEventCreate(&r->e1), "cudaEventCreate");
+    CK(cudaMemsetAsync(r->d_accum, 0, npx * 12, r->stream), "clear accumulator");
+    CK(cudaStreamSynchronize(r->stream), "renderer init");
+    *out = r.release();
+    return CVX_OK;
+}
+
+void cvx_renderer_destroy(cvx_renderer* r) { delete r; }
+
+int32_t cvx_renderer_set_camera(cvx_renderer* r, const cvx_camera* cam) {
+    if (!r || !cam) return set_error(CVX_ERR_INVALID, "null argument");
+    static_assert(sizeof(DeviceCamera) == sizeof(cvx_camera), "camera layout");
+    std::memcpy(&r->cam, cam, sizeof *cam);
+    return CVX_OK;
+}
+
+static int32_t run_frame(cvx_renderer* r, uint32_t frame, bool accumulate, uint32_t* rgba, uint32_t* gbuf) {
+    size_t npx = (size_t)r->w * r->h;
+    CK(cudaMemsetAsync(r->d_rays, 0, 8, r->stream), "reset counters");
+    CK(cudaMemsetAsync(r->d_err, 0, 4, r->stream), "reset status");
+    CK(cudaEventRecord(r->e0, r->stream), "event");
+    CK(launch_render(r->scene->view(), r->cam, r->w, r->h, frame, r->cfg.traversal == CVX_TRAVERSE_PACKET,
+                     r->cfg.rng_order == CVX_RNG_PATCH, accumulate ? nullptr : r->d_rgba, r->d_gbuf, r->d_color,
+                     accumulate ? r->d_accum : nullptr, r->d_rays, r->d_err, r->cfg.block_size, r->stream),
+       "render launch");
+    CK(cudaEventRecord(r->e1, r->stream), "event");
+    if (rgba) CK(cudaMemcpyAsync(rgba, r->d_rgba, npx * 4, cudaMemcpyDeviceToHost, r->stream), "copy colour");
+    if (gbuf) CK(cudaMemcpyAsync(gbuf, r->d_gbuf, npx * 4, cudaMemcpyDeviceToHost, r->stream), "copy gbuffer");
+    unsigned long long rays = 0;
+    uint32_t err = 0;
+    CK(cudaMemcpyAsync(&rays, r->d_rays, 8, cudaMemcpyDeviceToHost, r->stream), "copy counters");
+    CK(cudaMemcpyAsync(&err, r->d_err, 4, cudaMemcpyDeviceToHost, r->stream), "copy status");
+    CK(cudaStreamSynchronize(r->stream), "render");
+    cudaEventElapsedTime(&r->last_ms, r->e0, r->e1);
+    r->last_rays = rays;
+    if (err) return set_error(CVX_ERR_DEVICE, "traversal stack overflow reported by the kernel");
+    return CVX_OK;
+}
+
+int32_t cvx_render_frame_u8(cvx_renderer* r, uint32_t frame, uint32_t* rgba, uint32_t* gbuffer) {
+    if (!r) return set_error(CVX_ERR_INVALID, "null renderer");
+    return run_frame(r, frame, false, rgba, gbuffer);
+}
+
+int32_t cvx_accumulate_frame_f32(cvx_renderer* r, uint32_t frame, uint32_t* gbuffer) {
+    if (!r) return set_error(CVX_ERR_INVALID, "null renderer");
+    return run_frame(r, frame, true, nullptr, gbuffer);
+}
+
+int32_t cvx_resolve_u8(cvx_renderer* r, uint32_t n, uint32_t* rgba) {
+    if (!r || !rgba) return set_error(CVX_ERR_INVALID, "null argument");
+    if (n == 0) return set_error(CVX_ERR_INVALID, "number of samples must be positive");
+    size_t npx = (size_t)r->w * r->h;
+    CK(launch_resolve(r->d_accum, (uint32_t)npx, 1.0f / (float)n, r->d_rgba, r->stream), "resolve launch");
+    CK(cudaMemcpyAsync(rgba, r->d_rgba, npx * 4, cudaMemcpyDeviceToHost, r->stream), "copy colour");
+    CK(cudaStreamSynchronize(r->stream), "resolve");
+    return CVX_OK;
+}
+
+int32_t cvx_read_accumulator(cvx_renderer* r, float* out) {
+    if (!r || !out) return set_error(CVX_ERR_INVALID, "null argument");
+    CK(cudaMemcpy(out, r->d_accum, (size_t)r->w * r->h * 12, cudaMemcpyDeviceToHost), "copy accumulator");
+    return CVX_OK;
+}
+
+int32_t cvx_clear_accumulator(cvx_renderer* r) {
+    if (!r) return set_error(CVX_ERR_INVALID, "null renderer");
+    CK(cudaMemsetAsync(r->d_accum, 0, (size_t)r->w * r->h * 12, r->stream), "clear accumulator");
+    CK(cudaStreamSynchronize(r->stream), "clear accumulator");
+    return CVX_OK;
+}
+
+int32_t cvx_read_frame_f32(cvx_renderer* r, float* out) {
+    if (!r || !out) return set_error(CVX_ERR_INVALID, "null argument");
+    CK(cudaMemcpy(out, r->d_color, (size_t)r->w * r->h * 12, cudaMemcpyDeviceToHost), "copy frame");
+    return CVX_OK;
+}
+
+int32_t cvx_renderer_stats(cvx_renderer* r, uint64_t* rays, float* ms) {
+    if (!r) return set_error(CVX_ERR_INVALID, "null renderer");
+    if (rays) *rays = r->last_rays;
+    if (ms) *ms = r->last_ms;
+    return CVX_OK;
+}
+
+}  // extern "C"

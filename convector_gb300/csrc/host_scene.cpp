@@ -1,0 +1,557 @@
+// Host side of the boundary: OBJ loading (wavefront.rs), the BVH build
+// (bvh.rs) and the camera setters (scene.rs), restated in C++. The BVH build
+// is the reference's algorithm step for step, so the device sees the same
+// node order and triangle order as the reference's traversal. Compiled with
+// -ffp-contract=off so that every float operation rounds where the Rust
+// original rounds.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <future>
+#include <memory>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "internal.h"
+
+namespace cvx {
+
+static thread_local std::string g_last_error;
+static thread_local int32_t g_last_status = CVX_OK;
+
+int32_t set_error(int32_t status, const std::string& msg) {
+    g_last_status = status;
+    g_last_error = msg;
+    return status;
+}
+
+// ---------------------------------------------------------------------------
+// Scalar vector helpers (SVector3, vector3.rs:39-143)
+
+struct S3 {
+    float x, y, z;
+};
+static inline S3 s3(const float* p) { return S3{p[0], p[1], p[2]}; }
+static inline S3 operator-(S3 a, S3 b) { return S3{a.x - b.x, a.y - b.y, a.z - b.z}; }
+static inline S3 operator+(S3 a, S3 b) { return S3{a.x + b.x, a.y + b.y, a.z + b.z}; }
+static inline S3 operator*(S3 a, float k) { return S3{a.x * k, a.y * k, a.z * k}; }
+// SVector3::cross is cross_fma with `mul_add(b, -c)` (vector3.rs:63-70).
+static inline S3 scross(S3 a, S3 b) {
+    return S3{std::fma(a.y, b.z, -(a.z * b.y)), std::fma(a.z, b.x, -(a.x * b.z)), std::fma(a.x, b.y, -(a.y * b.x))};
+}
+// SVector3::dot is dot_fma (vector3.rs:86-98).
+static inline float sdot(S3 a, S3 b) { return std::fma(a.x, b.x, std::fma(a.y, b.y, a.z * b.z)); }
+// f32::min / f32::max (IEEE minNum / maxNum). On equal operands (+0 / -0) the
+// x86 lowering of llvm.minnum / maxnum returns the first operand.
+static inline float fmin_rs(float a, float b) { return a != a ? b : (b < a ? b : a); }
+static inline float fmax_rs(float a, float b) { return a != a ? b : (b > a ? b : a); }
+static inline S3 smin(S3 a, S3 b) { return S3{fmin_rs(a.x, b.x), fmin_rs(a.y, b.y), fmin_rs(a.z, b.z)}; }
+static inline S3 smax(S3 a, S3 b) { return S3{fmax_rs(a.x, b.x), fmax_rs(a.y, b.y), fmax_rs(a.z, b.z)}; }
+static inline float coord(S3 v, int axis) { return axis == 0 ? v.x : axis == 1 ? v.y : v.z; }
+
+// ---------------------------------------------------------------------------
+// OBJ loading (wavefront.rs:83-152)
+
+static bool parse_f32(const std::string& tok, float* out) {
+    if (tok.empty()) return false;
+    if (tok.find("0x") != std::string::npos || tok.find("0X") != std::string::npos) return false;
+    char* end = nullptr;
+    float v = std::strtof(tok.c_str(), &end);
+    if (end != tok.c_str() + tok.size()) return false;
+    *out = v;
+    return true;
+}
+
+static bool parse_u32(const std::string& tok, uint32_t* out) {
+    size_t i = 0;
+    if (i < tok.size() && tok[i] == '+') i++;
+    if (i == tok.size()) return false;
+    uint64_t v = 0;
+    for (; i < tok.size(); i++) {
+        if (tok[i] < '0' || tok[i] > '9') return false;
+        v = v * 10 + (uint64_t)(tok[i] - '0');
+        if (v > 0xffffffffull) return false;
+    }
+    *out = (uint32_t)v;
+    return true;
+}
+
+// wavefront.rs:49-55: "v" or "v/t" (further parts parsed and ignored).
+static bool parse_vertex_index(const std::string& tok, uint32_t* v, int64_t* t) {
+    std::vector<std::string> parts;
+    size_t start = 0;
+    for (;;) {
+        size_t p = tok.find('/', start);
+        parts.push_back(tok.substr(start, p == std::string::npos ? std::string::npos : p - start));
+        if (p == std::string::npos) break;
+        start = p + 1;
+    }
+    uint32_t vi = 0, ti = 0;
+    for (size_t k = 0; k < parts.size(); k++) {
+        uint32_t x;
+        if (!parse_u32(parts[k], &x) || x == 0) return false;
+        if (k == 0) vi = x;
+        if (k == 1) ti = x;
+    }
+    *v = vi - 1;
+    *t = parts.size() >= 2 ? (int64_t)ti - 1 : -1;
+    return true;
+}
+
+static int32_t parse_obj(const char* text, size_t len, const char* const* names, const uint32_t* materials,
+                         uint32_t n_materials, cvx_mesh** out) {
+    std::unique_ptr<cvx_mesh> mesh(new cvx_mesh());
+    uint32_t material = 0x00ffffffu;  // SMaterial::white() (material.rs:93-95)
+    size_t pos = 0;
+    uint32_t line_nr = 0;
+    std::vector<std::string> toks;
+    while (pos < len) {
+        size_t eol = pos;
+        while (eol < len && text[eol] != '\n') eol++;
+        size_t end = eol;
+        if (end > pos && text[end - 1] == '\r') end--;
+        line_nr++;
+        toks.clear();
+        size_t i = pos;
+        while (i < end) {
+            while (i < end && std::isspace((unsigned char)text[i])) i++;
+            size_t j = i;
+            while (j < end && !std::isspace((unsigned char)text[j])) j++;
+            if (j > i) toks.emplace_back(text + i, j - i);
+            i = j;
+        }
+        pos = eol + 1;
+        if (toks.empty()) continue;
+        const std::string& kw = toks[0];
+        char where[64];
+        std::snprintf(where, sizeof where, " (line %u)", line_nr);
+        if (kw == "v") {
+            float c[3];
+            if (toks.size() < 4) return set_error(CVX_ERR_PARSE, std::string("missing vertex coordinate") + where);
+            for (int k = 0; k < 3; k++)
+                if (!parse_f32(toks[1 + k], &c[k]))
+                    return set_error(CVX_ERR_PARSE, std::string("bad vertex coordinate") + where);
+            mesh->vertices.insert(mesh->vertices.end(), c, c + 3);
+        } else if (kw == "vt") {
+            float c[2];
+            if (toks.size() < 3) return set_error(CVX_ERR_PARSE, std::string("missing texture coordinate") + where);
+            for (int k = 0; k < 2; k++)
+                if (!parse_f32(toks[1 + k], &c[k]))
+                    return set_error(CVX_ERR_PARSE, std::string("bad texture coordinate") + where);
+            mesh->tex_coords.insert(mesh->tex_coords.end(), c, c + 2);
+        } else if (kw == "usemtl") {
+            if (toks.size() < 2) return set_error(CVX_ERR_PARSE, std::string("missing material name") + where);
+            bool found = false;
+            for (uint32_t k = 0; k < n_materials; k++)
+                if (toks[1] == names[k]) {
+                    material = materials[k];
+                    found = true;
+                }
+            if (!found)
+                return set_error(CVX_ERR_PARSE, "material '" + toks[1] + "' not present in material dictionary" + where);
+        } else if (kw == "f") {
+            if (toks.size() < 4) return set_error(CVX_ERR_PARSE, std::string("missing triangle index") + where);
+            std::vector<uint32_t> vi(toks.size() - 1);
+            std::vector<int64_t> ti(toks.size() - 1);
+            for (size_t k = 1; k < toks.size(); k++)
+                if (!parse_vertex_index(toks[k], &vi[k - 1], &ti[k - 1]))
+                    return set_error(CVX_ERR_PARSE, "bad face index '" + toks[k] + "'" + where);
+            size_t nv = mesh->vertices.size() / 3;
+            // Fan triangulation of convex n-gons (wavefront.rs:132-139).
+            for (size_t k = 2; k < vi.size(); k++) {
+                uint32_t a = vi[0], b = vi[k - 1], c = vi[k];
+                if (a >= nv || b >= nv || c >= nv)
+                    return set_error(CVX_ERR_PARSE, std::string("vertex index out of range") + where);
+                // wavefront.rs:30-46
+                S3 v0 = s3(&mesh->vertices[3 * a]), v1 = s3(&mesh->vertices[3 * b]), v2 = s3(&mesh->vertices[3 * c]);
+                S3 e1 = v0 - v2, e2 = v1 - v0;
+                S3 cr = scross(e1, e2);
+                if (sdot(cr, cr) == 0.0f)
+                    return set_error(CVX_ERR_DEGENERATE, std::string("encountered degenerate triangle") + where);
+                MeshTri t;
+                t.v[0] = a;
+                t.v[1] = b;
+                t.v[2] = c;
+                bool has_t = ti[0] >= 0 && ti[k - 1] >= 0 && ti[k] >= 0;
+                t.t[0] = has_t ? ti[0] : -1;
+                t.t[1] = has_t ? ti[k - 1] : -1;
+                t.t[2] = has_t ? ti[k] : -1;
+                t.material = material;
+                mesh->triangles.push_back(t);
+            }
+        }
+    }
+    *out = mesh.release();
+    return CVX_OK;
+}
+
+// ---------------------------------------------------------------------------
+// BVH build (bvh.rs:44-545)
+
+struct Aabb {
+    S3 lo, hi;
+};
+static inline Aabb enclose(const Aabb& a, const Aabb& b) { return Aabb{smin(a.lo, b.lo), smax(a.hi, b.hi)}; }
+// aabb.rs:97-103
+static inline float area(const Aabb& a) {
+    S3 s = a.hi - a.lo;
+    float x = s.y * s.z, y = s.z * s.x, z = s.x * s.y;
+    return 2.0f * (x + y + z);
+}
+
+struct TriRef {  // bvh.rs:44-50
+    Aabb aabb;
+    S3 bc;
+    uint32_t index;
+};
+
+struct Interim {  // bvh.rs:52-62
+    Aabb outer, inner;
+    std::vector<Interim> children;
+    std::vector<TriRef> tris;
+};
+
+static Interim from_refs(std::vector<TriRef>&& refs) {  // bvh.rs:125-132
+    Interim n;
+    n.outer = refs[0].aabb;
+    n.inner = Aabb{refs[0].bc, refs[0].bc};
+    for (size_t i = 1; i < refs.size(); i++) {
+        n.outer = enclose(n.outer, refs[i].aabb);
+        n.inner.lo = smin(n.inner.lo, refs[i].bc);
+        n.inner.hi = smax(n.inner.hi, refs[i].bc);
+    }
+    n.tris = std::move(refs);
+    return n;
+}
+
+struct Bin {  // bvh.rs:64-121
+    std::vector<const TriRef*> tris;
+    Aabb aabb;
+    void push(const TriRef* t) {
+        aabb = tris.empty() ? t->aabb : enclose(aabb, t->aabb);
+        tris.push_back(t);
+    }
+    void clear() { tris.clear(); }
+};
+
+// TreeSurfaceAreaHeuristic (bvh.rs:452-474) with the constants of bvh.rs:500-504.
+static inline float tsah_aabb_cost(const Aabb& parent, const Aabb& box, size_t num_tris) {
+    const float aabb_cost = 40.0f, tri_cost = 120.0f, p = 0.8f;
+    float ac_ap = area(box) / area(parent);
+    float n = (float)num_tris;
+    float m = std::log2(n);
+    float aabb_term = 1.0f + ac_ap * (2.0f * p - n * std::pow(p, m)) / (p - 2.0f * p * p);
+    float tri_term = n * std::pow(p, m - 1.0f) * ac_ap;
+    return aabb_term * aabb_cost + tri_term * tri_cost;
+}
+static inline float tsah_tris_cost(size_t n) { return (float)n * 120.0f; }
+
+static void bin_uniform(const Interim& node, std::vector<Bin>& bins, int axis) {  // bvh.rs:176-201
+    std::vector<const TriRef*> ptrs;
+    ptrs.reserve(node.tris.size());
+    for (const TriRef& t : node.tris) ptrs.push_back(&t);
+    std::stable_sort(ptrs.begin(), ptrs.end(),
+                     [axis](const TriRef* a, const TriRef* b) { return coord(a->bc, axis) < coord(b->bc, axis); });
+    size_t per = (ptrs.size() + bins.size() - 1) / bins.size();
+    if (per == 0) per = 1;
+    size_t b = 0;
+    for (size_t i = 0; i < ptrs.size(); i += per, b++)
+        for (size_t k = i; k < std::min(i + per, ptrs.size()); k++) bins[b].push(ptrs[k]);
+}
+
+static void bin_tris(const Interim& node, std::vector<Bin>& bins, int axis) {  // bvh.rs:142-171
+    size_t n = node.tris.size();
+    if (n <= bins.size() / 2) return bin_uniform(node, bins, axis);
+    float mn = coord(node.inner.lo, axis);
+    float size = coord(node.inner.hi, axis) - mn;
+    for (const TriRef& t : node.tris) {
+        float f = std::floor((float)bins.size() * (coord(t.bc, axis) - mn) / size);
+        // `as usize`: NaN and negative values saturate to 0.
+        size_t idx = (f != f || f <= 0.0f) ? 0 : (f >= 1.8446744e19f ? SIZE_MAX : (size_t)f);
+        if (idx >= bins.size()) idx = bins.size() - 1;
+        bins[idx].push(&t);
+        if (bins[idx].tris.size() > n / 8 && n > bins.size()) {
+            for (Bin& b : bins) b.clear();
+            return bin_uniform(node, bins, axis);
+        }
+    }
+}
+
+static bool enclose_bins(const std::vector<Bin>& bins, size_t from, size_t to, Aabb* out, size_t* count) {
+    bool any = false;
+    size_t c = 0;
+    for (size_t i = from; i < to; i++) {
+        if (bins[i].tris.empty()) continue;
+        *out = any ? enclose(*out, bins[i].aabb) : bins[i].aabb;
+        any = true;
+        c += bins[i].tris.size();
+    }
+    *count = c;
+    return any;
+}
+
+// bvh.rs:218-261
+static float cheapest_split(const Interim& node, const std::vector<Bin>& bins, size_t* at) {
+    size_t first = 0, last = 0;
+    for (size_t i = 0; i < bins.size(); i++)
+        if (!bins[i].tris.empty()) {
+            first = i + 1;
+            break;
+        }
+    for (size_t i = bins.size(); i-- > 0;)
+        if (!bins[i].tris.empty()) {
+            last = i + 1;
+            break;
+        }
+    float best = 0.0f;
+    bool is_first = true;
+    for (size_t i = first; i < last; i++) {
+        Aabb la, ra;
+        size_t lc, rc;
+        enclose_bins(bins, 0, i, &la, &lc);
+        enclose_bins(bins, i, bins.size(), &ra, &rc);
+        float cost = tsah_aabb_cost(node.outer, la, lc) + tsah_aabb_cost(node.outer, ra, rc);
+        if (cost < best || is_first) {
+            best = cost;
+            *at = i;
+            is_first = false;
+        }
+    }
+    return best;
+}
+
+// bvh.rs:265-322
+static void split(Interim& node) {
+    if (node.tris.size() <= 1) return;
+    std::vector<Bin> bins(64);
+    std::vector<TriRef> best_l, best_r;
+    float best_cost = 0.0f;
+    bool is_first = true;
+    for (int axis = 0; axis < 3; axis++) {
+        bin_tris(node, bins, axis);
+        size_t nonempty = 0;
+        for (const Bin& b : bins) nonempty += !b.tris.empty();
+        if (nonempty > 1) {
+            size_t at = 0;
+            float cost = cheapest_split(node, bins, &at);
+            if (cost < best_cost || is_first) {
+                best_l.clear();
+                best_r.clear();
+                for (size_t i = 0; i < bins.size(); i++)
+                    for (const TriRef* t : bins[i].tris) (i < at ? best_l : best_r).push_back(*t);
+                best_cost = cost;
+                is_first = false;
+            }
+        }
+        for (Bin& b : bins) b.clear();
+    }
+    if (is_first) return;  // the reference asserts here; all barycentres coincide
+    if (tsah_tris_cost(node.tris.size()) < best_cost) return;
+    node.children.push_back(from_refs(std::move(best_l)));
+    node.children.push_back(from_refs(std::move(best_r)));
+    node.tris.clear();
+    node.tris.shrink_to_fit();
+}
+
+// bvh.rs:325-356. Subtrees are built concurrently, as with rayon::join; the
+// result does not depend on the schedule.
+static void split_recursive(Interim& node, int par_depth) {
+    split(node);
+    if (node.children.empty()) return;
+    if (area(node.children[0].outer) > area(node.children[1].outer)) std::swap(node.children[0], node.children[1]);
+    size_t n = node.children[0].tris.size() + node.children[1].tris.size();
+    if (par_depth > 0 && n > 20000) {
+        auto fut = std::async(std::launch::async, [&]() { split_recursive(node.children[0], par_depth - 1); });
+        split_recursive(node.children[1], par_depth - 1);
+        fut.get();
+    } else {
+        split_recursive(node.children[0], 0);
+        split_recursive(node.children[1], 0);
+    }
+}
+
+static void count(const Interim& n, size_t* nodes, size_t* leaves, size_t* tris) {
+    (*nodes)++;
+    if (n.children.empty()) (*leaves)++;
+    *tris += n.tris.size();
+    for (const Interim& c : n.children) count(c, nodes, leaves, tris);
+}
+static float summed_area_ratio(const Interim& n) {  // bvh.rs:380-385
+    float child_contrib = 0.0f;
+    for (const Interim& c : n.children) child_contrib += summed_area_ratio(c);
+    float self_area = area(n.outer);
+    float child_sum = 0.0f;
+    for (const Interim& c : n.children) child_sum += area(c.outer) / self_area;
+    return child_sum + child_contrib;
+}
+
+// bvh.rs:389-428
+static void crystallize(const Interim& n, const std::vector<cvx_triangle>& src, cvx_bvh& out, size_t into,
+                        uint32_t depth) {
+    cvx_bvh_node& nd = out.nodes[into];
+    nd.origin[0] = n.outer.lo.x;
+    nd.origin[1] = n.outer.lo.y;
+    nd.origin[2] = n.outer.lo.z;
+    nd.far_[0] = n.outer.hi.x;
+    nd.far_[1] = n.outer.hi.y;
+    nd.far_[2] = n.outer.hi.z;
+    out.depth = std::max(out.depth, depth);
+    if (n.tris.empty()) {
+        size_t child = out.nodes.size();
+        out.nodes.push_back(cvx_bvh_node{});
+        out.nodes.push_back(cvx_bvh_node{});
+        crystallize(n.children[0], src, out, child, depth + 1);
+        crystallize(n.children[1], src, out, child + 1, depth + 1);
+        out.nodes[into].index = (uint32_t)child;
+        out.nodes[into].len = 0;
+    } else {
+        out.nodes[into].index = (uint32_t)out.triangles.size();
+        out.nodes[into].len = (uint32_t)n.tris.size();
+        for (const TriRef& t : n.tris) {
+            out.triangles.push_back(src[t.index]);
+            out.source_index.push_back(t.index);
+        }
+    }
+}
+
+static int32_t build(const cvx_triangle* tris, uint32_t n, cvx_bvh** out) {
+    if (n == 0) return set_error(CVX_ERR_INVALID, "cannot build a BVH of zero triangles");
+    std::vector<cvx_triangle> src(tris, tris + n);
+    std::vector<TriRef> refs(n);
+    const float third = 1.0f / 3.0f;  // 3.0f32.recip()
+    for (uint32_t i = 0; i < n; i++) {
+        S3 v0 = s3(tris[i].v0), v1 = s3(tris[i].v1), v2 = s3(tris[i].v2);
+        refs[i].aabb = Aabb{smin(smin(v0, v1), v2), smax(smax(v0, v1), v2)};
+        refs[i].bc = (v0 + v1 + v2) * third;
+        refs[i].index = i;
+    }
+    Interim root = from_refs(std::move(refs));
+    split_recursive(root, 4);
+    if (root.children.size() != 2)
+        return set_error(CVX_ERR_INVALID,
+                         "the BVH root did not split: the reference needs at least two root nodes (bvh.rs:509-512)");
+    std::unique_ptr<cvx_bvh> bvh(new cvx_bvh());
+    size_t num_nodes = 0, num_leaves = 0, num_tris = 0;
+    count(root, &num_nodes, &num_leaves, &num_tris);
+    bvh->nodes.reserve(num_nodes);
+    bvh->triangles.reserve(num_tris);
+    bvh->nodes.push_back(cvx_bvh_node{});
+    bvh->nodes.push_back(cvx_bvh_node{});
+    crystallize(root.children[0], src, *bvh, 0, 1);
+    crystallize(root.children[1], src, *bvh, 1, 1);
+    bvh->avg_area_ratio = summed_area_ratio(root) / (float)num_nodes;
+    bvh->avg_tris_per_leaf = (float)num_tris / (float)num_leaves;
+    *out = bvh.release();
+    return CVX_OK;
+}
+
+}  // namespace cvx
+
+using namespace cvx;
+
+extern "C" {
+
+int32_t cvx_last_error(char* buf, size_t len) {
+    if (buf && len) {
+        std::strncpy(buf, g_last_error.c_str(), len - 1);
+        buf[len - 1] = '\0';
+    }
+    return g_last_status;
+}
+
+int32_t cvx_mesh_parse_obj(const char* text, size_t len, const char* const* names, const uint32_t* materials,
+                           uint32_t n_materials, cvx_mesh** out) {
+    if (!out || (!text && len)) return set_error(CVX_ERR_INVALID, "null argument");
+    return parse_obj(text, len, names, materials, n_materials, out);
+}
+
+int32_t cvx_mesh_load_obj(const char* path, const char* const* names, const uint32_t* materials,
+                          uint32_t n_materials, cvx_mesh** out) {
+    if (!path || !out) return set_error(CVX_ERR_INVALID, "null argument");
+    std::ifstream f(path, std::ios::binary);
+    if (!f) return set_error(CVX_ERR_IO, std::string("failed to open file ") + path);
+    std::stringstream ss;
+    ss << f.rdbuf();
+    std::string s = ss.str();
+    return parse_obj(s.data(), s.size(), names, materials, n_materials, out);
+}
+
+uint32_t cvx_mesh_num_triangles(const cvx_mesh* m) { return m ? (uint32_t)m->triangles.size() : 0u; }
+void cvx_mesh_destroy(cvx_mesh* m) { delete m; }
+
+int32_t cvx_bvh_from_meshes(const cvx_mesh* const* meshes, uint32_t n_meshes, cvx_bvh** out) {
+    if (!out || (!meshes && n_meshes)) return set_error(CVX_ERR_INVALID, "null argument");
+    std::vector<cvx_triangle> tris;
+    for (uint32_t m = 0; m < n_meshes; m++) {
+        const cvx_mesh& mesh = *meshes[m];
+        size_t ntc = mesh.tex_coords.size() / 2;
+        for (const MeshTri& t : mesh.triangles) {
+            cvx_triangle tr;
+            std::memset(&tr, 0, sizeof tr);
+            std::memcpy(tr.v0, &mesh.vertices[3 * t.v[0]], 12);
+            std::memcpy(tr.v1, &mesh.vertices[3 * t.v[1]], 12);
+            std::memcpy(tr.v2, &mesh.vertices[3 * t.v[2]], 12);
+            if (t.t[0] >= 0) {
+                for (int k = 0; k < 3; k++)
+                    if ((size_t)t.t[k] >= ntc) return set_error(CVX_ERR_PARSE, "texture coordinate index out of range");
+                std::memcpy(tr.uv0, &mesh.tex_coords[2 * t.t[0]], 8);
+                std::memcpy(tr.uv1, &mesh.tex_coords[2 * t.t[1]], 8);
+                std::memcpy(tr.uv2, &mesh.tex_coords[2 * t.t[2]], 8);
+            }
+            tr.material = t.material;
+            tris.push_back(tr);
+        }
+    }
+    return build(tris.data(), (uint32_t)tris.size(), out);
+}
+
+int32_t cvx_bvh_build(const cvx_triangle* triangles, uint32_t n, cvx_bvh** out) {
+    if (!out || (!triangles && n)) return set_error(CVX_ERR_INVALID, "null argument");
+    return build(triangles, n, out);
+}
+
+uint32_t cvx_bvh_num_nodes(const cvx_bvh* b) { return b ? (uint32_t)b->nodes.size() : 0u; }
+uint32_t cvx_bvh_num_triangles(const cvx_bvh* b) { return b ? (uint32_t)b->triangles.size() : 0u; }
+void cvx_bvh_copy_nodes(const cvx_bvh* b, cvx_bvh_node* out) {
+    std::memcpy(out, b->nodes.data(), b->nodes.size() * sizeof(cvx_bvh_node));
+}
+void cvx_bvh_copy_triangles(const cvx_bvh* b, cvx_triangle* out) {
+    std::memcpy(out, b->triangles.data(), b->triangles.size() * sizeof(cvx_triangle));
+}
+void cvx_bvh_copy_source_index(const cvx_bvh* b, uint32_t* out) {
+    std::memcpy(out, b->source_index.data(), b->source_index.size() * sizeof(uint32_t));
+}
+void cvx_bvh_stats(const cvx_bvh* b, float* avg_tris_per_leaf, float* avg_area_ratio, uint32_t* depth) {
+    if (avg_tris_per_leaf) *avg_tris_per_leaf = b->avg_tris_per_leaf;
+    if (avg_area_ratio) *avg_area_ratio = b->avg_area_ratio;
+    if (depth) *depth = b->depth;
+}
+void cvx_bvh_destroy(cvx_bvh* b) { delete b; }
+
+// scene.rs:34-42
+void cvx_camera_default(cvx_camera* c) {
+    std::memset(c, 0, sizeof *c);
+    c->orientation[0] = 1.0f;
+    c->screen_distance = 1.0f / std::sin(3.14159265358979323846f / 5.0f);
+}
+// scene.rs:66-74
+void cvx_camera_set_rotation(cvx_camera* c, float radians, float delta) {
+    float x = std::cos(radians * 0.5f), y = std::sin(radians * 0.5f);
+    c->orientation[0] = x;
+    c->orientation[1] = 0.0f;
+    c->orientation[2] = -y;
+    c->orientation[3] = 0.0f;
+    float x_delta = 0.5f * -std::sin(radians * 0.5f) * delta;
+    float y_delta = 0.5f * std::cos(radians * 0.5f) * delta;
+    c->orientation_delta[0] = x_delta;
+    c->orientation_delta[1] = 0.0f;
+    c->orientation_delta[2] = -y_delta;
+    c->orientation_delta[3] = 0.0f;
+}
+// scene.rs:61-63
+void cvx_camera_set_fov(cvx_camera* c, float fov) { c->screen_distance = 1.0f / std::sin(fov / 2.0f); }
+
+}  // extern "C"

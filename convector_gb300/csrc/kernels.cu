@@ -1,0 +1,318 @@
+// Kernels of the render hot path and their launchers (declared in kernels.h).
+// Compiled with -fmad=false (see x86sem.cuh).
+#include <cuda_runtime.h>
+
+#include "kernels.h"
+#include "shade.cuh"
+
+namespace cvx {
+
+__device__ ApproxTables g_tables;
+
+// Copies the 8 KB approximation tables into shared memory.
+__device__ __forceinline__ void load_tables(ApproxTables& sm) {
+    const uint32_t* src = reinterpret_cast<const uint32_t*>(&g_tables);
+    uint32_t* dst = reinterpret_cast<uint32_t*>(&sm);
+    for (int i = threadIdx.x; i < (int)(sizeof(ApproxTables) / 4); i += blockDim.x) dst[i] = src[i];
+    __syncthreads();
+}
+
+// ---------------------------------------------------------------------------
+// Scene preparation
+
+__global__ void k_prep_geom(const cvx_triangle* __restrict__ tris, uint32_t n, float4* __restrict__ geom,
+                            TriShade* __restrict__ shade) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const cvx_triangle& t = tris[i];
+        F3 v0 = f3(t.v0[0], t.v0[1], t.v0[2]), v1 = f3(t.v1[0], t.v1[1], t.v1[2]), v2 = f3(t.v2[0], t.v2[1], t.v2[2]);
+        F3 e1 = sub(v0, v2), e2 = sub(v1, v0);
+        F3 n = cross(e1, e2);
+        geom[3 * i] = make_float4(v0.x, v0.y, v0.z, n.x);
+        geom[3 * i + 1] = make_float4(e1.x, e1.y, e1.z, n.y);
+        geom[3 * i + 2] = make_float4(e2.x, e2.y, e2.z, n.z);
+        TriShade s;
+        s.uv[0] = t.uv0[0];
+        s.uv[1] = t.uv0[1];
+        s.uv[2] = t.uv1[0];
+        s.uv[3] = t.uv1[1];
+        s.uv[4] = t.uv2[0];
+        s.uv[5] = t.uv2[1];
+        s.material = t.material;
+        s.pad = 0u;
+        shade[i] = s;
+    }
+}
+
+// LightRec (5 x float4): v0 area | e1 rnorm | e2 - | n - | normal -
+__global__ void k_prep_lights(const cvx_triangle* __restrict__ tris, const uint32_t* __restrict__ ds, uint32_t n,
+                              float4* __restrict__ lights) {
+    __shared__ ApproxTables tab;
+    load_tables(tab);
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const cvx_triangle& t = tris[ds[i]];
+        F3 v0 = f3(t.v0[0], t.v0[1], t.v0[2]), v1 = f3(t.v1[0], t.v1[1], t.v1[2]), v2 = f3(t.v2[0], t.v2[1], t.v2[2]);
+        F3 e1 = sub(v0, v2), e2 = sub(v1, v0);
+        F3 nn = cross(e1, e2);
+        float rnorm = x_rsqrt(dot(nn, nn), tab);
+        float area = 0.5f * x_rcp(rnorm, tab);
+        F3 normal = mulk(nn, rnorm);
+        lights[5 * i] = make_float4(v0.x, v0.y, v0.z, area);
+        lights[5 * i + 1] = make_float4(e1.x, e1.y, e1.z, rnorm);
+        lights[5 * i + 2] = make_float4(e2.x, e2.y, e2.z, 0.0f);
+        lights[5 * i + 3] = make_float4(nn.x, nn.y, nn.z, 0.0f);
+        lights[5 * i + 4] = make_float4(normal.x, normal.y, normal.z, 0.0f);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Nearest hit over SoA rays (Bvh::intersect_nearest, bvh.rs:659)
+
+template <bool PACKET>
+__global__ void __launch_bounds__(256) k_intersect(DeviceScene s, const float* __restrict__ rays, uint32_t n,
+                                                   float far_dist, float* __restrict__ t_out,
+                                                   int32_t* __restrict__ tri_out, uint32_t* __restrict__ counters,
+                                                   uint32_t* __restrict__ err) {
+    __shared__ ApproxTables tab;
+    load_tables(tab);
+    const uint32_t stride = gridDim.x * blockDim.x;
+    const unsigned omask = 0xffu << (threadIdx.x & 24u);
+    const uint32_t npad = (n + 7u) & ~7u;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < npad; i += stride) {
+        bool active = i < n;
+        uint32_t src = active ? i : (i & ~7u);
+        F3 o = f3(__ldg(rays + src), __ldg(rays + n + src), __ldg(rays + 2 * n + src));
+        F3 d = f3(__ldg(rays + 3 * n + src), __ldg(rays + 4 * n + src), __ldg(rays + 5 * n + src));
+        Hit h{far_dist, 0.0f, 0.0f, -1};
+        Counters c{0u, 0u};
+        bool ok = true;
+        if (PACKET || active) ok = traverse<PACKET>(s, o, d, active, omask, h, tab, counters ? &c : nullptr);
+        if (!ok) atomicOr(err, kErrStackOverflow);
+        if (active) {
+            t_out[i] = h.t;
+            tri_out[i] = h.tri;
+            if (counters) {
+                counters[i] = c.aabb;
+                counters[n + i] = c.tri;
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Frame rendering: one octet renders one 8-pixel group (RNG_GROUP), or walks
+// the 128 groups of one 32x32 patch in the reference's order (RNG_PATCH).
+
+struct FrameArgs {
+    DeviceScene s;
+    DeviceCamera cam;
+    uint32_t w, h, frame;
+    uint32_t* rgba;
+    uint32_t* gbuf;
+    float* color;
+    float* accum;
+    unsigned long long* rays;
+    uint32_t* err;
+};
+
+// Screen x (or y) of lane k of group g of the 16x4 block at (xb, yb), before
+// jitter (renderer.rs:171-198).
+__device__ __forceinline__ void block_coord(uint32_t w, uint32_t h, uint32_t xb, uint32_t yb, int g, int k,
+                                            float* x, float* y, float* scale_out) {
+    float scale = 2.0f / (float)w;
+    float s2 = 2.0f * scale, s4 = 4.0f * scale, s8 = 8.0f * scale, s12 = 12.0f * scale;
+    float bx = scale * ((float)(k & 3) + ((float)xb - (float)w * 0.5f));
+    float by = scale * ((float)(k >> 2) + ((float)yb - (float)h * 0.5f));
+    int col = g >> 1;
+    float gx = col == 0 ? bx : col == 1 ? bx + s4 : col == 2 ? bx + s8 : bx + s12;
+    float gy = (g & 1) ? by + s2 : by;
+    *x = gx;
+    *y = gy;
+    *scale_out = scale;
+}
+
+__device__ __forceinline__ void store_pixel(const FrameArgs& a, uint32_t px, uint32_t py, const PixelOut& p) {
+    if (px >= a.w || py >= a.h) return;
+    size_t idx = (size_t)py * a.w + px;
+    if (a.rgba) a.rgba[idx] = pack_color(p.color);
+    if (a.gbuf) a.gbuf[idx] = pack_gbuffer(p);
+    if (a.color) {
+        a.color[3 * idx] = p.color.x;
+        a.color[3 * idx + 1] = p.color.y;
+        a.color[3 * idx + 2] = p.color.z;
+    }
+    if (a.accum) {
+        a.accum[3 * idx] += p.color.x;
+        a.accum[3 * idx + 1] += p.color.y;
+        a.accum[3 * idx + 2] += p.color.z;
+    }
+}
+
+__device__ __forceinline__ void flush_rays(const FrameArgs& a, uint32_t rays) {
+    unsigned long long v = rays;
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+    if ((threadIdx.x & 31u) == 0u && v) atomicAdd(a.rays, v);
+}
+
+template <bool PACKET>
+__global__ void __launch_bounds__(128) k_render_group(FrameArgs a) {
+    __shared__ ApproxTables tab;
+    load_tables(tab);
+    const int k = threadIdx.x & 7;
+    const unsigned omask = 0xffu << (threadIdx.x & 24u);
+    const uint32_t bw = (a.w + 15u) / 16u, bh = (a.h + 3u) / 4u;
+    const uint32_t ngroups = bw * bh * 8u;
+    const uint32_t octets = (gridDim.x * blockDim.x) >> 3;
+    uint32_t rays = 0;
+    bool ok = true;
+    // Octet index runs through the 8 groups of a 16x4 block, then blocks in
+    // row-major order, so a warp covers half a block.
+    for (uint32_t gi = (blockIdx.x * blockDim.x + threadIdx.x) >> 3; gi < ngroups; gi += octets) {
+        uint32_t blk = gi >> 3;
+        int g = (int)(gi & 7u);
+        uint32_t xb = (blk % bw) * 16u, yb = (blk / bw) * 4u;
+        uint32_t gx = xb + 4u * (uint32_t)(g >> 1), gy = yb + 2u * (uint32_t)(g & 1);
+        if (gx >= a.w || gy >= a.h) continue;  // whole group outside the frame (octet-uniform)
+        float x, y, scale;
+        block_coord(a.w, a.h, xb, yb, g, k, &x, &y, &scale);
+        LaneRng rng;
+        rng.seed(gx, gy, a.frame, k);
+        x = fmaf(unit_from(rng.next()), scale, x);
+        y = fmaf(unit_from(rng.next()), scale, y);
+        PixelOut p;
+        ok &= render_pixels<PACKET>(a.s, a.cam, x, y, rng, omask, tab, p, rays);
+        store_pixel(a, gx + (uint32_t)(k & 3), gy + (uint32_t)(k >> 2), p);
+    }
+    if (!ok) atomicOr(a.err, kErrStackOverflow);
+    flush_rays(a, rays);
+}
+
+template <bool PACKET>
+__global__ void __launch_bounds__(128) k_render_patch(FrameArgs a) {
+    __shared__ ApproxTables tab;
+    load_tables(tab);
+    const int k = threadIdx.x & 7;
+    const unsigned omask = 0xffu << (threadIdx.x & 24u);
+    const uint32_t pw = (a.w + 31u) / 32u, ph = (a.h + 31u) / 32u;
+    const uint32_t octets = (gridDim.x * blockDim.x) >> 3;
+    uint32_t rays = 0;
+    bool ok = true;
+    for (uint32_t pi = (blockIdx.x * blockDim.x + threadIdx.x) >> 3; pi < pw * ph; pi += octets) {
+        uint32_t x0 = (pi / ph) * 32u, y0 = (pi % ph) * 32u;
+        LaneRng rng;
+        rng.seed(x0, y0, a.frame, k);
+        for (uint32_t i = 0; i < 2; i++) {
+            for (uint32_t j = 0; j < 8; j++) {
+                uint32_t xb = x0 + i * 16u, yb = y0 + j * 4u;
+                float jx[8], jy[8];
+                for (int q = 0; q < 8; q++) jx[q] = unit_from(rng.next());
+                for (int q = 0; q < 8; q++) jy[q] = unit_from(rng.next());
+#pragma unroll 1
+                for (int g = 0; g < 8; g++) {
+                    float x, y, scale;
+                    block_coord(a.w, a.h, xb, yb, g, k, &x, &y, &scale);
+                    x = fmaf(jx[g], scale, x);
+                    y = fmaf(jy[g], scale, y);
+                    PixelOut p;
+                    ok &= render_pixels<PACKET>(a.s, a.cam, x, y, rng, omask, tab, p, rays);
+                    store_pixel(a, xb + 4u * (uint32_t)(g >> 1) + (uint32_t)(k & 3),
+                                yb + 2u * (uint32_t)(g & 1) + (uint32_t)(k >> 2), p);
+                }
+            }
+        }
+    }
+    if (!ok) atomicOr(a.err, kErrStackOverflow);
+    flush_rays(a, rays);
+}
+
+__global__ void k_resolve(const float* __restrict__ accum, uint32_t npx, float factor, uint32_t* __restrict__ rgba) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < npx; i += gridDim.x * blockDim.x) {
+        F3 c = f3(accum[3 * i] * factor, accum[3 * i + 1] * factor, accum[3 * i + 2] * factor);
+        rgba[i] = pack_color(c);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Launchers
+
+static int g_num_sms = 0;
+static int num_sms() {
+    if (!g_num_sms) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev);
+        if (g_num_sms <= 0) g_num_sms = 1;
+    }
+    return g_num_sms;
+}
+
+cudaError_t upload_tables(const uint16_t* rcp, const uint16_t* rsqrt) {
+    ApproxTables t;
+    for (int i = 0; i < 2048; i++) {
+        t.rcp[i] = rcp[i];
+        t.rsqrt[i] = rsqrt[i];
+    }
+    return cudaMemcpyToSymbol(g_tables, &t, sizeof t);
+}
+
+cudaError_t launch_prep_geom(const cvx_triangle* tris, uint32_t n, float4* geom, TriShade* shade, cudaStream_t st) {
+    uint32_t blocks = (n + 255) / 256;
+    if (blocks > 4096) blocks = 4096;
+    if (blocks == 0) blocks = 1;
+    k_prep_geom<<<blocks, 256, 0, st>>>(tris, n, geom, shade);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_prep_lights(const cvx_triangle* tris, const uint32_t* ds, uint32_t n, float4* lights,
+                               cudaStream_t st) {
+    uint32_t blocks = (n + 127) / 128;
+    if (blocks > 1024) blocks = 1024;
+    if (blocks == 0) blocks = 1;
+    k_prep_lights<<<blocks, 128, 0, st>>>(tris, ds, n, lights);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_intersect(const DeviceScene& s, const float* rays, uint32_t n, float far_dist, bool packet,
+                             float* t_out, int32_t* tri_out, uint32_t* counters, uint32_t* err, uint32_t block,
+                             uint32_t blocks_per_sm, cudaStream_t st) {
+    if (block == 0) block = 128;
+    if (blocks_per_sm == 0) blocks_per_sm = 8;
+    uint32_t need = ((n + 7u) & ~7u) / block + 1u;
+    uint32_t blocks = (uint32_t)num_sms() * blocks_per_sm;
+    if (blocks > need) blocks = need;
+    if (packet)
+        k_intersect<true><<<blocks, block, 0, st>>>(s, rays, n, far_dist, t_out, tri_out, counters, err);
+    else
+        k_intersect<false><<<blocks, block, 0, st>>>(s, rays, n, far_dist, t_out, tri_out, counters, err);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_render(const DeviceScene& s, const DeviceCamera& cam, uint32_t w, uint32_t h, uint32_t frame,
+                          bool packet, bool patch_order, uint32_t* rgba, uint32_t* gbuf, float* color, float* accum,
+                          unsigned long long* rays, uint32_t* err, uint32_t block, cudaStream_t st) {
+    FrameArgs a{s, cam, w, h, frame, rgba, gbuf, color, accum, rays, err};
+    if (block == 0) block = 128;
+    if (patch_order) {
+        uint32_t units = ((w + 31) / 32) * ((h + 31) / 32);
+        uint32_t blocks = (units * 8 + block - 1) / block;
+        if (packet) k_render_patch<true><<<blocks, block, 0, st>>>(a);
+        else k_render_patch<false><<<blocks, block, 0, st>>>(a);
+    } else {
+        uint32_t units = ((w + 15) / 16) * ((h + 3) / 4) * 8;
+        uint32_t need = (units * 8 + block - 1) / block;
+        uint32_t blocks = (uint32_t)num_sms() * 16u;
+        if (blocks > need) blocks = need;
+        if (packet) k_render_group<true><<<blocks, block, 0, st>>>(a);
+        else k_render_group<false><<<blocks, block, 0, st>>>(a);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_resolve(const float* accum, uint32_t npx, float factor, uint32_t* rgba, cudaStream_t st) {
+    uint32_t blocks = (npx + 255) / 256;
+    if (blocks > 4096) blocks = 4096;
+    if (blocks == 0) blocks = 1;
+    k_resolve<<<blocks, 256, 0, st>>>(accum, npx, factor, rgba);
+    return cudaGetLastError();
+}
+
+}  // namespace cvx

@@ -1,0 +1,22 @@
+// Launchers of the device kernels (kernels.cu), used by the C-ABI (capi.cu).
+#pragma once
+#include <cuda_runtime.h>
+
+#include "../../include/convector_gpu.h"
+#include "layout.cuh"
+
+namespace cvx {
+
+cudaError_t upload_tables(const uint16_t* rcp, const uint16_t* rsqrt);
+cudaError_t launch_prep_geom(const cvx_triangle* tris, uint32_t n, float4* geom, TriShade* shade, cudaStream_t st);
+cudaError_t launch_prep_lights(const cvx_triangle* tris, const uint32_t* ds, uint32_t n, float4* lights,
+                               cudaStream_t st);
+cudaError_t launch_intersect(const DeviceScene& s, const float* rays, uint32_t n, float far_dist, bool packet,
+                             float* t_out, int32_t* tri_out, uint32_t* counters, uint32_t* err, uint32_t block,
+                             uint32_t blocks_per_sm, cudaStream_t st);
+cudaError_t launch_render(const DeviceScene& s, const DeviceCamera& cam, uint32_t w, uint32_t h, uint32_t frame,
+                          bool packet, bool patch_order, uint32_t* rgba, uint32_t* gbuf, float* color, float* accum,
+                          unsigned long long* rays, uint32_t* err, uint32_t block, cudaStream_t st);
+cudaError_t launch_resolve(const float* accum, uint32_t npx, float factor, uint32_t* rgba, cudaStream_t st);
+
+}  // namespace cvx

@@ -1,0 +1,141 @@
+// Nearest-hit BVH traversal (bvh.rs:589-657) with the reference's box test
+// (aabb.rs:105-141) and triangle test (triangle.rs:59-148), bit-exact.
+//
+// Two variants share the arithmetic:
+//  * PACKET: the 8 threads of an octet (lanes 8k..8k+7 of a warp) are one
+//    reference ray packet. Every decision the reference takes over the packet
+//    (child order by should_try_before, push by any_masked, cull by
+//    is_further_away_than) is a warp vote over the octet, so all 8 threads walk
+//    the same node sequence as the reference's packet, node fetches are
+//    broadcast loads, and the result is the reference's lane for lane.
+//  * SINGLE: each thread walks its own ray with the same decisions taken over
+//    itself alone. Results equal the packet traversal except where two
+//    triangles tie in t, or where the approximate-reciprocal box test is not
+//    conservative for a grazing ray.
+#pragma once
+#include "layout.cuh"
+#include "x86sem.cuh"
+
+namespace cvx {
+
+struct Hit {
+    float t, u, v;
+    int32_t tri;
+};
+
+struct BoxT {
+    float tmin, tmax;
+    bool mask;
+};
+
+__device__ __forceinline__ BoxT box_test(float lx, float ly, float lz, float hx, float hy, float hz, F3 o, F3 inv) {
+    float tx1 = (lx - o.x) * inv.x, tx2 = (hx - o.x) * inv.x;
+    float ty1 = (ly - o.y) * inv.y, ty2 = (hy - o.y) * inv.y;
+    float tz1 = (lz - o.z) * inv.z, tz2 = (hz - o.z) * inv.z;
+    float tmin = xmax(xmin(tx1, tx2), xmax(xmin(ty1, ty2), xmin(tz1, tz2)));
+    float tmax = xmin(xmax(tx1, tx2), xmin(xmax(ty1, ty2), xmax(tz1, tz2)));
+    return BoxT{tmin, tmax, geq(tmax, tmin)};
+}
+
+// One triangle against one lane; updates the hit when the reference would
+// pick the new intersection (triangle.rs:122-147).
+__device__ __forceinline__ void tri_test(const float4* __restrict__ geom, uint32_t i, F3 o, F3 d, bool active,
+                                         Hit& h) {
+    float4 A = __ldg(geom + 3 * i), B = __ldg(geom + 3 * i + 1), C = __ldg(geom + 3 * i + 2);
+    F3 v0 = f3(A.x, A.y, A.z), e1 = f3(B.x, B.y, B.z), e2 = f3(C.x, C.y, C.z), n = f3(A.w, B.w, C.w);
+    F3 fr = sub(v0, o);
+    float denom = 1.0f / dot(d, n);
+    float t = dot(fr, n) * denom;
+    F3 c = cross(d, fr);
+    float u = dot(c, e2) * denom;
+    float v = dot(c, e1) * denom;
+    float w = (1.0f - u) - v;
+    bool reject = sneg(t) | sneg(u) | sneg(v) | sneg(w) | !active | geq(t, h.t);
+    if (!reject) {
+        h.t = t;
+        h.u = u;
+        h.v = v;
+        h.tri = (int32_t)i;
+    }
+}
+
+__device__ __forceinline__ bool oct_all(unsigned m, bool p) { return (__ballot_sync(m, p) & m) == m; }
+__device__ __forceinline__ bool oct_any(unsigned m, bool p) { return (__ballot_sync(m, p) & m) != 0u; }
+
+struct Counters {
+    uint32_t aabb, tri;
+};
+
+// omask: the octet's lanes in the warp (PACKET) or the calling lane (SINGLE).
+// In SINGLE mode an inactive lane must not call this. Returns false on stack
+// overflow (the hit is then incomplete).
+template <bool PACKET>
+__device__ __forceinline__ bool traverse(const DeviceScene& s, F3 o, F3 d, bool active, unsigned omask, Hit& h,
+                                         const ApproxTables& tab, Counters* cnt) {
+    F3 inv = f3(x_rcp(d.x, tab), x_rcp(d.y, tab), x_rcp(d.z, tab));
+    uint32_t st_idx[kStackDepth];
+    uint32_t st_len[kStackDepth];
+    float st_t[kStackDepth];
+    int sp = 0;
+    uint32_t na = 2, nt = 0;
+    bool ok = true;
+
+    uint32_t pair = 0;
+    for (;;) {
+        // Test the two children of a pair and push them in the reference order.
+        const float4* np = s.nodes + 4 * pair;
+        float4 q0 = __ldg(np), q1 = __ldg(np + 1), q2 = __ldg(np + 2), q3 = __ldg(np + 3);
+        BoxT b0 = box_test(q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, o, inv);
+        BoxT b1 = box_test(q1.z, q1.w, q2.x, q2.y, q2.z, q2.w, o, inv);
+        bool first0 = !sneg(b0.tmin - b1.tmin);
+        bool hit0 = b0.mask & active & !sneg(b0.tmax);
+        bool hit1 = b1.mask & active & !sneg(b1.tmax);
+        if (PACKET) {
+            first0 = oct_all(omask, first0);
+            hit0 = oct_any(omask, hit0);
+            hit1 = oct_any(omask, hit1);
+        }
+        // Lanes outside the box never block a cull (aabb.rs:171-177): +inf.
+        float c0 = b0.mask ? b0.tmin : __int_as_float(0x7f800000);
+        float c1 = b1.mask ? b1.tmin : __int_as_float(0x7f800000);
+        uint32_t i0 = __float_as_uint(q3.x), l0 = __float_as_uint(q3.y);
+        uint32_t i1 = __float_as_uint(q3.z), l1 = __float_as_uint(q3.w);
+        int need = (int)hit0 + (int)hit1;
+        if (sp + need > kStackDepth) {
+            ok = false;
+            break;
+        }
+        if (first0) {
+            if (hit0) { st_idx[sp] = i0; st_len[sp] = l0; st_t[sp] = c0; sp++; }
+            if (hit1) { st_idx[sp] = i1; st_len[sp] = l1; st_t[sp] = c1; sp++; }
+        } else {
+            if (hit1) { st_idx[sp] = i1; st_len[sp] = l1; st_t[sp] = c1; sp++; }
+            if (hit0) { st_idx[sp] = i0; st_len[sp] = l0; st_t[sp] = c0; sp++; }
+        }
+        // Pop until an internal node whose children must be tested.
+        bool descend = false;
+        while (sp > 0) {
+            sp--;
+            uint32_t idx = st_idx[sp], len = st_len[sp];
+            bool skip = !active | geq(st_t[sp], h.t);
+            if (PACKET) skip = oct_all(omask, skip);
+            if (skip) continue;
+            if (len == 0u) {
+                na += 2;
+                pair = idx >> 1;
+                descend = true;
+                break;
+            }
+            for (uint32_t i = idx; i < idx + len; i++) tri_test(s.geom, i, o, d, active, h);
+            nt += len;
+        }
+        if (!descend) break;
+    }
+    if (cnt) {
+        cnt->aabb = na;
+        cnt->tri = nt;
+    }
+    return ok;
+}
+
+}  // namespace cvx

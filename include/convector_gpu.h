@@ -1,0 +1,191 @@
+/*
+ * convector_gpu.h -- C-ABI of the GB300 render hot path of ruuda/convector.
+ *
+ * The reference exposes its hot path as Rust methods, not an FFI; each entry
+ * point below names the reference interface it stands in for (paths relative
+ * to the reference's src/). The reference panics on bad input; here every call
+ * returns a status (0 = CVX_OK) and cvx_last_error() gives the message of the
+ * calling thread's last failure.
+ *
+ * Ownership and threading: the caller owns every host buffer it passes;
+ * handles own their device memory. A handle must be used by one thread at a
+ * time; distinct handles may be used concurrently. Calls that take host
+ * buffers are synchronous. Nothing here falls back to the CPU: without a
+ * usable CUDA device the GPU entry points return CVX_ERR_CUDA.
+ */
+#ifndef CONVECTOR_GPU_H
+#define CONVECTOR_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+    CVX_OK = 0,
+    CVX_ERR_INVALID = 1,    /* bad argument or unsupported size */
+    CVX_ERR_IO = 2,         /* file could not be read */
+    CVX_ERR_PARSE = 3,      /* malformed OBJ text */
+    CVX_ERR_DEGENERATE = 4, /* collinear triangle (wavefront.rs:30-46) */
+    CVX_ERR_CUDA = 5,       /* CUDA runtime failure or no device */
+    CVX_ERR_DEVICE = 6,     /* a kernel reported an error (e.g. stack overflow) */
+    CVX_ERR_CAPACITY = 7,   /* admission refused: not enough device memory */
+    CVX_ERR_TIMEOUT = 8,    /* a request did not finish in time */
+    CVX_ERR_CANCELLED = 9,  /* a request was cancelled */
+    CVX_ERR_NOT_FOUND = 10  /* unknown request or scene id */
+};
+
+/* Reference `Triangle` (triangle.rs:24-32), 64 bytes. `material` is the
+ * reference's 32-bit SMaterial encoding (material.rs:10-31). */
+typedef struct cvx_triangle {
+    float v0[3], v1[3], v2[3];
+    float uv0[2], uv1[2], uv2[2];
+    uint32_t material;
+} cvx_triangle;
+
+/* Reference `BvhNode` (bvh.rs:21-30), 32 bytes: len == 0 marks an internal
+ * node whose children are nodes index and index + 1; a leaf covers triangles
+ * index .. index + len. Nodes 0 and 1 are the two roots. */
+typedef struct cvx_bvh_node {
+    float origin[3];
+    float far_[3];
+    uint32_t index;
+    uint32_t len;
+} cvx_bvh_node;
+
+/* Reference `Camera` (scene.rs:20-30). */
+typedef struct cvx_camera {
+    float position[3];
+    float position_delta[3];
+    float orientation[4];       /* quaternion a, b, c, d */
+    float orientation_delta[4];
+    float screen_distance;
+} cvx_camera;
+
+typedef struct cvx_mesh cvx_mesh;
+typedef struct cvx_bvh cvx_bvh;
+typedef struct cvx_scene cvx_scene;
+typedef struct cvx_renderer cvx_renderer;
+
+/* Copies the calling thread's last error message; returns its status. */
+int32_t cvx_last_error(char* buf, size_t len);
+
+/* ---- host: scene loading and BVH build -------------------------------- */
+
+/* Mesh::load_with_materials (wavefront.rs:83-152). `names[i]` maps to the
+ * SMaterial bits `materials[i]`; an unknown `usemtl` name is an error. */
+int32_t cvx_mesh_load_obj(const char* path, const char* const* names, const uint32_t* materials,
+                          uint32_t n_materials, cvx_mesh** out);
+/* The same parser over OBJ text in memory. */
+int32_t cvx_mesh_parse_obj(const char* text, size_t len, const char* const* names, const uint32_t* materials,
+                           uint32_t n_materials, cvx_mesh** out);
+uint32_t cvx_mesh_num_triangles(const cvx_mesh* mesh);
+void cvx_mesh_destroy(cvx_mesh* mesh);
+
+/* Bvh::from_meshes (bvh.rs:547-568) and Bvh::build (bvh.rs:488-545): the
+ * reference's binned tree-SAH build, node order and triangle order. */
+int32_t cvx_bvh_from_meshes(const cvx_mesh* const* meshes, uint32_t n_meshes, cvx_bvh** out);
+int32_t cvx_bvh_build(const cvx_triangle* triangles, uint32_t n, cvx_bvh** out);
+uint32_t cvx_bvh_num_nodes(const cvx_bvh* bvh);
+uint32_t cvx_bvh_num_triangles(const cvx_bvh* bvh);
+/* Copies nodes / triangles (BVH order) / source index of each BVH-order
+ * triangle into caller buffers sized by the counts above. */
+void cvx_bvh_copy_nodes(const cvx_bvh* bvh, cvx_bvh_node* out);
+void cvx_bvh_copy_triangles(const cvx_bvh* bvh, cvx_triangle* out);
+void cvx_bvh_copy_source_index(const cvx_bvh* bvh, uint32_t* out);
+/* Bvh::print_stats (bvh.rs:570-583) figures, plus the tree depth. */
+void cvx_bvh_stats(const cvx_bvh* bvh, float* avg_tris_per_leaf, float* avg_area_ratio, uint32_t* depth);
+void cvx_bvh_destroy(cvx_bvh* bvh);
+
+/* Camera::new / set_rotation / set_fov (scene.rs:34-74), computed on the host. */
+void cvx_camera_default(cvx_camera* cam);
+void cvx_camera_set_rotation(cvx_camera* cam, float radians, float delta);
+void cvx_camera_set_fov(cvx_camera* cam, float fov);
+
+/* ---- device: scenes ------------------------------------------------------ */
+
+/* Scene::from_meshes (scene.rs:114-129) given a built BVH: uploads nodes and
+ * triangles in BVH order and the direct-sample list (triangles with material
+ * bit 30). Rejects trees deeper than the device traversal stack and
+ * glossiness indices above 5 (material.rs:497-512 has six entries). */
+int32_t cvx_scene_create(const cvx_triangle* triangles_bvh_order, uint32_t n_triangles, const cvx_bvh_node* nodes,
+                         uint32_t n_nodes, cvx_scene** out);
+int32_t cvx_scene_from_bvh(const cvx_bvh* bvh, cvx_scene** out);
+uint32_t cvx_scene_num_direct_samples(const cvx_scene* scene);
+/* light_pick 0: `bits >> 29` as scene.rs:159 (requires exactly 8 direct-sample
+ * triangles); 1 (default): `(bits * n) >> 32`, identical to it when n == 8. */
+int32_t cvx_scene_set_light_pick(cvx_scene* scene, uint32_t light_pick);
+void cvx_scene_destroy(cvx_scene* scene);
+
+/* Traversal variants (flags of cvx_intersect_nearest, traversal of cvx_render_config). */
+enum { CVX_TRAVERSE_PACKET = 0, CVX_TRAVERSE_SINGLE = 1 };
+
+/* Bvh::intersect_nearest (bvh.rs:659-662) over n rays in SoA form, packed
+ * 8 per reference packet in input order; the hit record starts at
+ * `far_dist` (MIntersection::with_max_distance, ray.rs:95-103). Outputs the
+ * hit distance and the BVH-order triangle index (-1 for no hit). Host
+ * buffers; copies in and out inside the call. */
+int32_t cvx_intersect_nearest(cvx_scene* scene, const float* ox, const float* oy, const float* oz,
+                              const float* dx, const float* dy, const float* dz, uint32_t n, float far_dist,
+                              uint32_t traversal, float* t_out, int32_t* tri_out);
+/* Device-pointer form: `rays` holds 6 arrays of n floats (ox oy oz dx dy dz);
+ * `stream` is a cudaStream_t (NULL: the default stream). Asynchronous.
+ * `counters`, when not NULL, receives 2 * n u32: per ray the boxes and the
+ * triangles its packet (or the ray, single mode) tested (bvh.rs:604-651). */
+int32_t cvx_intersect_nearest_device(cvx_scene* scene, const float* rays, uint32_t n, float far_dist,
+                                     uint32_t traversal, float* t_out, int32_t* tri_out, uint32_t* counters,
+                                     void* stream);
+
+/* ---- device: renderer ---------------------------------------------------- */
+
+/* RNG order: CVX_RNG_PATCH reproduces the reference's stream exactly (one
+ * generator per 32x32 patch, renderer.rs:306-327; one octet per patch on the
+ * GPU); CVX_RNG_GROUP seeds each 8-pixel group from its own pixel
+ * coordinates so that every group renders in parallel. */
+enum { CVX_RNG_PATCH = 0, CVX_RNG_GROUP = 1 };
+/* Kernel organisation: one fused kernel per frame, or the wavefront form
+ * (ray generation, traversal, shading and accumulation kernels over SoA ray
+ * queues with compaction), optionally replayed as a CUDA graph. */
+enum { CVX_MODE_MEGAKERNEL = 0, CVX_MODE_WAVEFRONT = 1 };
+
+typedef struct cvx_render_config {
+    uint32_t rng_order;   /* CVX_RNG_* */
+    uint32_t traversal;   /* CVX_TRAVERSE_* */
+    uint32_t mode;        /* CVX_MODE_* */
+    uint32_t block_size;  /* threads per block, multiple of 32 (0: default) */
+    uint32_t use_graph;   /* wavefront mode: capture the bounce loop in a CUDA graph */
+} cvx_render_config;
+
+/* Renderer::new (renderer.rs:121-130). Any width and height are accepted;
+ * sizes off the reference tiling are padded and cropped. */
+int32_t cvx_renderer_create(cvx_scene* scene, uint32_t width, uint32_t height, const cvx_render_config* config,
+                            cvx_renderer** out);
+void cvx_renderer_destroy(cvx_renderer* r);
+/* The scene's camera (scene.rs:103 `pub camera`). */
+int32_t cvx_renderer_set_camera(cvx_renderer* r, const cvx_camera* cam);
+/* Renderer::render_patch_u8 (renderer.rs:306-327) over every patch of the
+ * frame: RGBA8 colour and gbuffer words, row-major, row 0 at the bottom
+ * (renderer.rs:210-235 stores rows bottom-up). Either output may be NULL. */
+int32_t cvx_render_frame_u8(cvx_renderer* r, uint32_t frame_number, uint32_t* rgba, uint32_t* gbuffer);
+/* Renderer::accumulate_patch_f32 (renderer.rs:339-362) over the frame: adds
+ * this frame's colour to the device accumulator; gbuffer may be NULL. */
+int32_t cvx_accumulate_frame_f32(cvx_renderer* r, uint32_t frame_number, uint32_t* gbuffer);
+/* Renderer::buffer_f32_into_render_buffer (renderer.rs:378-410). */
+int32_t cvx_resolve_u8(cvx_renderer* r, uint32_t num_samples, uint32_t* rgba);
+/* Reads (row-major, 3 floats per pixel) or zeroes the accumulator
+ * (Renderer::new_buffer_f32, renderer.rs:366-374). */
+int32_t cvx_read_accumulator(cvx_renderer* r, float* out);
+int32_t cvx_clear_accumulator(cvx_renderer* r);
+/* Per-pixel linear colour of the last rendered frame (3 floats per pixel),
+ * before quantisation. */
+int32_t cvx_read_frame_f32(cvx_renderer* r, float* out);
+/* Rays traced by the last frame (camera plus bounce rays, active lanes only)
+ * and its device time. */
+int32_t cvx_renderer_stats(cvx_renderer* r, uint64_t* rays, float* ms);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

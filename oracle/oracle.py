@@ -1,0 +1,120 @@
+"""ctypes front end of liboracle.so (convector_oracle.cpp).
+
+ORACLE / TEST INFRASTRUCTURE: only tests/, __graft_entry__.smoke() and the
+CPU-baseline leg of bench.py use this module, as the checker. The product
+(convector_gb300) never imports it.
+"""
+
+import ctypes
+import os
+
+import numpy as np
+
+from . import build as _build
+
+_L = None
+
+P, U32, I32, F32, U64 = ctypes.c_void_p, ctypes.c_uint32, ctypes.c_int32, ctypes.c_float, ctypes.c_uint64
+
+RNG_PATCH, RNG_GROUP = 0, 1
+TRAVERSE_PACKET, TRAVERSE_SINGLE, BRUTE_FORCE = 0, 1, 2
+
+
+def lib():
+    global _L
+    if _L is None:
+        path = _build.build()
+        L = ctypes.CDLL(path)
+        sig = {
+            "orc_scene_new": (P, [P, U32, P, U32, P, U32, ctypes.c_int]),
+            "orc_scene_free": (None, [P]),
+            "orc_intersect": (None, [P, P, P, P, P, P, P, U32, F32, ctypes.c_int, P, P, P, P, P, P, ctypes.c_int]),
+            "orc_render": (U64, [P, P, U32, U32, U32, ctypes.c_int, ctypes.c_int, P, P, P, P, ctypes.c_int]),
+            "orc_resolve": (None, [P, U32, U32, U32, P]),
+            "orc_rcp": (F32, [F32]), "orc_rsqrt": (F32, [F32]), "orc_recip_precise": (F32, [F32]),
+            "orc_sin": (F32, [F32]), "orc_cos": (F32, [F32]), "orc_acos": (F32, [F32]),
+            "orc_acos_fast": (F32, [F32]), "orc_cvtps": (I32, [F32]),
+            "orc_rng_draws": (None, [U32, U32, U32, U32, P]),
+            "orc_rng_samples": (None, [U32, U32, U32, ctypes.c_int, U32, P]),
+            "orc_rotate_hemisphere": (None, [P, P, P]),
+            "orc_quat_rotate": (None, [P, P, P]),
+            "orc_quat_interpolate": (None, [P, P, F32, P]),
+            "orc_aabb_intersect": (ctypes.c_int, [P, P, P, P, P]),
+            "orc_triangle_intersect": (ctypes.c_int, [P, P, P, F32, P]),
+            "orc_intersect_direct": (ctypes.c_int, [P, P, P, P]),
+            "orc_camera_ray": (None, [P, F32, F32, F32, P]),
+            "orc_sky_intensity": (None, [P, P]),
+        }
+        for name, (res, args) in sig.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _L = L
+    return _L
+
+
+def _p(a):
+    return None if a is None else ctypes.c_void_p(a.ctypes.data)
+
+
+def f32(*v):
+    return np.ascontiguousarray(np.array(v, dtype=np.float32).ravel())
+
+
+def default_threads():
+    return max(1, os.cpu_count() or 1)
+
+
+class OracleScene:
+    """The hot path's scene: BVH-order triangles (n x 16 words) and nodes (n x 8 words)."""
+
+    def __init__(self, triangles, nodes, general_pick=True):
+        self.triangles = np.ascontiguousarray(triangles).view(np.uint32).reshape(-1, 16)
+        self.nodes = np.ascontiguousarray(nodes).view(np.uint32).reshape(-1, 8)
+        ds = np.nonzero((self.triangles[:, 15] >> 30) & 1)[0].astype(np.uint32)
+        self.ds = np.ascontiguousarray(ds)
+        self._h = lib().orc_scene_new(_p(self.triangles), self.triangles.shape[0], _p(self.nodes),
+                                      self.nodes.shape[0], _p(self.ds), self.ds.shape[0], int(general_pick))
+
+    @staticmethod
+    def from_bvh(bvh, general_pick=True):
+        return OracleScene(bvh.triangles, bvh.nodes, general_pick)
+
+    def intersect(self, origins, directions, far=1.0e5, mode=TRAVERSE_PACKET, nthreads=None, counters=False):
+        o = np.asarray(origins, dtype=np.float32)
+        d = np.asarray(directions, dtype=np.float32)
+        n = o.shape[0]
+        cols = [np.ascontiguousarray(o[:, k]) for k in range(3)] + [np.ascontiguousarray(d[:, k]) for k in range(3)]
+        t = np.empty(n, np.float32)
+        tri = np.empty(n, np.int32)
+        tu = np.empty(n, np.float32)
+        tv = np.empty(n, np.float32)
+        na = np.zeros(n, np.uint32) if counters else None
+        nt = np.zeros(n, np.uint32) if counters else None
+        lib().orc_intersect(self._h, *[_p(c) for c in cols], n, far, mode, _p(t), _p(tri), _p(tu), _p(tv), _p(na),
+                            _p(nt), nthreads or default_threads())
+        if counters:
+            return t, tri, na, nt
+        return t, tri
+
+    def render(self, camera, width, height, frame, rng_order=RNG_GROUP, traversal=TRAVERSE_PACKET, nthreads=None,
+               color=True, accum=None):
+        cam = np.ascontiguousarray(camera, dtype=np.float32)
+        rgba = np.zeros((height, width), np.uint32)
+        gbuf = np.zeros((height, width), np.uint32)
+        col = np.zeros((height, width, 3), np.float32) if color else None
+        rays = lib().orc_render(self._h, _p(cam), width, height, frame, rng_order, traversal, _p(rgba), _p(gbuf),
+                                _p(col), _p(accum), nthreads or default_threads())
+        return rgba, gbuf, col, rays
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _L is not None:
+            _L.orc_scene_free(self._h)
+            self._h = None
+
+
+def resolve(accum, n):
+    h, w = accum.shape[:2]
+    rgba = np.zeros((h, w), np.uint32)
+    lib().orc_resolve(_p(np.ascontiguousarray(accum, dtype=np.float32)), w, h, n, _p(rgba))
+    return rgba

@@ -1,0 +1,189 @@
+"""Host-side boundary tests (no GPU): C-ABI exports, OBJ loading, BVH build,
+camera setters and the procedural scenes."""
+
+import ctypes
+import math
+import os
+import re
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+REFERENCE = os.environ.get("CONVECTOR_REFERENCE", "/root/reference")
+
+
+def test_library_exports_every_declared_symbol(cvx):
+    decls = set()
+    inc = os.path.join(ROOT, "include")
+    for name in os.listdir(inc):
+        if name.endswith(".h"):
+            text = open(os.path.join(inc, name)).read()
+            decls |= set(re.findall(r"\b(cvx_[a-z0-9_]+)\s*\(", text))
+    assert len(decls) > 30
+    L = ctypes.CDLL(cvx._build.LIB)
+    missing = [d for d in sorted(decls) if not hasattr(L, d)]
+    assert not missing, missing
+
+
+def test_obj_fan_triangulation_and_tex_coords(cvx):
+    text = "v 0 0 0\nv 1 0 0\nv 1 1 0\nv 0 1 0\nvt 0 0\nvt 1 0\nvt 1 1\nvt 0 1\nf 1/1 2/2 3/3 4/4\n"
+    # a second quad far away, so that the root splits (bvh.rs:509-512)
+    text += "v 50 0 0\nv 51 0 0\nv 51 1 0\nv 50 1 0\nf 5 6 7 8\n"
+    m = cvx.Mesh.parse(text)
+    assert m.num_triangles == 4
+    bvh = cvx.Bvh.from_meshes([m])
+    tris = bvh.triangles_f32
+    assert sorted(bvh.source_index.tolist()) == [0, 1, 2, 3]
+    t1 = tris[list(bvh.source_index).index(1)]
+    # second fan triangle is (v0, v2, v3) with tex coords (t0, t2, t3) (wavefront.rs:132-139)
+    assert t1[0:9].tolist() == [0, 0, 0, 1, 1, 0, 0, 1, 0]
+    assert t1[9:15].tolist() == [0, 0, 1, 1, 0, 1]
+    assert bvh.triangles[0, 15] == cvx.SMaterial.white()
+
+
+def test_obj_errors(cvx):
+    ok = "v 0 0 0\nv 1 0 0\nv 0 1 0\n"
+    with pytest.raises(cvx.CvxError, match="degenerate"):
+        cvx.Mesh.parse("v 0 0 0\nv 1 0 0\nv 2 0 0\nf 1 2 3\n")
+    with pytest.raises(cvx.CvxError, match="not present"):
+        cvx.Mesh.parse(ok + "usemtl nope\nf 1 2 3\n")
+    with pytest.raises(cvx.CvxError, match="out of range"):
+        cvx.Mesh.parse(ok + "f 1 2 4\n")
+    with pytest.raises(cvx.CvxError, match="bad face index"):
+        cvx.Mesh.parse(ok + "f 1//1 2 3\n")
+    with pytest.raises(cvx.CvxError, match="bad vertex"):
+        cvx.Mesh.parse("v 0 x 0\n")
+    with pytest.raises(cvx.CvxError) as e:
+        cvx.Mesh.load("/nonexistent/file.obj")
+    assert e.value.status == 2
+    m = cvx.Mesh.parse(ok + "usemtl glass\nf 1 2 3\n", {"glass": cvx.SMaterial.sky()})
+    assert m.num_triangles == 1
+
+
+@pytest.mark.skipif(not os.path.isdir(os.path.join(REFERENCE, "models")), reason="reference models not present")
+@pytest.mark.parametrize("name,mats,count", [
+    ("box_walls.obj", {"wall": 0x00ffffff, "glass": 0xC0000000}, 204),
+    ("suzanne.obj", {}, 968),
+    ("stanford_bunny.obj", {}, 69666),
+    ("stanford_dragon.obj", {}, 100000),
+])
+def test_reference_models_load(cvx, name, mats, count):  # wavefront.rs:155-179
+    m = cvx.Mesh.load_with_materials(os.path.join(REFERENCE, "models", name), mats)
+    assert m.num_triangles == count
+
+
+@pytest.mark.skipif(not os.path.isdir(os.path.join(REFERENCE, "models")), reason="reference models not present")
+def test_reference_indoor_scene(cvx):
+    """The reference's own interactive scene (main.rs:70-88): 284 triangles,
+    8 direct-sample "glass" triangles, which is what the reference's light
+    pick `bits >> 29` needs (scene.rs:147-161)."""
+    from convector_gb300 import scenes
+    m = cvx.Mesh.load_with_materials(os.path.join(REFERENCE, "models", "indoor.obj"), scenes.reference_materials())
+    assert m.num_triangles == 284
+    bvh = cvx.Bvh.from_meshes([m])
+    assert bvh.direct_sample.shape[0] == 8
+    _check_bvh(bvh, 284)
+
+
+def _check_bvh(bvh, n_src):
+    nodes, tris = bvh.nodes, bvh.triangles
+    f = bvh.nodes_f32
+    tf = bvh.triangles_f32
+    assert nodes.shape[0] % 2 == 0
+    assert sorted(bvh.source_index.tolist()) == list(range(n_src))  # a permutation, no duplicates
+    covered = np.zeros(tris.shape[0], np.int64)
+    stack = [0, 1]
+    seen = 0
+    while stack:
+        i = stack.pop()
+        seen += 1
+        lo, hi = f[i, 0:3], f[i, 3:6]
+        idx, ln = nodes[i, 6], nodes[i, 7]
+        if ln == 0:
+            assert idx % 2 == 0 and idx >= 2
+            for c in (idx, idx + 1):
+                assert (f[c, 0:3] >= lo).all() and (f[c, 3:6] <= hi).all()
+                stack.append(c)
+        else:
+            covered[idx:idx + ln] += 1
+            v = tf[idx:idx + ln, 0:9].reshape(-1, 3)
+            assert (v >= lo).all() and (v <= hi).all()
+            # the node box is the tight box of its triangles (bvh.rs:125-132)
+            assert (v.min(0) == lo).all() and (v.max(0) == hi).all()
+    assert seen == nodes.shape[0]
+    assert (covered == 1).all()
+
+
+def _area(lo, hi):
+    s = (hi - lo).astype(np.float32)
+    return np.float32(2.0) * (s[1] * s[2] + s[2] * s[0] + s[0] * s[1])
+
+
+def test_bvh_invariants_room_sphere(cvx):
+    from convector_gb300 import scenes
+    text, mats = scenes.room_sphere()
+    mesh = cvx.Mesh.parse(text, mats)
+    assert mesh.num_triangles == 10 + 4960 + 2
+    bvh = cvx.Bvh.from_meshes([mesh])
+    _check_bvh(bvh, mesh.num_triangles)
+    assert bvh.direct_sample.shape[0] == 2
+    # smaller-area child first (bvh.rs:343-345)
+    f = bvh.nodes_f32
+    for i in range(bvh.nodes.shape[0]):
+        if bvh.nodes[i, 7] == 0:
+            c = bvh.nodes[i, 6]
+            assert _area(f[c, 0:3], f[c, 3:6]) <= _area(f[c + 1, 0:3], f[c + 1, 3:6])
+
+
+def test_bvh_build_is_deterministic(cvx):
+    from convector_gb300 import scenes
+    text, mats = scenes.spheres_and_boxes(3000, seed=3)
+    m = cvx.Mesh.parse(text, mats)
+    a, b = cvx.Bvh.from_meshes([m]), cvx.Bvh.from_meshes([m])
+    assert (a.nodes == b.nodes).all() and (a.triangles == b.triangles).all()
+    _check_bvh(a, m.num_triangles)
+
+
+def test_bvh_needs_a_root_split(cvx):
+    m = cvx.Mesh.parse("v 0 0 0\nv 1 0 0\nv 0 1 0\nf 1 2 3\n")
+    with pytest.raises(cvx.CvxError, match="root"):
+        cvx.Bvh.from_meshes([m])
+
+
+def test_icosphere_counts():
+    from convector_gb300 import scenes
+    v, f = scenes.icosphere(6)
+    assert f.shape[0] == 81920
+    assert v.shape[0] == 40962
+
+
+def test_camera_setters(cvx):
+    c = cvx.Camera()
+    a = c.as_array()
+    assert a[6:10].tolist() == [1, 0, 0, 0]
+    assert abs(a[14] - 1.0 / math.sin(math.pi / 5)) < 1e-6
+    c.set_rotation(1.0, 0.5)
+    a = c.as_array()
+    assert abs(a[6] - math.cos(0.5)) < 1e-6 and abs(a[8] + math.sin(0.5)) < 1e-6
+    assert abs(a[10] - 0.5 * -math.sin(0.5) * 0.5) < 1e-6
+
+
+def test_look_at_quaternion(orc):
+    from convector_gb300 import scenes
+    from oracle.oracle import f32
+    for eye, target in [((0, 1.2, 1.6), (0, 1, -2)), ((3, 0.5, 0.2), (0, 1, -2)), ((0.1, -2, 0.3), (0, 1, 0))]:
+        q = f32(*scenes.look_at_quaternion(eye, target))
+        v, out = f32(0, 0, -1), np.zeros(3, np.float32)
+        orc.lib().orc_quat_rotate(v.ctypes.data, q.ctypes.data, out.ctypes.data)
+        want = np.array(target, float) - np.array(eye, float)
+        assert np.allclose(out, want / np.linalg.norm(want), atol=1e-5)
+
+
+def test_materials_encoding(cvx):  # material.rs:84-136
+    M = cvx.SMaterial
+    assert M.sky() == 0xC0000000 and M.is_direct_sample(M.sky())
+    assert M.white() == 0x00FFFFFF
+    assert M.with_glossiness(M.white(), 4) == 0x10FFFFFF
+    assert M.with_texture(M.white(), 2) == 0x02FFFFFF
+    assert M.diffuse(1.0, 0.1, 0.4) == (0x66 << 16) | (0x19 << 8) | 0xFF
