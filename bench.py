@@ -127,19 +127,21 @@ def build_c0():
     return bvh
 
 
-def cpu_sample_rays_per_s(osc, o, d, target_s=12.0, max_rays=1 << 20):
-    """Times the oracle's packet traversal (all host cores) on a bounded sample."""
+def cpu_sample_rays_per_s(osc, o, d, target_s=10.0):
+    """Times the oracle's packet traversal (all host cores) on a bounded sample:
+    consecutive 1 Mi-ray slices of the workload until about `target_s`."""
     threads = os.cpu_count() or 1
-    n = 8192
-    t0 = time.perf_counter()
-    osc.intersect(o[:n], d[:n], nthreads=threads)
-    est = (time.perf_counter() - t0) / n
-    n = int(min(max_rays, max(8192, target_s / max(est, 1e-9))))
-    n -= n % 8
-    t0 = time.perf_counter()
-    osc.intersect(o[:n], d[:n], nthreads=threads)
-    dt = time.perf_counter() - t0
-    return n / dt, threads, n, dt
+    chunk = 1 << 20
+    osc.intersect(o[:8192], d[:8192], nthreads=threads)
+    done, dt, k = 0, 0.0, 0
+    while dt < target_s and k < 64:
+        lo = (k * chunk) % o.shape[0]
+        t0 = time.perf_counter()
+        osc.intersect(o[lo:lo + chunk], d[lo:lo + chunk], nthreads=threads)
+        dt += time.perf_counter() - t0
+        done += min(chunk, o.shape[0] - lo)
+        k += 1
+    return done / dt, threads, done, dt
 
 
 def run_reference(args):
