@@ -22,8 +22,8 @@ import numpy as np
 
 from . import _build
 
-__all__ = ["SMaterial", "Mesh", "Bvh", "Scene", "Camera", "Renderer", "RenderConfig", "CvxError", "lib",
-           "TRIANGLE_DTYPE_WORDS", "NODE_DTYPE_WORDS"]
+__all__ = ["SMaterial", "Mesh", "Bvh", "Scene", "Camera", "Renderer", "RenderConfig", "Batch", "View", "Server",
+           "CvxError", "lib", "TRIANGLE_DTYPE_WORDS", "NODE_DTYPE_WORDS"]
 
 TRIANGLE_DTYPE_WORDS = 16  # cvx_triangle: v0 v1 v2 (9 f32), uv0..2 (6 f32), material (u32)
 NODE_DTYPE_WORDS = 8       # cvx_bvh_node: origin far_ (6 f32), index, len (u32)
@@ -45,6 +45,26 @@ class _Camera(ctypes.Structure):
     _fields_ = [("position", ctypes.c_float * 3), ("position_delta", ctypes.c_float * 3),
                 ("orientation", ctypes.c_float * 4), ("orientation_delta", ctypes.c_float * 4),
                 ("screen_distance", ctypes.c_float)]
+
+
+class _View(ctypes.Structure):
+    _fields_ = [("scene", ctypes.c_uint32), ("width", ctypes.c_uint32), ("height", ctypes.c_uint32),
+                ("spp", ctypes.c_uint32), ("frame_base", ctypes.c_uint32), ("camera", _Camera)]
+
+
+class _ServerConfig(ctypes.Structure):
+    _fields_ = [("framebuffer_bytes", ctypes.c_uint64), ("max_groups", ctypes.c_uint32),
+                ("traversal", ctypes.c_uint32), ("use_graph", ctypes.c_uint32), ("sequential", ctypes.c_uint32)]
+
+
+class _Request(ctypes.Structure):
+    _fields_ = [("scene", ctypes.c_uint32), ("width", ctypes.c_uint32), ("height", ctypes.c_uint32),
+                ("spp", ctypes.c_uint32), ("frame_base", ctypes.c_uint32), ("camera", _Camera)]
+
+
+class _Result(ctypes.Structure):
+    _fields_ = [("status", ctypes.c_int32), ("submit_s", ctypes.c_double), ("start_s", ctypes.c_double),
+                ("done_s", ctypes.c_double), ("rays", ctypes.c_uint64)]
 
 
 class RenderConfig(ctypes.Structure):
@@ -98,6 +118,15 @@ def lib(build=False):
         "cvx_clear_accumulator": (I32, [P]),
         "cvx_read_frame_f32": (I32, [P, P]),
         "cvx_renderer_stats": (I32, [P, P, P]),
+        "cvx_batch_create": (I32, [P, U32, U32, ctypes.c_uint64, P, P]),
+        "cvx_batch_render": (I32, [P, P, U32, P, P, P]),
+        "cvx_batch_destroy": (None, [P]),
+        "cvx_server_create": (I32, [P, U32, P, P]),
+        "cvx_server_submit": (I32, [P, P, P, P]),
+        "cvx_server_wait": (I32, [P, ctypes.c_uint64, U32, P]),
+        "cvx_server_cancel": (I32, [P, ctypes.c_uint64]),
+        "cvx_server_stats": (I32, [P, P, P, P, P]),
+        "cvx_server_destroy": (None, [P]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -375,3 +404,90 @@ class Renderer:
         if getattr(self, "_h", None) and self._h.value and _LIB is not None:
             _LIB.cvx_renderer_destroy(self._h)
             self._h = None
+
+
+class View:
+    """One image of a batch: a scene index, size, samples and camera."""
+
+    def __init__(self, scene, width, height, spp=1, frame_base=0, camera=None):
+        self.scene, self.width, self.height, self.spp, self.frame_base = scene, width, height, spp, frame_base
+        self.camera = camera if camera is not None else Camera()
+
+    def _c(self):
+        return _View(self.scene, self.width, self.height, self.spp, self.frame_base, self.camera._c)
+
+
+class Batch:
+    """Many views of many resident scenes rendered in shared wavefronts."""
+
+    def __init__(self, scenes, max_groups=1 << 20, max_pixels=1 << 24, traversal=TRAVERSE_SINGLE, use_graph=1,
+                 blocks_per_sm=0):
+        self.scenes = list(scenes)
+        arr = (ctypes.c_void_p * len(self.scenes))(*[s._h.value for s in self.scenes])
+        cfg = RenderConfig(RNG_GROUP, traversal, MODE_WAVEFRONT, blocks_per_sm, use_graph)
+        out = ctypes.c_void_p()
+        _check(lib().cvx_batch_create(arr, len(self.scenes), max_groups, max_pixels, ctypes.byref(cfg),
+                                      ctypes.byref(out)))
+        self._h = out
+
+    def render(self, views, want_images=True):
+        cv = (_View * len(views))(*[v._c() for v in views])
+        imgs = [np.empty((v.height, v.width), dtype=np.uint32) for v in views] if want_images else None
+        ptrs = (ctypes.c_void_p * len(views))(*[im.ctypes.data for im in imgs]) if want_images else None
+        rays, ms = ctypes.c_uint64(), ctypes.c_float()
+        _check(lib().cvx_batch_render(self._h, cv, len(views), ptrs, ctypes.byref(rays), ctypes.byref(ms)))
+        return imgs, rays.value, ms.value
+
+    def __del__(self):
+        if getattr(self, "_h", None) and self._h.value and _LIB is not None:
+            _LIB.cvx_batch_destroy(self._h)
+            self._h = None
+
+
+class Server:
+    """Continuously batched request server over resident scenes."""
+
+    def __init__(self, scenes, framebuffer_bytes=4 << 30, max_groups=1 << 21, traversal=TRAVERSE_SINGLE,
+                 use_graph=1, sequential=False):
+        self.scenes = list(scenes)
+        arr = (ctypes.c_void_p * len(self.scenes))(*[s._h.value for s in self.scenes])
+        cfg = _ServerConfig(framebuffer_bytes, max_groups, traversal, use_graph, int(sequential))
+        out = ctypes.c_void_p()
+        _check(lib().cvx_server_create(arr, len(self.scenes), ctypes.byref(cfg), ctypes.byref(out)))
+        self._h = out
+        self._bufs = {}
+
+    def submit(self, scene, width, height, spp, camera, frame_base=0):
+        req = _Request(scene, width, height, spp, frame_base, camera._c)
+        img = np.empty((height, width), dtype=np.uint32)
+        rid = ctypes.c_uint64()
+        _check(lib().cvx_server_submit(self._h, ctypes.byref(req), ctypes.c_void_p(img.ctypes.data),
+                                       ctypes.byref(rid)))
+        self._bufs[rid.value] = img
+        return rid.value
+
+    def wait(self, rid, timeout_ms=60000):
+        """Returns (status, image or None, result dict); raises CvxError on a timeout."""
+        res = _Result()
+        _check(lib().cvx_server_wait(self._h, rid, timeout_ms, ctypes.byref(res)))
+        img = self._bufs.pop(rid, None)
+        info = {"status": res.status, "submit_s": res.submit_s, "start_s": res.start_s, "done_s": res.done_s,
+                "rays": res.rays}
+        return res.status, (img if res.status == 0 else None), info
+
+    def cancel(self, rid):
+        _check(lib().cvx_server_cancel(self._h, rid))
+
+    def stats(self):
+        now, waves, rays, busy = ctypes.c_double(), ctypes.c_uint64(), ctypes.c_uint64(), ctypes.c_double()
+        _check(lib().cvx_server_stats(self._h, ctypes.byref(now), ctypes.byref(waves), ctypes.byref(rays),
+                                      ctypes.byref(busy)))
+        return {"now_s": now.value, "waves": waves.value, "rays": rays.value, "busy_s": busy.value}
+
+    def close(self):
+        if getattr(self, "_h", None) and self._h.value and _LIB is not None:
+            _LIB.cvx_server_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()

@@ -8,6 +8,7 @@
 #include <string>
 #include <vector>
 
+#include "engine.h"
 #include "internal.h"
 #include "kernels.h"
 #include "x86_approx_tables.h"
@@ -48,6 +49,7 @@ int32_t ensure_device(int* dev_out) {
             s[i] = (uint16_t)(kRsqrt32[i] >> 11);
         }
         CK(upload_tables(r, s), "upload approximation tables");
+        CK(upload_tables_wave(r, s), "upload approximation tables");
         g_tables_ready[dev] = true;
     }
     *dev_out = dev;
@@ -110,7 +112,11 @@ struct cvx_scene {
     }
 };
 
+DeviceScene cvx::scene_view(const cvx_scene* s) { return s->view(); }
+uint32_t cvx::scene_num_lights(const cvx_scene* s) { return s->n_lights; }
+
 struct cvx_renderer {
+    std::unique_ptr<WaveEngine> engine;  // wavefront mode
     cvx_scene* scene = nullptr;
     uint32_t w = 0, h = 0;
     cvx_render_config cfg{};
@@ -194,7 +200,7 @@ int32_t cvx_scene_create(const cvx_triangle* tris, uint32_t n_tris, const cvx_bv
     if ((st = dalloc(&s->d_geom, (size_t)n_tris * 3, "triangles"))) return st;
     if ((st = dalloc(&s->d_shade, n_tris, "shading data"))) return st;
     if ((st = dalloc(&s->d_lights, (size_t)s->n_lights * 5, "lights"))) return st;
-    if ((st = dalloc(&s->d_err, 1, "status"))) return st;
+    if ((st = dalloc(&s->d_err, 2, "status"))) return st;  // [0] status, [1] ray counter
     // Node pairs: q0 = lo0 hi0.x | q1 = hi0.yz lo1.xy | q2 = lo1.z hi1 | q3 = index/len x2
     std::vector<float4> pairs((size_t)n_nodes / 2 * 4);
     for (uint32_t p = 0; p < n_nodes / 2; p++) {
@@ -308,6 +314,10 @@ int32_t cvx_renderer_create(cvx_scene* scene, uint32_t w, uint32_t h, const cvx_
     if (cfg) c = *cfg;
     if (c.rng_order > 1 || c.traversal > 1 || c.mode > 1 || (c.block_size % 32) || c.block_size > 1024)
         return set_error(CVX_ERR_INVALID, "bad render configuration");
+    if (c.mode == CVX_MODE_WAVEFRONT && c.rng_order != CVX_RNG_GROUP)
+        return set_error(CVX_ERR_INVALID,
+                         "the wavefront form needs the per-group RNG order (the patch order is one serial chain "
+                         "per patch)");
     std::unique_ptr<cvx_renderer> r(new cvx_renderer());
     r->scene = scene;
     r->w = w;
@@ -329,6 +339,14 @@ int32_t cvx_renderer_create(cvx_scene* scene, uint32_t w, uint32_t h, const cvx_
     CK(cudaEventCreate(&r->e1), "cudaEventCreate");
     CK(cudaMemsetAsync(r->d_accum, 0, npx * 12, r->stream), "clear accumulator");
     CK(cudaStreamSynchronize(r->stream), "renderer init");
+    if (c.mode == CVX_MODE_WAVEFRONT) {
+        r->engine.reset(new WaveEngine());
+        if ((st = r->engine->init(groups_of(w, h), 1, c.traversal == CVX_TRAVERSE_PACKET, c.use_graph != 0,
+                                  c.block_size / 32)))
+            return st;
+        cvx_scene* sc[1] = {scene};
+        if ((st = r->engine->set_scenes(sc, 1))) return st;
+    }
     *out = r.release();
     return CVX_OK;
 }
@@ -342,7 +360,35 @@ int32_t cvx_renderer_set_camera(cvx_renderer* r, const cvx_camera* cam) {
     return CVX_OK;
 }
 
+static int32_t run_frame_wavefront(cvx_renderer* r, uint32_t frame, bool accumulate, uint32_t* rgba,
+                                   uint32_t* gbuf) {
+    size_t npx = (size_t)r->w * r->h;
+    Job j{};
+    j.cam = r->cam;
+    j.scene = 0;
+    j.w = r->w;
+    j.h = r->h;
+    j.frame = frame;
+    j.out_offset = 0;
+    WaveOutputs out{};
+    out.rgba = accumulate ? nullptr : r->d_rgba;
+    out.gbuf = r->d_gbuf;
+    out.color = r->d_color;
+    out.accum = accumulate ? r->d_accum : nullptr;
+    uint64_t rays = 0;
+    float ms = 0.0f;
+    int32_t st = r->engine->run(std::vector<Job>{j}, out, r->stream, &rays, nullptr, &ms);
+    if (st) return st;
+    r->last_rays = rays;
+    r->last_ms = ms;
+    if (rgba) CK(cudaMemcpyAsync(rgba, r->d_rgba, npx * 4, cudaMemcpyDeviceToHost, r->stream), "copy colour");
+    if (gbuf) CK(cudaMemcpyAsync(gbuf, r->d_gbuf, npx * 4, cudaMemcpyDeviceToHost, r->stream), "copy gbuffer");
+    CK(cudaStreamSynchronize(r->stream), "render");
+    return CVX_OK;
+}
+
 static int32_t run_frame(cvx_renderer* r, uint32_t frame, bool accumulate, uint32_t* rgba, uint32_t* gbuf) {
+    if (r->engine) return run_frame_wavefront(r, frame, accumulate, rgba, gbuf);
     size_t npx = (size_t)r->w * r->h;
     CK(cudaMemsetAsync(r->d_rays, 0, 8, r->stream), "reset counters");
     CK(cudaMemsetAsync(r->d_err, 0, 4, r->stream), "reset status");

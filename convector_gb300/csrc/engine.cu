@@ -1,0 +1,618 @@
+// Host side of the wavefront engine: the wave buffers, the resident scene
+// table, job staging and CUDA-graph replay; the renderer's wavefront mode,
+// the batch API and the request server are built on it.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <unordered_map>
+#include <vector>
+
+#include "engine.h"
+#include "internal.h"
+#include "kernels.h"
+
+namespace cvx {
+
+static int32_t cuda_err(cudaError_t e, const char* what) {
+    return set_error(CVX_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+#define ECK(call, what)                                     \
+    do {                                                    \
+        cudaError_t e_ = (call);                            \
+        if (e_ != cudaSuccess) return cuda_err(e_, what);   \
+    } while (0)
+
+template <class T>
+static int32_t alloc(T** p, size_t n, std::vector<void*>& owned) {
+    *p = nullptr;
+    cudaError_t e = cudaMalloc((void**)p, (n ? n : 1) * sizeof(T));
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return set_error(e == cudaErrorMemoryAllocation ? CVX_ERR_CAPACITY : CVX_ERR_CUDA,
+                         std::string("cudaMalloc for the wave buffers: ") + cudaGetErrorString(e));
+    }
+    owned.push_back(*p);
+    return CVX_OK;
+}
+
+uint32_t groups_of(uint32_t w, uint32_t h) { return 8u * ((w + 15u) / 16u) * ((h + 3u) / 4u); }
+
+WaveEngine::~WaveEngine() {
+    for (auto& g : graphs_) cudaGraphExecDestroy(g.exec);
+    for (void* p : owned_) cudaFree(p);
+    if (h_jobs_) cudaFreeHost(h_jobs_);
+    if (h_hdr_) cudaFreeHost(h_hdr_);
+    if (e0_) cudaEventDestroy(e0_);
+    if (e1_) cudaEventDestroy(e1_);
+}
+
+int32_t WaveEngine::init(uint32_t max_groups, uint32_t max_jobs, bool packet, bool use_graph,
+                         uint32_t blocks_per_sm) {
+    max_groups_ = max_groups;
+    max_jobs_ = max_jobs;
+    packet_ = packet;
+    use_graph_ = use_graph;
+    blocks_per_sm_ = blocks_per_sm;
+    size_t L = (size_t)max_groups * 8;
+    int32_t st = 0;
+    float** f[] = {&st_.ox, &st_.oy, &st_.oz, &st_.dx, &st_.dy, &st_.dz, &st_.cr, &st_.cg, &st_.cb,
+                   &st_.ht, &st_.hu, &st_.hv};
+    for (float** p : f)
+        if ((st = alloc(p, L, owned_))) return st;
+    if ((st = alloc(&st_.rng, L, owned_))) return st;
+    if ((st = alloc(&st_.gbuf, L, owned_))) return st;
+    if ((st = alloc(&st_.flags, L, owned_))) return st;
+    if ((st = alloc(&st_.htri, L, owned_))) return st;
+    if ((st = alloc(&st_.group_job, max_groups, owned_))) return st;
+    if ((st = alloc(&st_.queue[0], max_groups, owned_))) return st;
+    if ((st = alloc(&st_.queue[1], max_groups, owned_))) return st;
+    if ((st = alloc(&st_.counts, 16, owned_))) return st;
+    if ((st = alloc(&d_jobs_, max_jobs, owned_))) return st;
+    if ((st = alloc(&d_hdr_, 1, owned_))) return st;
+    if ((st = alloc(&d_rays_, 1, owned_))) return st;
+    if ((st = alloc(&d_job_rays_, max_jobs, owned_))) return st;
+    if ((st = alloc(&d_err_, 1, owned_))) return st;
+    ECK(cudaMallocHost((void**)&h_jobs_, max_jobs * sizeof(Job)), "pinned job staging");
+    ECK(cudaMallocHost((void**)&h_hdr_, sizeof(WaveHeader)), "pinned job staging");
+    ECK(cudaEventCreate(&e0_), "cudaEventCreate");
+    ECK(cudaEventCreate(&e1_), "cudaEventCreate");
+    return CVX_OK;
+}
+
+int32_t WaveEngine::set_scenes(cvx_scene* const* scenes, uint32_t n) {
+    std::vector<DeviceScene> v(n);
+    for (uint32_t i = 0; i < n; i++) v[i] = scene_view(scenes[i]);
+    if (n > scene_cap_) {
+        if (d_scenes_) {
+            cudaFree(d_scenes_);
+            owned_.erase(std::remove(owned_.begin(), owned_.end(), (void*)d_scenes_), owned_.end());
+        }
+        int32_t st = alloc(&d_scenes_, n, owned_);
+        if (st) return st;
+        scene_cap_ = n;
+        for (auto& g : graphs_) cudaGraphExecDestroy(g.exec);
+        graphs_.clear();
+    }
+    ECK(cudaMemcpy(d_scenes_, v.data(), n * sizeof(DeviceScene), cudaMemcpyHostToDevice), "upload scene table");
+    n_scenes_ = n;
+    return CVX_OK;
+}
+
+static bool same_out(const WaveOutputs& a, const WaveOutputs& b) { return std::memcmp(&a, &b, sizeof a) == 0; }
+
+int32_t WaveEngine::launch(const WaveOutputs& out, cudaStream_t stream) {
+    if (!use_graph_) {
+        ECK(launch_wave(d_jobs_, d_hdr_, d_scenes_, st_, out, packet_, blocks_per_sm_, stream), "wave launch");
+        return CVX_OK;
+    }
+    for (auto& g : graphs_)
+        if (same_out(g.out, out)) {
+            ECK(cudaGraphLaunch(g.exec, stream), "graph launch");
+            return CVX_OK;
+        }
+    cudaGraph_t graph;
+    ECK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal), "begin capture");
+    cudaError_t e = launch_wave(d_jobs_, d_hdr_, d_scenes_, st_, out, packet_, blocks_per_sm_, stream);
+    cudaError_t e2 = cudaStreamEndCapture(stream, &graph);
+    if (e != cudaSuccess) return cuda_err(e, "capture wave");
+    if (e2 != cudaSuccess) return cuda_err(e2, "end capture");
+    cudaGraphExec_t exec;
+    e = cudaGraphInstantiate(&exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) return cuda_err(e, "instantiate graph");
+    if (graphs_.size() >= 4) {
+        cudaGraphExecDestroy(graphs_.front().exec);
+        graphs_.erase(graphs_.begin());
+    }
+    graphs_.push_back(Graph{out, exec});
+    ECK(cudaGraphLaunch(exec, stream), "graph launch");
+    return CVX_OK;
+}
+
+int32_t WaveEngine::run(const std::vector<Job>& jobs_in, WaveOutputs out, cudaStream_t stream, uint64_t* rays,
+                        std::vector<uint64_t>* job_rays, float* ms) {
+    if (jobs_in.size() > max_jobs_) return set_error(CVX_ERR_CAPACITY, "too many jobs for one wave");
+    uint32_t groups = 0;
+    for (size_t i = 0; i < jobs_in.size(); i++) {
+        Job j = jobs_in[i];
+        j.group_base = groups;
+        j.n_groups = groups_of(j.w, j.h);
+        groups += j.n_groups;
+        h_jobs_[i] = j;
+    }
+    if (groups > max_groups_) return set_error(CVX_ERR_CAPACITY, "wave exceeds the ray-queue capacity");
+    h_hdr_->n_jobs = (uint32_t)jobs_in.size();
+    h_hdr_->n_groups = groups;
+    if (jobs_in.empty()) return CVX_OK;
+    out.rays = d_rays_;
+    out.job_rays = job_rays ? d_job_rays_ : nullptr;
+    out.err = d_err_;
+    ECK(cudaMemcpyAsync(d_jobs_, h_jobs_, jobs_in.size() * sizeof(Job), cudaMemcpyHostToDevice, stream),
+        "upload jobs");
+    ECK(cudaMemcpyAsync(d_hdr_, h_hdr_, sizeof(WaveHeader), cudaMemcpyHostToDevice, stream), "upload jobs");
+    ECK(cudaMemsetAsync(d_rays_, 0, 8, stream), "reset counters");
+    ECK(cudaMemsetAsync(d_err_, 0, 4, stream), "reset status");
+    if (job_rays) ECK(cudaMemsetAsync(d_job_rays_, 0, jobs_in.size() * 8, stream), "reset counters");
+    ECK(cudaEventRecord(e0_, stream), "event");
+    int32_t st = launch(out, stream);
+    if (st) return st;
+    ECK(cudaEventRecord(e1_, stream), "event");
+    unsigned long long r = 0;
+    uint32_t err = 0;
+    ECK(cudaMemcpyAsync(&r, d_rays_, 8, cudaMemcpyDeviceToHost, stream), "read counters");
+    ECK(cudaMemcpyAsync(&err, d_err_, 4, cudaMemcpyDeviceToHost, stream), "read status");
+    if (job_rays) {
+        job_rays->assign(jobs_in.size(), 0);
+        ECK(cudaMemcpyAsync(job_rays->data(), d_job_rays_, jobs_in.size() * 8, cudaMemcpyDeviceToHost, stream),
+            "read counters");
+    }
+    ECK(cudaStreamSynchronize(stream), "wave");
+    float t = 0.0f;
+    cudaEventElapsedTime(&t, e0_, e1_);
+    if (ms) *ms = t;
+    if (rays) *rays = r;
+    if (err) return set_error(CVX_ERR_DEVICE, "traversal stack overflow reported by the kernel");
+    return CVX_OK;
+}
+
+}  // namespace cvx
+
+using namespace cvx;
+
+// ---------------------------------------------------------------------------
+// Batch API
+
+struct cvx_batch {
+    std::vector<cvx_scene*> scenes;
+    WaveEngine engine;
+    uint64_t max_pixels = 0;
+    float* d_accum = nullptr;
+    uint32_t* d_rgba = nullptr;
+    ResolveItem* d_items = nullptr;
+    uint32_t max_items = 0;
+    cudaStream_t stream = nullptr;
+    ~cvx_batch() {
+        cudaFree(d_accum);
+        cudaFree(d_rgba);
+        cudaFree(d_items);
+        if (stream) cudaStreamDestroy(stream);
+    }
+};
+
+extern "C" int32_t cvx_batch_create(cvx_scene* const* scenes, uint32_t n_scenes, uint32_t max_groups,
+                                    uint64_t max_pixels, const cvx_render_config* cfg, cvx_batch** out) {
+    if (!scenes || !n_scenes || !out || !max_groups || !max_pixels)
+        return set_error(CVX_ERR_INVALID, "bad batch arguments");
+    cvx_render_config c{};
+    if (cfg) c = *cfg;
+    for (uint32_t i = 0; i < n_scenes; i++)
+        if (!scenes[i] || scene_num_lights(scenes[i]) == 0)
+            return set_error(CVX_ERR_INVALID, "every batch scene needs a direct-sample triangle");
+    std::unique_ptr<cvx_batch> b(new cvx_batch());
+    b->scenes.assign(scenes, scenes + n_scenes);
+    b->max_pixels = max_pixels;
+    ECK(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking), "cudaStreamCreate");
+    int32_t st = b->engine.init(max_groups, 4096, c.traversal == CVX_TRAVERSE_PACKET, c.use_graph != 0,
+                                c.block_size /* blocks per SM for the wave kernels */);
+    if (st) return st;
+    if ((st = b->engine.set_scenes(scenes, n_scenes))) return st;
+    std::vector<void*> owned;
+    if ((st = alloc(&b->d_accum, max_pixels * 3, owned))) return st;
+    if ((st = alloc(&b->d_rgba, max_pixels, owned))) return st;
+    b->max_items = 4096;
+    if ((st = alloc(&b->d_items, b->max_items, owned))) return st;
+    *out = b.release();
+    return CVX_OK;
+}
+
+extern "C" int32_t cvx_batch_render(cvx_batch* b, const cvx_view* views, uint32_t n, uint32_t* const* rgba,
+                                    uint64_t* rays_out, float* ms_out) {
+    if (!b || (!views && n)) return set_error(CVX_ERR_INVALID, "null argument");
+    if (n > b->max_items) return set_error(CVX_ERR_CAPACITY, "too many views in one batch call");
+    std::vector<uint64_t> offset(n);
+    uint64_t total = 0;
+    uint32_t max_spp = 0;
+    for (uint32_t i = 0; i < n; i++) {
+        const cvx_view& v = views[i];
+        if (v.scene >= b->scenes.size() || v.width == 0 || v.height == 0 || v.spp == 0)
+            return set_error(CVX_ERR_INVALID, "bad view");
+        if (groups_of(v.width, v.height) > b->engine.max_groups())
+            return set_error(CVX_ERR_CAPACITY, "a view is larger than the ray-queue capacity");
+        offset[i] = total;
+        total += (uint64_t)v.width * v.height;
+        max_spp = std::max(max_spp, v.spp);
+    }
+    if (total > b->max_pixels) return set_error(CVX_ERR_CAPACITY, "views exceed the batch framebuffer");
+    ECK(cudaMemsetAsync(b->d_accum, 0, total * 12, b->stream), "clear accumulator");
+    uint64_t rays = 0;
+    float ms = 0.0f;
+    WaveOutputs out{};
+    out.accum = b->d_accum;
+    for (uint32_t s = 0; s < max_spp; s++) {
+        std::vector<Job> jobs;
+        uint32_t groups = 0;
+        auto flush = [&]() -> int32_t {
+            uint64_t r = 0;
+            float t = 0.0f;
+            int32_t st = b->engine.run(jobs, out, b->stream, &r, nullptr, &t);
+            rays += r;
+            ms += t;
+            jobs.clear();
+            groups = 0;
+            return st;
+        };
+        for (uint32_t i = 0; i < n; i++) {
+            const cvx_view& v = views[i];
+            if (v.spp <= s) continue;
+            uint32_t g = groups_of(v.width, v.height);
+            if (groups + g > b->engine.max_groups() || jobs.size() == b->engine.max_jobs()) {
+                int32_t st = flush();
+                if (st) return st;
+            }
+            Job j{};
+            std::memcpy(&j.cam, &v.camera, sizeof(cvx_camera));
+            j.scene = v.scene;
+            j.w = v.width;
+            j.h = v.height;
+            j.frame = v.frame_base + s;
+            j.out_offset = offset[i];
+            jobs.push_back(j);
+            groups += g;
+        }
+        if (!jobs.empty()) {
+            int32_t st = flush();
+            if (st) return st;
+        }
+    }
+    std::vector<ResolveItem> items(n);
+    for (uint32_t i = 0; i < n; i++)
+        items[i] = ResolveItem{offset[i], views[i].width * views[i].height, 1.0f / (float)views[i].spp};
+    ECK(cudaMemcpyAsync(b->d_items, items.data(), n * sizeof(ResolveItem), cudaMemcpyHostToDevice, b->stream),
+        "upload resolve list");
+    ECK(launch_resolve_multi(b->d_items, n, b->d_accum, b->d_rgba, b->stream), "resolve");
+    if (rgba)
+        for (uint32_t i = 0; i < n; i++)
+            if (rgba[i])
+                ECK(cudaMemcpyAsync(rgba[i], b->d_rgba + offset[i], (size_t)items[i].npx * 4, cudaMemcpyDeviceToHost,
+                                    b->stream),
+                    "copy image");
+    ECK(cudaStreamSynchronize(b->stream), "batch");
+    if (rays_out) *rays_out = rays;
+    if (ms_out) *ms_out = ms;
+    return CVX_OK;
+}
+
+extern "C" void cvx_batch_destroy(cvx_batch* b) { delete b; }
+
+// ---------------------------------------------------------------------------
+// Request server
+
+namespace {
+
+using Clock = std::chrono::steady_clock;
+
+struct Request {
+    uint64_t id = 0;
+    cvx_request r{};
+    uint32_t* host_rgba = nullptr;
+    uint64_t npx = 0;
+    uint32_t groups = 0;
+    uint64_t offset = 0;  // pixel offset in the framebuffer pool
+    uint32_t next_sample = 0;
+    bool admitted = false, finished = false, cancelled = false;
+    cvx_request_result res{};
+};
+
+// First-fit allocator over pixel ranges of the framebuffer pool.
+struct RangeAlloc {
+    std::map<uint64_t, uint64_t> free_;  // offset -> length
+    void init(uint64_t n) { free_ = {{0, n}}; }
+    bool take(uint64_t n, uint64_t* off) {
+        for (auto it = free_.begin(); it != free_.end(); ++it)
+            if (it->second >= n) {
+                *off = it->first;
+                uint64_t rest = it->second - n, at = it->first + n;
+                free_.erase(it);
+                if (rest) free_[at] = rest;
+                return true;
+            }
+        return false;
+    }
+    void give(uint64_t off, uint64_t n) {
+        auto it = free_.emplace(off, n).first;
+        auto nx = std::next(it);
+        if (nx != free_.end() && it->first + it->second == nx->first) {
+            it->second += nx->second;
+            free_.erase(nx);
+        }
+        if (it != free_.begin()) {
+            auto pv = std::prev(it);
+            if (pv->first + pv->second == it->first) {
+                pv->second += it->second;
+                free_.erase(it);
+            }
+        }
+    }
+};
+
+}  // namespace
+
+struct cvx_server {
+    std::vector<cvx_scene*> scenes;
+    cvx_server_config cfg{};
+    WaveEngine engine;
+    float* d_accum = nullptr;
+    uint32_t* d_rgba = nullptr;
+    ResolveItem* d_items = nullptr;
+    uint64_t pool_px = 0;
+    RangeAlloc pool;
+    cudaStream_t stream = nullptr;
+    std::mutex mu;
+    std::condition_variable cv, done_cv;
+    std::deque<std::shared_ptr<Request>> pending;
+    std::vector<std::shared_ptr<Request>> admitted;
+    std::unordered_map<uint64_t, std::shared_ptr<Request>> all;
+    uint64_t next_id = 1;
+    uint32_t admitted_groups = 0;
+    bool stop = false;
+    std::thread worker;
+    Clock::time_point t0 = Clock::now();
+    std::atomic<uint64_t> waves{0}, rays{0};
+    double busy_s = 0.0;
+    int32_t fatal = CVX_OK;
+    std::string fatal_msg;
+
+    double now() const { return std::chrono::duration<double>(Clock::now() - t0).count(); }
+
+    void finish(const std::shared_ptr<Request>& q, int32_t status) {
+        q->finished = true;
+        q->res.status = status;
+        q->res.done_s = now();
+        if (q->admitted) {
+            pool.give(q->offset, q->npx);
+            admitted_groups -= q->groups;
+            q->admitted = false;
+        }
+    }
+
+    void loop() {
+        std::vector<Job> jobs;
+        std::vector<std::shared_ptr<Request>> wave;
+        std::vector<uint64_t> job_rays;
+        for (;;) {
+            {
+                std::unique_lock<std::mutex> lk(mu);
+                cv.wait(lk, [&] { return stop || !pending.empty() || !admitted.empty(); });
+                if (stop) return;
+                // Admission, FIFO: stop at the first request that does not fit.
+                while (!pending.empty()) {
+                    auto& q = pending.front();
+                    if (cfg.sequential && !admitted.empty()) break;
+                    uint64_t off = 0;
+                    if (admitted_groups + q->groups > engine.max_groups() || admitted.size() >= engine.max_jobs() ||
+                        !pool.take(q->npx, &off))
+                        break;
+                    q->offset = off;
+                    q->admitted = true;
+                    q->res.start_s = now();
+                    admitted_groups += q->groups;
+                    admitted.push_back(q);
+                    pending.pop_front();
+                }
+                for (auto it = admitted.begin(); it != admitted.end();) {
+                    if ((*it)->cancelled) {
+                        finish(*it, CVX_ERR_CANCELLED);
+                        it = admitted.erase(it);
+                    } else {
+                        ++it;
+                    }
+                }
+                done_cv.notify_all();
+                wave = admitted;
+            }
+            if (wave.empty()) continue;
+            jobs.clear();
+            for (auto& q : wave) {
+                Job j{};
+                std::memcpy(&j.cam, &q->r.camera, sizeof(cvx_camera));
+                j.scene = q->r.scene;
+                j.w = q->r.width;
+                j.h = q->r.height;
+                j.frame = q->r.frame_base + q->next_sample;
+                j.out_offset = q->offset;
+                jobs.push_back(j);
+            }
+            // A request's accumulator starts at zero with its first sample.
+            for (auto& q : wave)
+                if (q->next_sample == 0) cudaMemsetAsync(d_accum + 3 * q->offset, 0, q->npx * 12, stream);
+            WaveOutputs out{};
+            out.accum = d_accum;
+            uint64_t r = 0;
+            float ms = 0.0f;
+            int32_t st = engine.run(jobs, out, stream, &r, &job_rays, &ms);
+            std::vector<std::shared_ptr<Request>> done;
+            std::vector<ResolveItem> items;
+            {
+                std::lock_guard<std::mutex> lk(mu);
+                waves++;
+                rays += r;
+                busy_s += ms * 1e-3;
+                for (size_t i = 0; i < wave.size(); i++) {
+                    auto& q = wave[i];
+                    if (st) {
+                        if (!q->finished) {
+                            finish(q, st);
+                            admitted.erase(std::find(admitted.begin(), admitted.end(), q));
+                        }
+                        continue;
+                    }
+                    q->res.rays += job_rays.empty() ? 0 : job_rays[i];
+                    q->next_sample++;
+                    if (q->next_sample == q->r.spp && !q->cancelled) {
+                        done.push_back(q);
+                        items.push_back(ResolveItem{q->offset, (uint32_t)q->npx, 1.0f / (float)q->r.spp});
+                    }
+                }
+                if (st) {
+                    char buf[256];
+                    cvx_last_error(buf, sizeof buf);
+                    fatal_msg = buf;
+                }
+            }
+            if (!done.empty()) {
+                cudaError_t e = cudaMemcpyAsync(d_items, items.data(), items.size() * sizeof(ResolveItem),
+                                                cudaMemcpyHostToDevice, stream);
+                if (e == cudaSuccess) e = launch_resolve_multi(d_items, (uint32_t)items.size(), d_accum, d_rgba, stream);
+                for (auto& q : done)
+                    if (e == cudaSuccess && q->host_rgba)
+                        e = cudaMemcpyAsync(q->host_rgba, d_rgba + q->offset, q->npx * 4, cudaMemcpyDeviceToHost,
+                                            stream);
+                if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+                std::lock_guard<std::mutex> lk(mu);
+                for (auto& q : done) {
+                    finish(q, e == cudaSuccess ? CVX_OK : CVX_ERR_CUDA);
+                    admitted.erase(std::find(admitted.begin(), admitted.end(), q));
+                }
+                done_cv.notify_all();
+            } else if (st) {
+                std::lock_guard<std::mutex> lk(mu);
+                done_cv.notify_all();
+            }
+        }
+    }
+
+    ~cvx_server() {
+        {
+            std::lock_guard<std::mutex> lk(mu);
+            stop = true;
+        }
+        cv.notify_all();
+        if (worker.joinable()) worker.join();
+        cudaFree(d_accum);
+        cudaFree(d_rgba);
+        cudaFree(d_items);
+        if (stream) cudaStreamDestroy(stream);
+    }
+};
+
+extern "C" int32_t cvx_server_create(cvx_scene* const* scenes, uint32_t n_scenes, const cvx_server_config* cfg,
+                                     cvx_server** out) {
+    if (!scenes || !n_scenes || !cfg || !out) return set_error(CVX_ERR_INVALID, "null argument");
+    if (cfg->max_groups == 0 || cfg->framebuffer_bytes < 16) return set_error(CVX_ERR_INVALID, "empty budget");
+    for (uint32_t i = 0; i < n_scenes; i++)
+        if (!scenes[i] || scene_num_lights(scenes[i]) == 0)
+            return set_error(CVX_ERR_INVALID, "every served scene needs a direct-sample triangle");
+    std::unique_ptr<cvx_server> s(new cvx_server());
+    s->scenes.assign(scenes, scenes + n_scenes);
+    s->cfg = *cfg;
+    ECK(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking), "cudaStreamCreate");
+    int32_t st = s->engine.init(cfg->max_groups, 1024, cfg->traversal == CVX_TRAVERSE_PACKET, cfg->use_graph != 0, 0);
+    if (st) return st;
+    if ((st = s->engine.set_scenes(scenes, n_scenes))) return st;
+    s->pool_px = cfg->framebuffer_bytes / 16;  // 12 B accumulator + 4 B RGBA per pixel
+    std::vector<void*> owned;
+    if ((st = alloc(&s->d_accum, s->pool_px * 3, owned))) return st;
+    if ((st = alloc(&s->d_rgba, s->pool_px, owned))) return st;
+    if ((st = alloc(&s->d_items, 1024, owned))) return st;
+    s->pool.init(s->pool_px);
+    s->worker = std::thread([p = s.get()] { p->loop(); });
+    *out = s.release();
+    return CVX_OK;
+}
+
+extern "C" int32_t cvx_server_submit(cvx_server* s, const cvx_request* req, uint32_t* rgba, uint64_t* id) {
+    if (!s || !req || !id) return set_error(CVX_ERR_INVALID, "null argument");
+    if (req->scene >= s->scenes.size() || req->width == 0 || req->height == 0 || req->spp == 0)
+        return set_error(CVX_ERR_INVALID, "bad request");
+    auto q = std::make_shared<Request>();
+    q->r = *req;
+    q->host_rgba = rgba;
+    q->npx = (uint64_t)req->width * req->height;
+    q->groups = groups_of(req->width, req->height);
+    if (q->npx > s->pool_px || q->groups > s->engine.max_groups())
+        return set_error(CVX_ERR_CAPACITY, "request larger than the server's framebuffer or ray-queue budget");
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        q->id = s->next_id++;
+        q->res.submit_s = s->now();
+        s->pending.push_back(q);
+        s->all[q->id] = q;
+        *id = q->id;
+    }
+    s->cv.notify_all();
+    return CVX_OK;
+}
+
+extern "C" int32_t cvx_server_wait(cvx_server* s, uint64_t id, uint32_t timeout_ms, cvx_request_result* result) {
+    if (!s) return set_error(CVX_ERR_INVALID, "null server");
+    std::unique_lock<std::mutex> lk(s->mu);
+    auto it = s->all.find(id);
+    if (it == s->all.end()) return set_error(CVX_ERR_NOT_FOUND, "unknown request id");
+    auto q = it->second;
+    if (!q->finished)
+        s->done_cv.wait_for(lk, std::chrono::milliseconds(timeout_ms), [&] { return q->finished; });
+    if (!q->finished) return set_error(CVX_ERR_TIMEOUT, "request not finished");
+    if (result) *result = q->res;
+    s->all.erase(id);
+    return CVX_OK;
+}
+
+extern "C" int32_t cvx_server_cancel(cvx_server* s, uint64_t id) {
+    if (!s) return set_error(CVX_ERR_INVALID, "null server");
+    std::lock_guard<std::mutex> lk(s->mu);
+    auto it = s->all.find(id);
+    if (it == s->all.end()) return set_error(CVX_ERR_NOT_FOUND, "unknown request id");
+    auto q = it->second;
+    if (q->finished) return CVX_OK;
+    q->cancelled = true;
+    auto p = std::find(s->pending.begin(), s->pending.end(), q);
+    if (p != s->pending.end()) {
+        s->pending.erase(p);
+        s->finish(q, CVX_ERR_CANCELLED);
+        s->done_cv.notify_all();
+    }
+    s->cv.notify_all();
+    return CVX_OK;
+}
+
+extern "C" int32_t cvx_server_stats(cvx_server* s, double* now_s, uint64_t* waves, uint64_t* rays, double* busy_s) {
+    if (!s) return set_error(CVX_ERR_INVALID, "null server");
+    std::lock_guard<std::mutex> lk(s->mu);
+    if (now_s) *now_s = s->now();
+    if (waves) *waves = s->waves;
+    if (rays) *rays = s->rays;
+    if (busy_s) *busy_s = s->busy_s;
+    return CVX_OK;
+}
+
+extern "C" void cvx_server_destroy(cvx_server* s) { delete s; }

@@ -1,0 +1,52 @@
+// Host class of the wavefront engine (engine.cu).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <vector>
+
+#include "../../include/convector_gpu.h"
+#include "layout.cuh"
+#include "wavefront.cuh"
+
+namespace cvx {
+
+DeviceScene scene_view(const cvx_scene* s);
+uint32_t scene_num_lights(const cvx_scene* s);
+uint32_t groups_of(uint32_t w, uint32_t h);
+
+class WaveEngine {
+   public:
+    ~WaveEngine();
+    // max_groups: ray-queue capacity (8-pixel groups) of one wave.
+    int32_t init(uint32_t max_groups, uint32_t max_jobs, bool packet, bool use_graph, uint32_t blocks_per_sm);
+    int32_t set_scenes(cvx_scene* const* scenes, uint32_t n);
+    // Runs one wave synchronously on `stream`; group_base / n_groups of the
+    // jobs are filled in here. rays, job_rays and ms may be null.
+    int32_t run(const std::vector<Job>& jobs, WaveOutputs out, cudaStream_t stream, uint64_t* rays,
+                std::vector<uint64_t>* job_rays, float* ms);
+    uint32_t max_groups() const { return max_groups_; }
+    uint32_t max_jobs() const { return max_jobs_; }
+
+   private:
+    int32_t launch(const WaveOutputs& out, cudaStream_t stream);
+    struct Graph {
+        WaveOutputs out;
+        cudaGraphExec_t exec;
+    };
+    WaveState st_{};
+    Job* d_jobs_ = nullptr;
+    Job* h_jobs_ = nullptr;
+    WaveHeader* d_hdr_ = nullptr;
+    WaveHeader* h_hdr_ = nullptr;
+    DeviceScene* d_scenes_ = nullptr;
+    unsigned long long* d_rays_ = nullptr;
+    unsigned long long* d_job_rays_ = nullptr;
+    uint32_t* d_err_ = nullptr;
+    uint32_t n_scenes_ = 0, scene_cap_ = 0, max_groups_ = 0, max_jobs_ = 0, blocks_per_sm_ = 0;
+    bool packet_ = false, use_graph_ = false;
+    std::vector<void*> owned_;
+    std::vector<Graph> graphs_;
+    cudaEvent_t e0_ = nullptr, e1_ = nullptr;
+};
+
+}  // namespace cvx

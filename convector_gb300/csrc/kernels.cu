@@ -98,6 +98,42 @@ __global__ void __launch_bounds__(256) k_intersect(DeviceScene s, const float* _
     }
 }
 
+// Ray source of the isolated nearest-hit query: SoA rays in, (t, index) out.
+struct SoaRays {
+    const float4* nodes;
+    const float4* geom;
+    const float* rays;
+    uint32_t n;
+    float far_dist;
+    float* t_out;
+    int32_t* tri_out;
+    uint32_t* counters;
+    __device__ __forceinline__ bool load(uint32_t r, F3& o, F3& d, float& far, const float4*& nd,
+                                         const float4*& gm) const {
+        nd = nodes;
+        gm = geom;
+        o = f3(__ldg(rays + r), __ldg(rays + n + r), __ldg(rays + 2 * n + r));
+        d = f3(__ldg(rays + 3 * n + r), __ldg(rays + 4 * n + r), __ldg(rays + 5 * n + r));
+        far = far_dist;
+        return true;
+    }
+    __device__ __forceinline__ void store(uint32_t r, const Hit& h, uint32_t na, uint32_t nt) const {
+        t_out[r] = h.t;
+        tri_out[r] = h.tri;
+        if (counters) {
+            counters[r] = na;
+            counters[n + r] = nt;
+        }
+    }
+};
+
+__global__ void __launch_bounds__(128) k_intersect_refill(SoaRays src, uint32_t* __restrict__ next_ray,
+                                                          uint32_t* __restrict__ err) {
+    __shared__ ApproxTables tab;
+    load_tables(tab);
+    if (!traverse_refill(src, src.n, next_ray, tab)) atomicOr(err, kErrStackOverflow);
+}
+
 // ---------------------------------------------------------------------------
 // Frame rendering: one octet renders one 8-pixel group (RNG_GROUP), or walks
 // the 128 groups of one 32x32 patch in the reference's order (RNG_PATCH).
@@ -274,6 +310,18 @@ cudaError_t launch_prep_lights(const cvx_triangle* tris, const uint32_t* ds, uin
 cudaError_t launch_intersect(const DeviceScene& s, const float* rays, uint32_t n, float far_dist, bool packet,
                              float* t_out, int32_t* tri_out, uint32_t* counters, uint32_t* err, uint32_t block,
                              uint32_t blocks_per_sm, cudaStream_t st) {
+    if (!packet) {
+        // persistent ray-refill kernel; err[1] is its ray counter
+        cudaError_t e = cudaMemsetAsync(err + 1, 0, 4, st);
+        if (e != cudaSuccess) return e;
+        uint32_t bps = blocks_per_sm ? blocks_per_sm : 10;
+        uint32_t blocks = (uint32_t)num_sms() * bps;
+        uint32_t need = (n + 127u) / 128u;
+        if (blocks > need) blocks = need;
+        SoaRays src{s.nodes, s.geom, rays, n, far_dist, t_out, tri_out, counters};
+        k_intersect_refill<<<blocks, 128, 0, st>>>(src, err + 1, err);
+        return cudaGetLastError();
+    }
     if (block == 0) block = 128;
     if (blocks_per_sm == 0) blocks_per_sm = 8;
     uint32_t need = ((n + 7u) & ~7u) / block + 1u;

@@ -4,10 +4,12 @@
 
 #include "../../include/convector_gpu.h"
 #include "layout.cuh"
+#include "wavefront.cuh"
 
 namespace cvx {
 
 cudaError_t upload_tables(const uint16_t* rcp, const uint16_t* rsqrt);
+cudaError_t upload_tables_wave(const uint16_t* rcp, const uint16_t* rsqrt);
 cudaError_t launch_prep_geom(const cvx_triangle* tris, uint32_t n, float4* geom, TriShade* shade, cudaStream_t st);
 cudaError_t launch_prep_lights(const cvx_triangle* tris, const uint32_t* ds, uint32_t n, float4* lights,
                                cudaStream_t st);
@@ -18,5 +20,9 @@ cudaError_t launch_render(const DeviceScene& s, const DeviceCamera& cam, uint32_
                           bool packet, bool patch_order, uint32_t* rgba, uint32_t* gbuf, float* color, float* accum,
                           unsigned long long* rays, uint32_t* err, uint32_t block, cudaStream_t st);
 cudaError_t launch_resolve(const float* accum, uint32_t npx, float factor, uint32_t* rgba, cudaStream_t st);
+cudaError_t launch_wave(const Job* jobs, const WaveHeader* hdr, const DeviceScene* scenes, const WaveState& st,
+                        const WaveOutputs& out, bool packet, uint32_t blocks_per_sm, cudaStream_t stream);
+cudaError_t launch_resolve_multi(const ResolveItem* items, uint32_t n_items, const float* accum, uint32_t* rgba,
+                                 cudaStream_t stream);
 
 }  // namespace cvx

@@ -39,6 +39,16 @@ struct LaneRng {
         s *= f;
         return v;
     }
+    // Resumes lane `lane` of a generator from its saved 64-bit state.
+    __device__ __forceinline__ void resume(uint64_t state, int lane) {
+        int k = lane >> 1;
+        f = k == 0 ? 3ull * 1073243692214514217ull
+          : k == 1 ? 5ull * 3335100457702756523ull
+          : k == 2 ? 7ull * 8789056573444181ull
+                   : 11ull * 781436371140792079ull;
+        s = state;
+        hi = (uint32_t)(lane & 1);
+    }
 };
 __device__ __forceinline__ float unit_from(uint32_t u) { return fmaf((float)(int32_t)u, 0.5f / -2147483648.0f, 0.5f); }
 __device__ __forceinline__ float biunit_from(uint32_t u) { return (float)(int32_t)u * (1.0f / -2147483648.0f); }

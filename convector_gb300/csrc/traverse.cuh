@@ -138,4 +138,101 @@ __device__ __forceinline__ bool traverse(const DeviceScene& s, F3 o, F3 d, bool 
     return ok;
 }
 
+// Persistent single-ray traversal with ray refill over rays 0..n-1 of `src`.
+// Every iteration each lane pops one stack entry and processes it (a node
+// pair or a leaf); a lane whose ray is finished takes the next unclaimed ray
+// (one warp-aggregated atomic on `next_ray`), so warps stay full while rays of
+// different lengths finish. Per-ray decisions are exactly those of
+// traverse<false>. The whole warp must call this. `src` provides
+//   bool load(r, F3& o, F3& d, float& far, const float4*& nodes, const float4*& geom)
+//        (false: nothing to trace for r; load then stores r's result itself)
+//   void store(r, const Hit&, uint32_t boxes, uint32_t triangles)
+// Returns false if a ray overflowed the stack (its hit is then incomplete).
+template <class Src>
+__device__ __forceinline__ bool traverse_refill(const Src& src, uint32_t n, uint32_t* next_ray,
+                                                const ApproxTables& tab) {
+    const float4* nodes = nullptr;
+    const float4* geom = nullptr;
+    const int lane = threadIdx.x & 31;
+    uint32_t st_idx[kStackDepth];
+    uint32_t st_len[kStackDepth];
+    float st_t[kStackDepth];
+    int sp = 0;
+    uint32_t ray = 0, na = 0, nt = 0, pair = 0;
+    bool have = false, done = false, overflow = false, pending_pair = false;
+    F3 o = f3(0, 0, 0), d = f3(0, 0, 0), inv = f3(0, 0, 0);
+    Hit h{0.0f, 0.0f, 0.0f, -1};
+    for (;;) {
+        bool want = !have && !done;
+        unsigned b = __ballot_sync(0xffffffffu, want);
+        if (b) {
+            uint32_t base = 0;
+            int first = __ffs(b) - 1;
+            if (lane == first) base = atomicAdd(next_ray, (uint32_t)__popc(b));
+            base = __shfl_sync(0xffffffffu, base, first);
+            if (want) {
+                uint32_t r = base + __popc(b & ((1u << lane) - 1u));
+                if (r < n) {
+                    float far;
+                    ray = r;
+                    if (src.load(r, o, d, far, nodes, geom)) {
+                        inv = f3(x_rcp(d.x, tab), x_rcp(d.y, tab), x_rcp(d.z, tab));
+                        h = Hit{far, 0.0f, 0.0f, -1};
+                        sp = 0;
+                        na = 2;
+                        nt = 0;
+                        pair = 0;
+                        pending_pair = true;
+                        have = true;
+                    }
+                } else {
+                    done = true;
+                }
+            }
+        }
+        if (__all_sync(0xffffffffu, done)) break;
+        if (!have) continue;
+        if (!pending_pair) {
+            if (sp == 0) {
+                src.store(ray, h, na, nt);
+                have = false;
+                continue;
+            }
+            sp--;
+            uint32_t idx = st_idx[sp], len = st_len[sp];
+            if (geq(st_t[sp], h.t)) continue;
+            if (len != 0u) {
+                for (uint32_t i = idx; i < idx + len; i++) tri_test(geom, i, o, d, true, h);
+                nt += len;
+                continue;
+            }
+            na += 2;
+            pair = idx >> 1;
+        }
+        pending_pair = false;
+        const float4* np = nodes + 4 * pair;
+        float4 q0 = __ldg(np), q1 = __ldg(np + 1), q2 = __ldg(np + 2), q3 = __ldg(np + 3);
+        BoxT b0 = box_test(q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, o, inv);
+        BoxT b1 = box_test(q1.z, q1.w, q2.x, q2.y, q2.z, q2.w, o, inv);
+        bool first0 = !sneg(b0.tmin - b1.tmin);
+        bool hit0 = b0.mask & !sneg(b0.tmax);
+        bool hit1 = b1.mask & !sneg(b1.tmax);
+        if (sp + (int)hit0 + (int)hit1 > kStackDepth) {
+            overflow = true;
+            sp = 0;
+            continue;
+        }
+        uint32_t i0 = __float_as_uint(q3.x), l0 = __float_as_uint(q3.y);
+        uint32_t i1 = __float_as_uint(q3.z), l1 = __float_as_uint(q3.w);
+        if (first0) {
+            if (hit0) { st_idx[sp] = i0; st_len[sp] = l0; st_t[sp] = b0.tmin; sp++; }
+            if (hit1) { st_idx[sp] = i1; st_len[sp] = l1; st_t[sp] = b1.tmin; sp++; }
+        } else {
+            if (hit1) { st_idx[sp] = i1; st_len[sp] = l1; st_t[sp] = b1.tmin; sp++; }
+            if (hit0) { st_idx[sp] = i0; st_len[sp] = l0; st_t[sp] = b0.tmin; sp++; }
+        }
+    }
+    return !overflow;
+}
+
 }  // namespace cvx

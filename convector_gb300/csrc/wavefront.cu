@@ -1,0 +1,340 @@
+// Wavefront kernels (see wavefront.cuh). All three are persistent: a fixed
+// grid walks the queue whose length it reads from device memory, so the whole
+// bounce loop of a wave is a fixed sequence of launches that a CUDA graph can
+// replay. Compiled with -fmad=false (x86sem.cuh).
+#include <cuda_runtime.h>
+
+#include "kernels.h"
+#include "shade.cuh"
+#include "wavefront.cuh"
+
+namespace cvx {
+
+// This translation unit's copy of the approximation tables (device globals
+// are per translation unit without relocatable device code).
+__device__ ApproxTables g_tables_wf;
+
+cudaError_t upload_tables_wave(const uint16_t* rcp, const uint16_t* rsqrt) {
+    ApproxTables t;
+    for (int i = 0; i < 2048; i++) {
+        t.rcp[i] = rcp[i];
+        t.rsqrt[i] = rsqrt[i];
+    }
+    return cudaMemcpyToSymbol(g_tables_wf, &t, sizeof t);
+}
+
+__device__ __forceinline__ void load_tables_wf(ApproxTables& sm) {
+    const uint32_t* src = reinterpret_cast<const uint32_t*>(&g_tables_wf);
+    uint32_t* dst = reinterpret_cast<uint32_t*>(&sm);
+    for (int i = threadIdx.x; i < (int)(sizeof(ApproxTables) / 4); i += blockDim.x) dst[i] = src[i];
+    __syncthreads();
+}
+
+// Appends `gi` for every octet leader whose `keep` is set; one atomic per
+// converged set of threads.
+__device__ __forceinline__ void enqueue_octets(bool leader_keep, uint32_t gi, uint32_t* queue, uint32_t* count) {
+    unsigned m = __activemask();
+    unsigned b = __ballot_sync(m, leader_keep);
+    if (!b) return;
+    int lane = threadIdx.x & 31;
+    int first = __ffs(m) - 1;
+    uint32_t base = 0;
+    if (lane == first) base = atomicAdd(count, (uint32_t)__popc(b));
+    base = __shfl_sync(m, base, first);
+    if (leader_keep) queue[base + __popc(b & ((1u << lane) - 1u))] = gi;
+}
+
+__device__ __forceinline__ uint32_t find_job(const Job* jobs, uint32_t n_jobs, uint32_t gi) {
+    uint32_t lo = 0, hi = n_jobs;
+    while (hi - lo > 1) {
+        uint32_t mid = (lo + hi) >> 1;
+        if (__ldg(&jobs[mid].group_base) <= gi) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
+// Pixel origin of group `local` of a job (octet order of k_render_group).
+__device__ __forceinline__ void group_origin(const Job& j, uint32_t local, uint32_t* xb, uint32_t* yb, int* g,
+                                             uint32_t* gx, uint32_t* gy) {
+    uint32_t bw = (j.w + 15u) / 16u, blk = local >> 3;
+    *g = (int)(local & 7u);
+    *xb = (blk % bw) * 16u;
+    *yb = (blk / bw) * 4u;
+    *gx = *xb + 4u * (uint32_t)(*g >> 1);
+    *gy = *yb + 2u * (uint32_t)(*g & 1);
+}
+
+__device__ __forceinline__ void block_coord_wf(uint32_t w, uint32_t h, uint32_t xb, uint32_t yb, int g, int k,
+                                               float* x, float* y, float* scale_out) {
+    float scale = 2.0f / (float)w;
+    float s2 = 2.0f * scale, s4 = 4.0f * scale, s8 = 8.0f * scale, s12 = 12.0f * scale;
+    float bx = scale * ((float)(k & 3) + ((float)xb - (float)w * 0.5f));
+    float by = scale * ((float)(k >> 2) + ((float)yb - (float)h * 0.5f));
+    int col = g >> 1;
+    *x = col == 0 ? bx : col == 1 ? bx + s4 : col == 2 ? bx + s8 : bx + s12;
+    *y = (g & 1) ? by + s2 : by;
+    *scale_out = scale;
+}
+
+__global__ void __launch_bounds__(128) k_wf_raygen(const Job* __restrict__ jobs, const WaveHeader* __restrict__ hdr,
+                                                   WaveState st) {
+    __shared__ ApproxTables tab;
+    load_tables_wf(tab);
+    const int k = threadIdx.x & 7;
+    const uint32_t n_groups = hdr->n_groups, n_jobs = hdr->n_jobs;
+    const uint32_t octets = (gridDim.x * blockDim.x) >> 3;
+    for (uint32_t gi = (blockIdx.x * blockDim.x + threadIdx.x) >> 3; gi < n_groups; gi += octets) {
+        uint32_t ji = find_job(jobs, n_jobs, gi);
+        const Job& j = jobs[ji];
+        uint32_t xb, yb, gx, gy;
+        int g;
+        group_origin(j, gi - j.group_base, &xb, &yb, &g, &gx, &gy);
+        bool inside = gx < j.w && gy < j.h;
+        if (inside) {
+            float x, y, scale;
+            block_coord_wf(j.w, j.h, xb, yb, g, k, &x, &y, &scale);
+            LaneRng rng;
+            rng.seed(gx, gy, j.frame, k);
+            x = fmaf(unit_from(rng.next()), scale, x);
+            y = fmaf(unit_from(rng.next()), scale, y);
+            F3 o, d;
+            camera_ray(j.cam, x, y, unit_from(rng.next()), tab, o, d);
+            size_t l = (size_t)gi * 8 + k;
+            st.ox[l] = o.x;
+            st.oy[l] = o.y;
+            st.oz[l] = o.z;
+            st.dx[l] = d.x;
+            st.dy[l] = d.y;
+            st.dz[l] = d.z;
+            st.cr[l] = 1.0f;
+            st.cg[l] = 1.0f;
+            st.cb[l] = 1.0f;
+            st.rng[l] = rng.s;
+            st.gbuf[l] = 0u;
+            st.flags[l] = 1u;
+            if (k == 0) st.group_job[gi] = ji;
+        }
+        enqueue_octets(k == 0 && inside, gi, st.queue[0], &st.counts[0]);
+    }
+}
+
+// Packet traversal: one octet per queued group, decisions over the octet.
+__global__ void __launch_bounds__(128) k_wf_traverse_packet(const Job* __restrict__ jobs,
+                                                            const DeviceScene* __restrict__ scenes, WaveState st,
+                                                            int bounce, WaveOutputs out) {
+    __shared__ ApproxTables tab;
+    load_tables_wf(tab);
+    const int k = threadIdx.x & 7;
+    const unsigned omask = 0xffu << (threadIdx.x & 24u);
+    const uint32_t n = st.counts[bounce];
+    const uint32_t* queue = st.queue[bounce & 1];
+    const uint32_t octets = (gridDim.x * blockDim.x) >> 3;
+    bool ok = true;
+    for (uint32_t qi = (blockIdx.x * blockDim.x + threadIdx.x) >> 3; qi < n; qi += octets) {
+        uint32_t gi = queue[qi];
+        size_t l = (size_t)gi * 8 + k;
+        const DeviceScene s = scenes[jobs[st.group_job[gi]].scene];
+        bool active = (st.flags[l] & 1u) != 0u;
+        F3 o = f3(st.ox[l], st.oy[l], st.oz[l]), d = f3(st.dx[l], st.dy[l], st.dz[l]);
+        Hit h{1.0e5f, 0.0f, 0.0f, -1};
+        ok &= traverse<true>(s, o, d, active, omask, h, tab, nullptr);
+        st.ht[l] = h.t;
+        st.hu[l] = h.u;
+        st.hv[l] = h.v;
+        st.htri[l] = h.tri;
+    }
+    if (!ok) atomicOr(out.err, kErrStackOverflow);
+}
+
+// Single-ray traversal over the lanes of the queued groups, with ray refill
+// (traverse_refill): ray r is lane r % 8 of queue entry r / 8.
+struct QueueRays {
+    const Job* jobs;
+    const DeviceScene* scenes;
+    WaveState st;
+    const uint32_t* queue;
+    __device__ __forceinline__ bool load(uint32_t r, F3& o, F3& d, float& far, const float4*& nodes,
+                                         const float4*& geom) const {
+        uint32_t gi = queue[r >> 3];
+        size_t l = (size_t)gi * 8 + (r & 7u);
+        if (!(st.flags[l] & 1u)) {
+            st.ht[l] = 1.0e5f;
+            st.hu[l] = 0.0f;
+            st.hv[l] = 0.0f;
+            st.htri[l] = -1;
+            return false;
+        }
+        const DeviceScene* s = scenes + jobs[st.group_job[gi]].scene;
+        nodes = s->nodes;
+        geom = s->geom;
+        o = f3(st.ox[l], st.oy[l], st.oz[l]);
+        d = f3(st.dx[l], st.dy[l], st.dz[l]);
+        far = 1.0e5f;
+        return true;
+    }
+    __device__ __forceinline__ void store(uint32_t r, const Hit& h, uint32_t, uint32_t) const {
+        size_t l = (size_t)queue[r >> 3] * 8 + (r & 7u);
+        st.ht[l] = h.t;
+        st.hu[l] = h.u;
+        st.hv[l] = h.v;
+        st.htri[l] = h.tri;
+    }
+};
+
+__global__ void __launch_bounds__(128) k_wf_traverse_single(const Job* __restrict__ jobs,
+                                                            const DeviceScene* __restrict__ scenes, WaveState st,
+                                                            int bounce, WaveOutputs out) {
+    __shared__ ApproxTables tab;
+    load_tables_wf(tab);
+    QueueRays src{jobs, scenes, st, st.queue[bounce & 1]};
+    if (!traverse_refill(src, st.counts[bounce] * 8u, &st.counts[6 + bounce], tab))
+        atomicOr(out.err, kErrStackOverflow);
+}
+
+__device__ __forceinline__ void finalize(const Job& j, uint32_t gi, int k, F3 color, F3 d, bool hit_em,
+                                         uint32_t gword, const WaveOutputs& out) {
+    uint32_t xb, yb, gx, gy;
+    int g;
+    group_origin(j, gi - j.group_base, &xb, &yb, &g, &gx, &gy);
+    uint32_t px = gx + (uint32_t)(k & 3), py = gy + (uint32_t)(k >> 2);
+    if (px >= j.w || py >= j.h) return;
+    F3 em = sky_intensity(d);
+    F3 c = f3(color.x * em.x, color.y * em.y, color.z * em.z);
+    c = hit_em ? c : f3(0.0f, 0.0f, 0.0f);
+    size_t idx = (size_t)j.out_offset + (size_t)py * j.w + px;
+    if (out.rgba) out.rgba[idx] = pack_color(c);
+    if (out.gbuf) out.gbuf[idx] = gword;
+    if (out.color) {
+        out.color[3 * idx] = c.x;
+        out.color[3 * idx + 1] = c.y;
+        out.color[3 * idx + 2] = c.z;
+    }
+    if (out.accum) {
+        out.accum[3 * idx] += c.x;
+        out.accum[3 * idx + 1] += c.y;
+        out.accum[3 * idx + 2] += c.z;
+    }
+}
+
+__global__ void __launch_bounds__(128) k_wf_shade(const Job* __restrict__ jobs, const DeviceScene* __restrict__ scenes,
+                                                  WaveState st, int bounce, WaveOutputs out) {
+    __shared__ ApproxTables tab;
+    load_tables_wf(tab);
+    const int k = threadIdx.x & 7;
+    const unsigned omask = 0xffu << (threadIdx.x & 24u);
+    const uint32_t n = st.counts[bounce];
+    const uint32_t* queue = st.queue[bounce & 1];
+    uint32_t* next_q = st.queue[(bounce + 1) & 1];
+    uint32_t* next_n = &st.counts[bounce + 1];
+    const uint32_t octets = (gridDim.x * blockDim.x) >> 3;
+    uint32_t rays = 0;
+    for (uint32_t qi = (blockIdx.x * blockDim.x + threadIdx.x) >> 3; qi < n; qi += octets) {
+        uint32_t gi = queue[qi];
+        size_t l = (size_t)gi * 8 + k;
+        const Job& j = jobs[st.group_job[gi]];
+        const DeviceScene s = scenes[j.scene];
+        uint32_t flags = st.flags[l];
+        bool active = (flags & 1u) != 0u;
+        F3 o = f3(st.ox[l], st.oy[l], st.oz[l]), d = f3(st.dx[l], st.dy[l], st.dz[l]);
+        Hit h{st.ht[l], st.hu[l], st.hv[l], st.htri[l]};
+        Isect I = make_isect(s, h, o, d, tab);
+        bool hit_em = (I.mat >> 31) != 0u;
+        F3 color = f3(st.cr[l], st.cg[l], st.cb[l]);
+        unsigned traced = __popc(__ballot_sync(omask, active) & omask);  // rays this group traced this bounce
+        rays += traced;
+        if (out.job_rays && k == 0 && traced) atomicAdd(&out.job_rays[st.group_job[gi]], (unsigned long long)traced);
+        bool keep = false;
+        if (oct_all(omask, hit_em)) {
+            finalize(j, gi, k, color, d, hit_em, st.gbuf[l], out);
+        } else {
+            LaneRng rng;
+            rng.resume(st.rng[l], k);
+            F3 cm;
+            float fr;
+            continue_path(s, o, d, active, I, rng, bounce == 0, tab, cm, fr);
+            color = f3(color.x * cm.x, color.y * cm.y, color.z * cm.z);
+            uint32_t gword = st.gbuf[l];
+            if (bounce == 0) {
+                PixelOut p;
+                p.tex = ((int32_t)I.mat >> 24) & 3;
+                p.tu = I.tu;
+                p.tv = I.tv;
+                p.fresnel = fr;
+                gword = pack_gbuffer(p);
+            }
+            if (bounce == 4) {
+                finalize(j, gi, k, color, d, hit_em, gword, out);
+            } else {
+                st.ox[l] = o.x;
+                st.oy[l] = o.y;
+                st.oz[l] = o.z;
+                st.dx[l] = d.x;
+                st.dy[l] = d.y;
+                st.dz[l] = d.z;
+                st.cr[l] = color.x;
+                st.cg[l] = color.y;
+                st.cb[l] = color.z;
+                st.rng[l] = rng.s;
+                st.gbuf[l] = gword;
+                st.flags[l] = active ? 1u : 0u;
+                keep = true;
+            }
+        }
+        enqueue_octets(k == 0 && keep, gi, next_q, next_n);
+    }
+    // each octet counted its rays on all 8 lanes: keep lane 0's
+    unsigned long long v = (threadIdx.x & 7u) == 0u ? rays : 0u;
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+    if ((threadIdx.x & 31u) == 0u && v) atomicAdd(out.rays, v);
+}
+
+__global__ void k_resolve_multi(const ResolveItem* __restrict__ items, uint32_t n_items, const float* __restrict__ accum,
+                                uint32_t* __restrict__ rgba) {
+    for (uint32_t it = blockIdx.y; it < n_items; it += gridDim.y) {
+        ResolveItem r = items[it];
+        for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < r.npx; i += gridDim.x * blockDim.x) {
+            size_t p = (size_t)r.offset + i;
+            F3 c = f3(accum[3 * p] * r.factor, accum[3 * p + 1] * r.factor, accum[3 * p + 2] * r.factor);
+            rgba[p] = pack_color(c);
+        }
+    }
+}
+
+cudaError_t launch_resolve_multi(const ResolveItem* items, uint32_t n_items, const float* accum, uint32_t* rgba,
+                                 cudaStream_t stream) {
+    if (n_items == 0) return cudaSuccess;
+    dim3 grid(64, n_items < 1024 ? n_items : 1024);
+    k_resolve_multi<<<grid, 256, 0, stream>>>(items, n_items, accum, rgba);
+    return cudaGetLastError();
+}
+
+static int g_sms_wf = 0;
+static int sms() {
+    if (!g_sms_wf) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&g_sms_wf, cudaDevAttrMultiProcessorCount, dev);
+        if (g_sms_wf <= 0) g_sms_wf = 1;
+    }
+    return g_sms_wf;
+}
+
+cudaError_t launch_wave(const Job* jobs, const WaveHeader* hdr, const DeviceScene* scenes, const WaveState& st,
+                        const WaveOutputs& out, bool packet, uint32_t blocks_per_sm, cudaStream_t stream) {
+    if (blocks_per_sm == 0) blocks_per_sm = 12;
+    uint32_t grid = (uint32_t)sms() * blocks_per_sm;
+    // counts[0..5]: queue lengths per bounce; counts[6..10]: ray counters of
+    // the refill traversal, one per bounce
+    cudaError_t e = cudaMemsetAsync(st.counts, 0, 16 * sizeof(uint32_t), stream);
+    if (e != cudaSuccess) return e;
+    k_wf_raygen<<<grid, 128, 0, stream>>>(jobs, hdr, st);
+    for (int b = 0; b < 5; b++) {
+        if (packet) k_wf_traverse_packet<<<grid, 128, 0, stream>>>(jobs, scenes, st, b, out);
+        else k_wf_traverse_single<<<grid, 128, 0, stream>>>(jobs, scenes, st, b, out);
+        k_wf_shade<<<grid, 128, 0, stream>>>(jobs, scenes, st, b, out);
+    }
+    return cudaGetLastError();
+}
+
+}  // namespace cvx

@@ -185,6 +185,72 @@ int32_t cvx_read_frame_f32(cvx_renderer* r, float* out);
  * and its device time. */
 int32_t cvx_renderer_stats(cvx_renderer* r, uint64_t* rays, float* ms);
 
+/* ---- device: batched rendering -----------------------------------------
+ * Many images of many resident scenes in shared wavefronts: sample s of
+ * every view goes into wave s, so each view accumulates its samples in order
+ * and its image equals the one cvx_accumulate_frame_f32 + cvx_resolve_u8
+ * give for it alone. No reference counterpart: the reference renders one
+ * frame of one scene (main.rs:124-217). */
+typedef struct cvx_view {
+    uint32_t scene;       /* index into the scenes given to cvx_batch_create */
+    uint32_t width, height;
+    uint32_t spp;         /* samples, frames frame_base .. frame_base + spp - 1 */
+    uint32_t frame_base;
+    cvx_camera camera;
+} cvx_view;
+
+typedef struct cvx_batch cvx_batch;
+/* max_groups bounds the 8-pixel groups of one wave (ray-queue capacity);
+ * max_pixels bounds the pixels of all views of one call. */
+int32_t cvx_batch_create(cvx_scene* const* scenes, uint32_t n_scenes, uint32_t max_groups, uint64_t max_pixels,
+                         const cvx_render_config* config, cvx_batch** out);
+/* Renders every view; rgba[i] (host, width*height words, may be NULL)
+ * receives view i. rays and ms (may be NULL) receive the totals. */
+int32_t cvx_batch_render(cvx_batch* b, const cvx_view* views, uint32_t n_views, uint32_t* const* rgba,
+                         uint64_t* rays, float* ms);
+void cvx_batch_destroy(cvx_batch* b);
+
+/* ---- device: request server ----------------------------------------------
+ * A request loop on its own host thread over resident scenes: submitted
+ * requests wait in FIFO order and are admitted while their framebuffer and
+ * ray-queue memory fit the budget; every wave renders the next sample of
+ * every admitted request, so requests that arrive while others are on the
+ * GPU join the next wave (continuous batching). No reference counterpart. */
+typedef struct cvx_server_config {
+    uint64_t framebuffer_bytes; /* device memory for admitted requests' images */
+    uint32_t max_groups;        /* ray-queue capacity of one wave, in 8-pixel groups */
+    uint32_t traversal;         /* CVX_TRAVERSE_* */
+    uint32_t use_graph;
+    uint32_t sequential;        /* 1: one request at a time (the plain path, for comparison) */
+} cvx_server_config;
+
+typedef struct cvx_request {
+    uint32_t scene, width, height, spp, frame_base;
+    cvx_camera camera;
+} cvx_request;
+
+typedef struct cvx_request_result {
+    int32_t status;          /* CVX_OK, or the request's error */
+    double submit_s, start_s, done_s; /* server clock, seconds */
+    uint64_t rays;
+} cvx_request_result;
+
+typedef struct cvx_server cvx_server;
+int32_t cvx_server_create(cvx_scene* const* scenes, uint32_t n_scenes, const cvx_server_config* config,
+                          cvx_server** out);
+/* Queues a request; rgba (host, width*height words) must stay valid until the
+ * request completes. CVX_ERR_CAPACITY if it can never be admitted. */
+int32_t cvx_server_submit(cvx_server* s, const cvx_request* req, uint32_t* rgba, uint64_t* id);
+/* Waits up to timeout_ms (0: just polls) for a request; CVX_ERR_TIMEOUT if
+ * it is not done yet. The result is returned once and then forgotten. */
+int32_t cvx_server_wait(cvx_server* s, uint64_t id, uint32_t timeout_ms, cvx_request_result* result);
+/* Cancels a queued or running request (its result status becomes
+ * CVX_ERR_CANCELLED). */
+int32_t cvx_server_cancel(cvx_server* s, uint64_t id);
+/* The server clock (seconds), waves run, rays traced and device busy time. */
+int32_t cvx_server_stats(cvx_server* s, double* now_s, uint64_t* waves, uint64_t* rays, double* busy_s);
+void cvx_server_destroy(cvx_server* s);
+
 #ifdef __cplusplus
 }
 #endif

@@ -58,18 +58,19 @@ def test_intersect_bitexact(icosphere, orc, traversal):
     assert (tri >= 0).mean() > 0.5
 
 
-def test_intersect_counters_match_reference_debug_counts(icosphere, orc):
-    """Per-packet box and triangle counts (bvh.rs:604-651, the debug view)."""
+@pytest.mark.parametrize("traversal", [0, 1])
+def test_intersect_counters_match_reference_debug_counts(icosphere, orc, traversal):
+    """Box and triangle counts per packet (bvh.rs:604-651, the debug view) or per ray."""
     import torch
     bvh, scene, osc = icosphere
     o, d = scenes.random_rays(1 << 14, seed=3)
-    _, _, na, nt = osc.intersect(o, d, mode=0, counters=True)
+    _, _, na, nt = osc.intersect(o, d, mode=traversal, counters=True)
     rays = torch.from_numpy(np.concatenate([o.T, d.T]).copy()).cuda()
     n = o.shape[0]
     t = torch.empty(n, dtype=torch.float32, device="cuda")
     tri = torch.empty(n, dtype=torch.int32, device="cuda")
     cnt = torch.empty(2 * n, dtype=torch.int32, device="cuda")
-    scene.intersect_nearest_device(rays, t, tri, traversal=0, counters=cnt)
+    scene.intersect_nearest_device(rays, t, tri, traversal=traversal, counters=cnt)
     torch.cuda.synchronize()
     c = cnt.cpu().numpy().view(np.uint32)
     assert (c[:n] == na).all() and (c[n:] == nt).all()

@@ -1,0 +1,149 @@
+"""Wavefront form, batching and serving on the GPU.
+
+The wavefront kernels must give the same bits as the oracle (per-group RNG
+order); a view rendered in a batch or served in a mix must give the same
+image as the same view rendered alone; the server's admission, cancellation
+and timeouts are exercised on the host side of its request loop.
+"""
+
+import time
+
+import numpy as np
+import pytest
+
+from convector_gb300 import scenes
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def two_scenes(gpu, orc):
+    out = []
+    for text, mats in (scenes.room_sphere(), scenes.spheres_and_boxes(3000, seed=5)):
+        bvh = gpu.Bvh.from_meshes([gpu.Mesh.parse(text, mats)])
+        sc = gpu.Scene(bvh)
+        scenes.default_camera(sc.camera)
+        out.append((bvh, sc, orc.OracleScene.from_bvh(bvh)))
+    return out
+
+
+@pytest.mark.parametrize("traversal", [0, 1])
+@pytest.mark.parametrize("use_graph", [0, 1])
+def test_wavefront_frame_bitexact(two_scenes, gpu, orc, traversal, use_graph):
+    bvh, scene, osc = two_scenes[0]
+    w, h = 200, 120
+    r = gpu.Renderer(scene, w, h, rng_order=gpu.RNG_GROUP, traversal=traversal, mode=gpu.MODE_WAVEFRONT,
+                     use_graph=use_graph)
+    for frame in (42, 43):
+        rgba, gb = r.render_frame_u8(frame)
+        col = r.read_frame_f32()
+        orgba, ogb, ocol, orays = osc.render(scene.camera.as_array(), w, h, frame, rng_order=1, traversal=traversal)
+        assert (col.view(np.uint32) == ocol.view(np.uint32)).all()
+        assert (rgba == orgba).all() and (gb == ogb).all()
+        assert r.stats()[0] == orays
+
+
+def test_wavefront_matches_megakernel_full_frame(two_scenes, gpu):
+    bvh, scene, osc = two_scenes[0]
+    a = gpu.Renderer(scene, 1280, 736, rng_order=gpu.RNG_GROUP, traversal=1)
+    b = gpu.Renderer(scene, 1280, 736, rng_order=gpu.RNG_GROUP, traversal=1, mode=gpu.MODE_WAVEFRONT, use_graph=1)
+    ra, ga = a.render_frame_u8(42)
+    rb, gb = b.render_frame_u8(42)
+    assert (ra == rb).all() and (ga == gb).all()
+    assert a.stats()[0] == b.stats()[0]
+
+
+def test_wavefront_rejects_patch_order(two_scenes, gpu):
+    bvh, scene, osc = two_scenes[0]
+    with pytest.raises(gpu.CvxError):
+        gpu.Renderer(scene, 64, 64, rng_order=gpu.RNG_PATCH, mode=gpu.MODE_WAVEFRONT)
+
+
+def _alone(gpu, scene, view):
+    r = gpu.Renderer(scene, view.width, view.height, rng_order=gpu.RNG_GROUP, traversal=1)
+    r.set_camera(view.camera)
+    for s in range(view.spp):
+        r.accumulate_frame_f32(view.frame_base + s)
+    return r.resolve_u8(view.spp)
+
+
+def test_batch_images_equal_alone(two_scenes, gpu, orc):
+    scs = [s for _, s, _ in two_scenes]
+    views = []
+    for i, (w, h, spp) in enumerate([(160, 96, 2), (33, 17, 3), (96, 64, 1), (320, 184, 4)]):
+        cam = gpu.Camera()
+        scenes.default_camera(cam, eye=(0.3 * i, 1.2, 1.6))
+        views.append(gpu.View(i % 2, w, h, spp, 100 * i, cam))
+    batch = gpu.Batch(scs, max_groups=1 << 16, max_pixels=1 << 20)
+    imgs, rays, ms = batch.render(views)
+    assert rays > 0
+    for v, img in zip(views, imgs):
+        assert (img == _alone(gpu, scs[v.scene], v)).all()
+    # and against the oracle for one view
+    v = views[1]
+    acc = np.zeros((v.height, v.width, 3), np.float32)
+    osc = two_scenes[v.scene][2]
+    for s in range(v.spp):
+        osc.render(v.camera.as_array(), v.width, v.height, v.frame_base + s, rng_order=1, traversal=1, color=False,
+                   accum=acc)
+    assert (imgs[1] == orc.resolve(acc, v.spp)).all()
+
+
+def test_batch_splits_waves_when_queue_is_small(two_scenes, gpu):
+    scs = [s for _, s, _ in two_scenes]
+    views = [gpu.View(k % 2, 128, 64, 2, 7 * k, scenes.default_camera(gpu.Camera())) for k in range(6)]
+    big, _, _ = gpu.Batch(scs, max_groups=1 << 16, max_pixels=1 << 20).render(views)
+    small, _, _ = gpu.Batch(scs, max_groups=1100, max_pixels=1 << 20).render(views)
+    for a, b in zip(big, small):
+        assert (a == b).all()
+
+
+def test_server_mix_equals_alone(two_scenes, gpu):
+    scs = [s for _, s, _ in two_scenes]
+    rng = np.random.default_rng(4)
+    reqs = []
+    for k in range(12):
+        cam = gpu.Camera()
+        scenes.default_camera(cam, eye=(rng.uniform(-1, 1), 1.2, 1.6))
+        reqs.append((int(k % 2), int(rng.choice([64, 100, 160])), int(rng.choice([32, 50, 96])),
+                     int(rng.integers(1, 5)), cam))
+    for sequential in (False, True):
+        srv = gpu.Server(scs, framebuffer_bytes=64 << 20, max_groups=1 << 14, sequential=sequential)
+        ids = []
+        for i, (sc, w, h, spp, cam) in enumerate(reqs):
+            ids.append(srv.submit(sc, w, h, spp, cam, frame_base=10 * i))
+            time.sleep(0.002)
+        for i, rid in enumerate(ids):
+            st, img, info = srv.wait(rid)
+            assert st == 0 and info["done_s"] >= info["start_s"] >= info["submit_s"]
+            sc, w, h, spp, cam = reqs[i]
+            assert (img == _alone(gpu, scs[sc], gpu.View(sc, w, h, spp, 10 * i, cam))).all()
+        assert srv.stats()["waves"] > 0
+        srv.close()
+
+
+def test_server_admission_cancel_timeout(two_scenes, gpu):
+    scs = [s for _, s, _ in two_scenes]
+    cam = scenes.default_camera(gpu.Camera())
+    srv = gpu.Server(scs, framebuffer_bytes=64 * 64 * 16 * 2, max_groups=2048)
+    with pytest.raises(gpu.CvxError) as e:  # can never fit the framebuffer budget
+        srv.submit(0, 1280, 736, 1, cam)
+    assert e.value.status == 7
+    long_id = srv.submit(0, 64, 64, 400, cam)
+    queued = [srv.submit(1, 64, 64, 1, cam) for _ in range(3)]  # at most two fit at once
+    srv.cancel(queued[-1])
+    with pytest.raises(gpu.CvxError) as e:
+        srv.wait(long_id, timeout_ms=0)
+    assert e.value.status == 8
+    st, img, info = srv.wait(queued[-1])
+    assert st == 9 and img is None
+    srv.cancel(long_id)
+    st, img, info = srv.wait(long_id)
+    assert st == 9
+    for rid in queued[:-1]:
+        st, img, info = srv.wait(rid)
+        assert st == 0 and img.shape == (64, 64)
+    with pytest.raises(gpu.CvxError) as e:
+        srv.wait(123456)
+    assert e.value.status == 10
+    srv.close()
