@@ -290,9 +290,13 @@ def run_ours(args):
         e2e_s = float(tt.item())
     e2e_value = world * n * e2e_steps / e2e_s / 1e6
 
-    render = None
+    render = batched = served = large = None
     if rank == 0 and not args.no_render:
-        render = bench_render(cg, torch)
+        render = _guard(bench_render, cg)
+    if rank == 0 and not args.no_extra:
+        large = _guard(bench_large, cg)
+        batched = _guard(bench_batched, cg)
+        served = _guard(bench_served, cg)
 
     if rank == 0:
         peak, peak_kind = _peaks()
@@ -325,38 +329,176 @@ def run_ours(args):
             "wall_s_timed": wall,
             "step_ms_p50": statistics.median(step_ms),
             "render": render,
+            "large_accumulate": large,
+            "batched": batched,
+            "served": served,
         }
         print(json.dumps(line))
     if world > 1:
         dist.destroy_process_group()
 
 
-def bench_render(cg, torch):
-    """1280x736, 1 spp, 5 bounces on the room-and-sphere scene: frame p50/p99."""
+def _guard(fn, *a):
+    try:
+        return fn(*a)
+    except Exception as e:  # an extra section must not cost the headline line
+        return {"error": "%s: %s" % (type(e).__name__, e)}
+
+
+def _frames(r, frames, first=42, accumulate=False):
+    for f in range(3):
+        (r.accumulate_frame_f32 if accumulate else r.render_frame_u8)(f)
+    ms, rays = [], 0
+    for f in range(frames):
+        if accumulate:
+            r.accumulate_frame_f32(first + f)
+        else:
+            r.render_frame_u8(first + f, gbuffer=False)
+        nr, m = r.stats()
+        ms.append(m)
+        rays += nr
+    return {"frame_ms_p50": float(np.percentile(ms, 50)), "frame_ms_p99": float(np.percentile(ms, 99)),
+            "mrays_per_s": rays / (sum(ms) * 1e-3) / 1e6, "rays_per_frame": rays / frames, "frames": frames}
+
+
+def bench_render(cg):
+    """1280x736, 1 spp, 5 bounces on the room-and-sphere scene: frame p50/p99
+    (device time per frame) for every kernel organisation."""
     from convector_gb300 import scenes
     bvh = build_c0()
     scene = cg.Scene(bvh)
     scenes.default_camera(scene.camera)
     out = {}
-    for name, order, frames in (("per_group", cg.RNG_GROUP, 30), ("patch_exact", cg.RNG_PATCH, 10)):
-        best = None
-        for trav in (cg.TRAVERSE_PACKET, cg.TRAVERSE_SINGLE):
-            r = cg.Renderer(scene, 1280, 736, rng_order=order, traversal=trav)
-            for f in range(3):
-                r.render_frame_u8(f, gbuffer=False)
-            ms, rays = [], 0
-            for f in range(frames):
-                r.render_frame_u8(42 + f, gbuffer=False)
-                nr, m = r.stats()
-                ms.append(m)
-                rays += nr
-            res = {"traversal": "packet8" if trav == 0 else "single", "frame_ms_p50": float(np.percentile(ms, 50)),
-                   "frame_ms_p99": float(np.percentile(ms, 99)), "mrays_per_s": rays / (sum(ms) * 1e-3) / 1e6,
-                   "rays_per_frame": rays / frames}
-            if best is None or res["frame_ms_p50"] < best["frame_ms_p50"]:
-                best = res
-        out[name] = best
+    variants = [("megakernel_packet8", cg.RNG_GROUP, 0, cg.MODE_MEGAKERNEL, 0),
+                ("megakernel_single", cg.RNG_GROUP, 1, cg.MODE_MEGAKERNEL, 0),
+                ("wavefront_single_graph", cg.RNG_GROUP, 1, cg.MODE_WAVEFRONT, 1),
+                ("wavefront_packet8_graph", cg.RNG_GROUP, 0, cg.MODE_WAVEFRONT, 1),
+                ("patch_exact_packet8", cg.RNG_PATCH, 0, cg.MODE_MEGAKERNEL, 0)]
+    for name, order, trav, mode, graph in variants:
+        r = cg.Renderer(scene, 1280, 736, rng_order=order, traversal=trav, mode=mode, use_graph=graph)
+        out[name] = _frames(r, 10 if order == cg.RNG_PATCH else 30)
     return out
+
+
+def bench_large(cg):
+    """Accumulative 1280x736, 64 spp, 5 bounces on the ~870k-triangle random-walk
+    tube (seed 11): wavefront + CUDA graph against the megakernel."""
+    from convector_gb300 import scenes
+    tris, _ = scenes.random_walk_tube(obj=False)
+    bvh = cg.Bvh.build(tris)
+    scene = cg.Scene(bvh)
+    scenes.default_camera(scene.camera)
+    out = {"triangles": int(tris.shape[0]), "bvh_depth": int(bvh.depth)}
+    for name, trav, mode, graph in (("wavefront_single_graph", 1, cg.MODE_WAVEFRONT, 1),
+                                    ("megakernel_single", 1, cg.MODE_MEGAKERNEL, 0)):
+        r = cg.Renderer(scene, 1280, 736, rng_order=cg.RNG_GROUP, traversal=trav, mode=mode, use_graph=graph)
+        res = _frames(r, 64, accumulate=True)
+        res["spp"] = 64
+        out[name] = res
+    return out
+
+
+def _c3_views(cg, n=256, seed=3):
+    """256 scenes of spheres and boxes, log-uniform 500..20,000 triangles, one
+    camera and a resolution from {320x184, 640x368, 1280x736} each, 4 spp."""
+    from concurrent.futures import ThreadPoolExecutor
+    from convector_gb300 import scenes
+    rng = np.random.default_rng(seed)
+    counts = np.exp(rng.uniform(np.log(500), np.log(20000), n)).astype(int)
+    sizes = [(320, 184), (640, 368), (1280, 736)]
+    res = [sizes[i] for i in rng.integers(0, 3, n)]
+    tri_arrays = [scenes.spheres_and_boxes(int(c), seed=seed * 100003 + i, obj=False)[0] for i, c in enumerate(counts)]
+    with ThreadPoolExecutor(8) as ex:
+        bvhs = list(ex.map(cg.Bvh.build, tri_arrays))
+    scs = [cg.Scene(b) for b in bvhs]
+    views = []
+    for i in range(n):
+        cam = scenes.default_camera(cg.Camera(), eye=(rng.uniform(-1, 1), rng.uniform(0.8, 1.6), 1.6))
+        views.append(cg.View(i, res[i][0], res[i][1], 4, 1000 * i, cam))
+    return scs, views, int(counts.sum())
+
+
+def bench_batched(cg):
+    """256 uneven scenes in shared wavefronts against one scene at a time."""
+    scs, views, total_tris = _c3_views(cg)
+    batch = cg.Batch(scs, max_groups=1 << 21, max_pixels=sum(v.width * v.height for v in views))
+    batch.render(views[:8], want_images=False)  # warm-up (graph capture)
+    t0 = time.perf_counter()
+    _, rays_b, ms_b = batch.render(views, want_images=False)
+    wall_b = time.perf_counter() - t0
+    # one at a time: the plain per-scene renderer, 4 accumulated frames + resolve
+    rays_p, ms_p = 0, 0.0
+    t0 = time.perf_counter()
+    for v in views:
+        r = cg.Renderer(scs[v.scene], v.width, v.height, rng_order=cg.RNG_GROUP, traversal=cg.TRAVERSE_SINGLE)
+        r.set_camera(v.camera)
+        for s in range(v.spp):
+            r.accumulate_frame_f32(v.frame_base + s)
+            nr, m = r.stats()
+            rays_p += nr
+            ms_p += m
+        r.resolve_u8(v.spp)
+    wall_p = time.perf_counter() - t0
+    return {"scenes": len(scs), "triangles_total": total_tris, "spp": 4, "rays": rays_b,
+            "batched_mrays_per_s_device": rays_b / (ms_b * 1e-3) / 1e6, "batched_wall_s": wall_b,
+            "batched_mrays_per_s_wall": rays_b / wall_b / 1e6,
+            "one_at_a_time_mrays_per_s_device": rays_p / (ms_p * 1e-3) / 1e6, "one_at_a_time_wall_s": wall_p,
+            "one_at_a_time_mrays_per_s_wall": rays_p / wall_p / 1e6,
+            "speedup_wall": wall_p / wall_b}
+
+
+def _served_run(cg, scs, reqs, sequential):
+    srv = cg.Server(scs, framebuffer_bytes=24 << 30, max_groups=1 << 21, traversal=cg.TRAVERSE_SINGLE,
+                    sequential=sequential)
+    # warm-up: one small request per scene
+    for k in range(len(scs)):
+        srv.wait(srv.submit(k, 64, 64, 1, reqs[0][5]))
+    ids = []
+    t0 = time.perf_counter()
+    for at, sc, w, h, spp, cam in reqs:
+        dt = t0 + at - time.perf_counter()
+        if dt > 0:
+            time.sleep(dt)
+        ids.append(srv.submit(sc, w, h, spp, cam, frame_base=len(ids) * 16))
+    res = [srv.wait(i, 600000)[2] for i in ids]
+    lat = np.array([r["done_s"] - r["submit_s"] for r in res]) * 1e3
+    rays = sum(r["rays"] for r in res)
+    span = max(r["done_s"] for r in res) - min(r["submit_s"] for r in res)
+    st = srv.stats()
+    srv.close()
+    return {"requests": len(res), "latency_ms_p50": float(np.percentile(lat, 50)),
+            "latency_ms_p99": float(np.percentile(lat, 99)), "mrays_per_s": rays / span / 1e6, "span_s": span,
+            "waves": st["waves"], "device_busy_s": st["busy_s"]}
+
+
+def bench_served(cg, duration=2.0, rate=200.0, seed=4):
+    """Poisson arrivals (200 req/s) over 3 resident scenes (room+sphere,
+    displaced icosphere, random-walk tube); camera on a radius-3 sphere around
+    the room centre, resolution log-uniform 320x184..1920x1080, 1..16 spp.
+    Continuously batched server against the one-request-at-a-time path."""
+    from convector_gb300 import scenes
+    scs = []
+    for gen in (scenes.room_sphere, scenes.displaced_icosphere, scenes.random_walk_tube):
+        tris, _ = gen(obj=False)
+        scs.append(cg.Scene(cg.Bvh.build(tris)))
+    rng = np.random.default_rng(seed)
+    center = np.array([0.0, 1.25, -2.0])
+    reqs, t = [], 0.0
+    while True:
+        t += rng.exponential(1.0 / rate)
+        if t > duration:
+            break
+        z = rng.uniform(-1, 1)
+        ph = rng.uniform(0, 2 * np.pi)
+        eye = center + 3.0 * np.array([np.sqrt(1 - z * z) * np.cos(ph), z, np.sqrt(1 - z * z) * np.sin(ph)])
+        cam = scenes.default_camera(cg.Camera(), eye=tuple(eye), target=tuple(center))
+        w = int(round(np.exp(rng.uniform(np.log(320), np.log(1920)))))
+        h = int(min(1080, max(184, round(w * 184 / 320))))
+        reqs.append((t, int(rng.integers(0, 3)), w, h, int(rng.integers(1, 17)), cam))
+    served = _served_run(cg, scs, reqs, sequential=False)
+    plain = _served_run(cg, scs, reqs, sequential=True)
+    return {"rate_per_s": rate, "duration_s": duration, "served": served, "plain_sequential": plain,
+            "throughput_ratio": served["mrays_per_s"] / plain["mrays_per_s"]}
 
 
 def main():
@@ -366,9 +508,18 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-render", action="store_true")
+    ap.add_argument("--no-extra", action="store_true", help="skip the large, batched and served sections")
+    ap.add_argument("--section", choices=["render", "large", "batched", "served"],
+                    help="run one extra section alone and print its JSON (no headline line)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
+    if args.section:
+        import convector_gb300 as cg
+        cg.lib(build=True)
+        fn = {"render": bench_render, "large": bench_large, "batched": bench_batched, "served": bench_served}
+        print(json.dumps({args.section: fn[args.section](cg)}))
+        return
     if args.impl == "reference":
         run_reference(args)
     else:

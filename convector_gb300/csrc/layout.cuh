@@ -40,7 +40,7 @@ struct DeviceCamera {
 };
 
 constexpr uint32_t kSkyMaterial = 0xC0000000u;  // material.rs:85-90
-constexpr int kStackDepth = 64;
+constexpr int kStackDepth = 128;  // >= BVH depth + 2 (checked at scene creation)
 
 // Error bits a kernel reports through its status word instead of trapping.
 constexpr uint32_t kErrStackOverflow = 1u;

@@ -41,38 +41,74 @@ def reference_materials():
 
 
 class ObjWriter:
+    """Collects vertices, faces and materials; emits OBJ text for the loader,
+    or the triangle array (n x 16 words, cvx_triangle) that loading that text
+    gives, without the text round trip for large meshes. Vertices are rounded
+    to float32 on entry, which is what the text's %.9g round-trips to."""
+
     def __init__(self):
         self.lines = []
         self.nv = 0
         self.nvt = 0
+        self.verts = []
+        self.texs = []
+        self.blocks = []  # (faces (k x 3, global 0-based), tex faces or None, material name)
+        self.mat = None
 
     def material(self, name):
         self.lines.append("usemtl %s" % name)
+        self.mat = name
 
     def vertices(self, v):
         v = np.asarray(v, dtype=np.float32)
         base = self.nv
-        self.lines.extend("v %.9g %.9g %.9g" % (a, b, c) for a, b, c in v.tolist())
+        self.verts.append(v)
         self.nv += v.shape[0]
         return base
 
     def tex_coords(self, t):
         t = np.asarray(t, dtype=np.float32)
         base = self.nvt
-        self.lines.extend("vt %.9g %.9g" % (a, b) for a, b in t.tolist())
+        self.texs.append(t)
         self.nvt += t.shape[0]
         return base
 
     def faces(self, f, base, tbase=None):
-        f = np.asarray(f, dtype=np.int64) + base + 1
-        if tbase is None:
-            self.lines.extend("f %d %d %d" % tuple(r) for r in f.tolist())
-        else:
-            for r in f.tolist():
-                self.lines.append("f " + " ".join("%d/%d" % (i, i - base - 1 + tbase + 1) for i in r))
+        f = np.asarray(f, dtype=np.int64)
+        self.blocks.append((f + base, None if tbase is None else f + tbase, self.mat))
+        self.lines.append(("faces", len(self.blocks) - 1))
 
     def text(self):
-        return "\n".join(self.lines) + "\n"
+        verts = np.concatenate(self.verts) if self.verts else np.zeros((0, 3), np.float32)
+        texs = np.concatenate(self.texs) if self.texs else np.zeros((0, 2), np.float32)
+        out = ["v %.9g %.9g %.9g" % tuple(r) for r in verts.tolist()]
+        out += ["vt %.9g %.9g" % tuple(r) for r in texs.tolist()]
+        for item in self.lines:
+            if isinstance(item, tuple):
+                f, tf, _ = self.blocks[item[1]]
+                if tf is None:
+                    out.extend("f %d %d %d" % tuple(r) for r in (f + 1).tolist())
+                else:
+                    out.extend("f %d/%d %d/%d %d/%d" % (a, x, b, y, c, z)
+                               for (a, b, c), (x, y, z) in zip((f + 1).tolist(), (tf + 1).tolist()))
+            else:
+                out.append(item)
+        return "\n".join(out) + "\n"
+
+    def triangles(self, materials):
+        """The cvx_triangle array (n x 16 uint32) in face order."""
+        verts = np.concatenate(self.verts).astype(np.float32)
+        texs = np.concatenate(self.texs).astype(np.float32) if self.texs else np.zeros((0, 2), np.float32)
+        parts = []
+        for f, tf, mat in self.blocks:
+            t = np.zeros((f.shape[0], 16), np.float32)
+            t[:, 0:9] = verts[f].reshape(-1, 9)
+            if tf is not None:
+                t[:, 9:15] = texs[tf].reshape(-1, 6)
+            u = t.view(np.uint32)
+            u[:, 15] = materials[mat] if mat is not None else SMaterial.white()
+            parts.append(u)
+        return np.concatenate(parts)
 
 
 def _room(w, lo=ROOM_LO, hi=ROOM_HI, floor_tex=True):
@@ -107,39 +143,37 @@ def _ceiling_light(w, y=None, cx=0.0, cz=-2.0, half=0.5):
 
 def uv_sphere(center, radius, segments, rings):
     """UV sphere with 2*S*(R-1) triangles: pole caps as triangles, bands as quads."""
-    verts = [(0.0, radius, 0.0)]
-    for r in range(1, rings):
-        th = math.pi * r / rings
-        for s in range(segments):
-            ph = 2.0 * math.pi * s / segments
-            verts.append((radius * math.sin(th) * math.cos(ph), radius * math.cos(th),
-                          radius * math.sin(th) * math.sin(ph)))
-    verts.append((0.0, -radius, 0.0))
-    verts = np.array(verts) + np.asarray(center)
-    faces = []
-    ring = lambda r, s: 1 + (r - 1) * segments + (s % segments)
-    for s in range(segments):
-        faces.append((0, ring(1, s + 1), ring(1, s)))
-    for r in range(1, rings - 1):
-        for s in range(segments):
-            a, b, c, d = ring(r, s), ring(r, s + 1), ring(r + 1, s + 1), ring(r + 1, s)
-            faces.append((a, b, c))
-            faces.append((a, c, d))
-    south = len(verts) - 1
-    for s in range(segments):
-        faces.append((south, ring(rings - 1, s), ring(rings - 1, s + 1)))
-    return verts, np.array(faces)
+    th = math.pi * np.arange(1, rings)[:, None] / rings
+    ph = 2.0 * math.pi * np.arange(segments)[None, :] / segments
+    ring_pts = np.stack([radius * np.sin(th) * np.cos(ph), np.broadcast_to(radius * np.cos(th), (rings - 1, segments)),
+                         radius * np.sin(th) * np.sin(ph)], -1).reshape(-1, 3)
+    verts = np.concatenate([[[0.0, radius, 0.0]], ring_pts, [[0.0, -radius, 0.0]]]) + np.asarray(center)
+    s = np.arange(segments)
+    ring = lambda r, k: 1 + (r - 1) * segments + (k % segments)
+    top = np.stack([np.zeros(segments, np.int64), ring(1, s + 1), ring(1, s)], 1)
+    r = np.arange(1, rings - 1)[:, None]
+    a, b, c, d = ring(r, s[None, :]), ring(r, s[None, :] + 1), ring(r + 1, s[None, :] + 1), ring(r + 1, s[None, :])
+    band = np.stack([np.stack([a, b, c], -1), np.stack([a, c, d], -1)], 2).reshape(-1, 3)
+    south = verts.shape[0] - 1
+    bottom = np.stack([np.full(segments, south, np.int64), ring(rings - 1, s), ring(rings - 1, s + 1)], 1)
+    return verts, np.concatenate([top, band, bottom])
 
 
-def room_sphere():
-    """1280x736 interactive scene: 10 + 4,960 + 2 triangles."""
+def _emit(w, obj):
+    mats = reference_materials()
+    return (w.text(), mats) if obj else (w.triangles(mats), mats)
+
+
+def room_sphere(obj=True):
+    """1280x736 interactive scene: 10 + 4,960 + 2 triangles. Returns (OBJ text,
+    materials), or (triangle array, materials) when obj is false."""
     w = ObjWriter()
     _room(w)
     w.material("fauteuil")
     v, f = uv_sphere((0.0, 0.5, -2.0), 0.5, 80, 32)
     w.faces(f, w.vertices(v))
     _ceiling_light(w)
-    return w.text(), reference_materials()
+    return _emit(w, obj)
 
 
 def _splitmix64(x):
@@ -200,7 +234,7 @@ def icosphere(subdivisions):
     return v, f
 
 
-def displaced_icosphere(subdivisions=6, seed=7, center=(0.0, 1.1, -2.0), radius=0.8):
+def displaced_icosphere(subdivisions=6, seed=7, center=(0.0, 1.1, -2.0), radius=0.8, obj=True):
     """Icosphere of 20*4^s triangles displaced by 0.05 * value_noise(seed) in the room."""
     d, f = icosphere(subdivisions)
     r = radius + 0.05 * value_noise(d, seed)
@@ -209,7 +243,7 @@ def displaced_icosphere(subdivisions=6, seed=7, center=(0.0, 1.1, -2.0), radius=
     _room(w)
     w.material("wall")
     w.faces(f, w.vertices(v))
-    return w.text(), reference_materials()
+    return _emit(w, obj)
 
 
 def random_rays(n, seed=7, lo=ROOM_LO, hi=ROOM_HI):
@@ -223,7 +257,7 @@ def random_rays(n, seed=7, lo=ROOM_LO, hi=ROOM_HI):
     return o.astype(np.float32), d.astype(np.float32)
 
 
-def random_walk_tube(segments=256, rings=1700, seed=11, radius=0.04):
+def random_walk_tube(segments=256, rings=1700, seed=11, radius=0.04, obj=True):
     """A tube of `segments` radial segments around a random-walk centre line of
     `rings` rings (2*segments*(rings-1) triangles) inside the room, plus the room
     and the ceiling light."""
@@ -272,7 +306,7 @@ def random_walk_tube(segments=256, rings=1700, seed=11, radius=0.04):
     w.material("wood_light")
     w.faces(faces, w.vertices(verts))
     _ceiling_light(w)
-    return w.text(), reference_materials()
+    return _emit(w, obj)
 
 
 def _box(center, size):
@@ -284,7 +318,7 @@ def _box(center, size):
     return v, f
 
 
-def spheres_and_boxes(n_tris, seed):
+def spheres_and_boxes(n_tris, seed, obj=True):
     """Random spheres and boxes in the room until about `n_tris` triangles,
     plus the ceiling light."""
     rng = np.random.default_rng(seed)
@@ -305,7 +339,7 @@ def spheres_and_boxes(n_tris, seed):
         w.faces(f, w.vertices(v))
         total += f.shape[0]
     _ceiling_light(w)
-    return w.text(), reference_materials()
+    return _emit(w, obj)
 
 
 def look_at_quaternion(eye, target):

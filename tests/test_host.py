@@ -187,3 +187,15 @@ def test_materials_encoding(cvx):  # material.rs:84-136
     assert M.with_glossiness(M.white(), 4) == 0x10FFFFFF
     assert M.with_texture(M.white(), 2) == 0x02FFFFFF
     assert M.diffuse(1.0, 0.1, 0.4) == (0x66 << 16) | (0x19 << 8) | 0xFF
+
+
+@pytest.mark.parametrize("gen", ["room_sphere", "spheres_and_boxes"])
+def test_scene_triangle_arrays_equal_loaded_obj(cvx, gen):
+    """The direct triangle arrays are what the OBJ loader gives for the same scene."""
+    from convector_gb300 import scenes
+    args = (1500, 9) if gen == "spheres_and_boxes" else ()
+    text, mats = getattr(scenes, gen)(*args)
+    tris, _ = getattr(scenes, gen)(*args, obj=False)
+    a = cvx.Bvh.from_meshes([cvx.Mesh.parse(text, mats)])
+    b = cvx.Bvh.build(tris)
+    assert (a.triangles == b.triangles).all() and (a.nodes == b.nodes).all()
