@@ -478,7 +478,8 @@ def bench_served(cg, duration=2.0, rate=200.0, seed=4):
     Continuously batched server against the one-request-at-a-time path."""
     from convector_gb300 import scenes
     scs = []
-    for gen in (scenes.room_sphere, scenes.displaced_icosphere, scenes.random_walk_tube):
+    for gen in (scenes.room_sphere, lambda obj: scenes.displaced_icosphere(obj=obj, light=True),
+                scenes.random_walk_tube):
         tris, _ = gen(obj=False)
         scs.append(cg.Scene(cg.Bvh.build(tris)))
     rng = np.random.default_rng(seed)

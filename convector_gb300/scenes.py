@@ -234,8 +234,9 @@ def icosphere(subdivisions):
     return v, f
 
 
-def displaced_icosphere(subdivisions=6, seed=7, center=(0.0, 1.1, -2.0), radius=0.8, obj=True):
-    """Icosphere of 20*4^s triangles displaced by 0.05 * value_noise(seed) in the room."""
+def displaced_icosphere(subdivisions=6, seed=7, center=(0.0, 1.1, -2.0), radius=0.8, obj=True, light=False):
+    """Icosphere of 20*4^s triangles displaced by 0.05 * value_noise(seed) in
+    the room; with `light`, plus the 2-triangle ceiling light."""
     d, f = icosphere(subdivisions)
     r = radius + 0.05 * value_noise(d, seed)
     v = d * r[:, None] + np.asarray(center)
@@ -243,6 +244,8 @@ def displaced_icosphere(subdivisions=6, seed=7, center=(0.0, 1.1, -2.0), radius=
     _room(w)
     w.material("wall")
     w.faces(f, w.vertices(v))
+    if light:  # the ray-cast workload has none; rendering it needs one
+        _ceiling_light(w)
     return _emit(w, obj)
 
 
