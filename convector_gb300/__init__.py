@@ -108,6 +108,7 @@ def lib(build=False):
         "cvx_scene_destroy": (None, [P]),
         "cvx_intersect_nearest": (I32, [P, P, P, P, P, P, P, U32, F32, U32, P, P]),
         "cvx_intersect_nearest_device": (I32, [P, P, U32, F32, U32, P, P, P, P]),
+        "cvx_intersect_nearest_noalloc": (I32, [P, P, P, P, P, P, P, U32, F32, U32, P, P]),
         "cvx_renderer_create": (I32, [P, U32, U32, P, P]),
         "cvx_renderer_destroy": (None, [P]),
         "cvx_renderer_set_camera": (I32, [P, P]),
@@ -334,6 +335,19 @@ class Scene:
         t = np.empty(n, dtype=np.float32)
         tri = np.empty(n, dtype=np.int32)
         _check(lib().cvx_intersect_nearest(self._h, *[_ptr(c) for c in cols], n, far, traversal, _ptr(t), _ptr(tri)))
+        return t, tri
+
+    def intersect_nearest_noalloc(self, origins, directions, far=1.0e5, traversal=TRAVERSE_PACKET):
+        """intersect_nearest without any device allocation: stages through the
+        library's static 16 MiB device buffer (at most 524,288 rays per call)."""
+        o = np.ascontiguousarray(origins, dtype=np.float32)
+        d = np.ascontiguousarray(directions, dtype=np.float32)
+        n = o.shape[0]
+        cols = [np.ascontiguousarray(o[:, k]) for k in range(3)] + [np.ascontiguousarray(d[:, k]) for k in range(3)]
+        t = np.empty(n, dtype=np.float32)
+        tri = np.empty(n, dtype=np.int32)
+        _check(lib().cvx_intersect_nearest_noalloc(self._h, *[_ptr(c) for c in cols], n, far, traversal, _ptr(t),
+                                                   _ptr(tri)))
         return t, tri
 
     def intersect_nearest_device(self, rays_soa, t_out, tri_out, far=1.0e5, traversal=TRAVERSE_PACKET,

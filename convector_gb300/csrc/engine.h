@@ -11,6 +11,7 @@
 namespace cvx {
 
 DeviceScene scene_view(const cvx_scene* s);
+cudaStream_t scene_stream(const cvx_scene* s);
 uint32_t scene_num_lights(const cvx_scene* s);
 uint32_t groups_of(uint32_t w, uint32_t h);
 

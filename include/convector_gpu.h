@@ -138,6 +138,23 @@ int32_t cvx_intersect_nearest_device(cvx_scene* scene, const float* rays, uint32
                                      uint32_t traversal, float* t_out, int32_t* tri_out, uint32_t* counters,
                                      void* stream);
 
+/* The query of cvx_intersect_nearest for callers that must not allocate device
+ * memory: a host application that owns the GPU's memory budget through its
+ * own allocator and forbids plugins to call cudaMalloc, or a real-time loop in
+ * which an allocation (which can synchronise the device and take an
+ * unpredictable time) would break the frame budget. The scene must already
+ * exist; this call allocates nothing. Rays and hits are staged through one
+ * static device buffer of 16 MiB + 256 B that the library reserves on every
+ * GPU it is loaded on, until the process exits: at most 524,288 rays per call
+ * (CVX_ERR_INVALID beyond). Every call shares that buffer: calls that overlap
+ * on the GPU (from several threads or scenes at once) race on it and must be
+ * serialised by the caller. The first call on each device looks up the
+ * buffer's device address; make that first call before any stream capture.
+ * No counterpart in the reference. */
+int32_t cvx_intersect_nearest_noalloc(cvx_scene* scene, const float* ox, const float* oy, const float* oz,
+                                      const float* dx, const float* dy, const float* dz, uint32_t n,
+                                      float far_dist, uint32_t traversal, float* t_out, int32_t* tri_out);
+
 /* ---- device: renderer ---------------------------------------------------- */
 
 /* RNG order: CVX_RNG_PATCH reproduces the reference's stream exactly (one
