@@ -377,6 +377,12 @@ def bench_render(cg):
     for name, order, trav, mode, graph in variants:
         r = cg.Renderer(scene, 1280, 736, rng_order=order, traversal=trav, mode=mode, use_graph=graph)
         out[name] = _frames(r, 10 if order == cg.RNG_PATCH else 30)
+    from convector_gb300 import autotune
+    best, table = autotune.tune(scene, 1280, 736, use_cache=False)
+    res = _frames(cg.Renderer(scene, 1280, 736, **best), 30)
+    res["config"] = best
+    res["candidates_ms"] = {k: round(v, 4) for k, v in table.items()}
+    out["autotuned"] = res
     return out
 
 
@@ -389,11 +395,18 @@ def bench_large(cg):
     scene = cg.Scene(bvh)
     scenes.default_camera(scene.camera)
     out = {"triangles": int(tris.shape[0]), "bvh_depth": int(bvh.depth)}
-    for name, trav, mode, graph in (("wavefront_single_graph", 1, cg.MODE_WAVEFRONT, 1),
-                                    ("megakernel_single", 1, cg.MODE_MEGAKERNEL, 0)):
-        r = cg.Renderer(scene, 1280, 736, rng_order=cg.RNG_GROUP, traversal=trav, mode=mode, use_graph=graph)
+    from convector_gb300 import autotune
+    best, table = autotune.tune(scene, 1280, 736, use_cache=False, frames=3)
+    for name, kw in (("wavefront_single_graph", dict(traversal=1, mode=cg.MODE_WAVEFRONT, use_graph=1)),
+                     ("megakernel_single", dict(traversal=1, mode=cg.MODE_MEGAKERNEL)),
+                     ("autotuned", best)):
+        kw = dict(kw)
+        kw.setdefault("rng_order", cg.RNG_GROUP)
+        r = cg.Renderer(scene, 1280, 736, **kw)
         res = _frames(r, 64, accumulate=True)
         res["spp"] = 64
+        if name == "autotuned":
+            res["config"] = best
         out[name] = res
     return out
 

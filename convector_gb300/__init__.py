@@ -29,6 +29,7 @@ TRIANGLE_DTYPE_WORDS = 16  # cvx_triangle: v0 v1 v2 (9 f32), uv0..2 (6 f32), mat
 NODE_DTYPE_WORDS = 8       # cvx_bvh_node: origin far_ (6 f32), index, len (u32)
 
 TRAVERSE_PACKET, TRAVERSE_SINGLE = 0, 1
+REFILL_AFTER_CAMERA, REFILL_ALL, REFILL_NONE = 0, 1, 2
 RNG_PATCH, RNG_GROUP = 0, 1
 MODE_MEGAKERNEL, MODE_WAVEFRONT = 0, 1
 
@@ -54,7 +55,8 @@ class _View(ctypes.Structure):
 
 class _ServerConfig(ctypes.Structure):
     _fields_ = [("framebuffer_bytes", ctypes.c_uint64), ("max_groups", ctypes.c_uint32),
-                ("traversal", ctypes.c_uint32), ("use_graph", ctypes.c_uint32), ("sequential", ctypes.c_uint32)]
+                ("traversal", ctypes.c_uint32), ("use_graph", ctypes.c_uint32), ("sequential", ctypes.c_uint32),
+                ("blocks_per_sm", ctypes.c_uint32), ("refill_mode", ctypes.c_uint32)]
 
 
 class _Request(ctypes.Structure):
@@ -69,7 +71,8 @@ class _Result(ctypes.Structure):
 
 class RenderConfig(ctypes.Structure):
     _fields_ = [("rng_order", ctypes.c_uint32), ("traversal", ctypes.c_uint32), ("mode", ctypes.c_uint32),
-                ("block_size", ctypes.c_uint32), ("use_graph", ctypes.c_uint32)]
+                ("block_size", ctypes.c_uint32), ("use_graph", ctypes.c_uint32), ("blocks_per_sm", ctypes.c_uint32),
+                ("refill_mode", ctypes.c_uint32)]
 
 
 def lib(build=False):
@@ -369,9 +372,9 @@ class Renderer:
     """renderer.rs:120-410 as whole-frame GPU calls."""
 
     def __init__(self, scene, width, height, rng_order=RNG_GROUP, traversal=TRAVERSE_PACKET,
-                 mode=MODE_MEGAKERNEL, block_size=0, use_graph=0):
+                 mode=MODE_MEGAKERNEL, block_size=0, use_graph=0, blocks_per_sm=0, refill_mode=REFILL_AFTER_CAMERA):
         self.scene, self.width, self.height = scene, width, height
-        self.config = RenderConfig(rng_order, traversal, mode, block_size, use_graph)
+        self.config = RenderConfig(rng_order, traversal, mode, block_size, use_graph, blocks_per_sm, refill_mode)
         out = ctypes.c_void_p()
         _check(lib().cvx_renderer_create(scene._h, width, height, ctypes.byref(self.config), ctypes.byref(out)))
         self._h = out
@@ -435,10 +438,10 @@ class Batch:
     """Many views of many resident scenes rendered in shared wavefronts."""
 
     def __init__(self, scenes, max_groups=1 << 20, max_pixels=1 << 24, traversal=TRAVERSE_SINGLE, use_graph=1,
-                 blocks_per_sm=0):
+                 blocks_per_sm=0, refill_mode=REFILL_AFTER_CAMERA):
         self.scenes = list(scenes)
         arr = (ctypes.c_void_p * len(self.scenes))(*[s._h.value for s in self.scenes])
-        cfg = RenderConfig(RNG_GROUP, traversal, MODE_WAVEFRONT, blocks_per_sm, use_graph)
+        cfg = RenderConfig(RNG_GROUP, traversal, MODE_WAVEFRONT, 0, use_graph, blocks_per_sm, refill_mode)
         out = ctypes.c_void_p()
         _check(lib().cvx_batch_create(arr, len(self.scenes), max_groups, max_pixels, ctypes.byref(cfg),
                                       ctypes.byref(out)))
@@ -462,10 +465,11 @@ class Server:
     """Continuously batched request server over resident scenes."""
 
     def __init__(self, scenes, framebuffer_bytes=4 << 30, max_groups=1 << 21, traversal=TRAVERSE_SINGLE,
-                 use_graph=1, sequential=False):
+                 use_graph=1, sequential=False, blocks_per_sm=0, refill_mode=REFILL_AFTER_CAMERA):
         self.scenes = list(scenes)
         arr = (ctypes.c_void_p * len(self.scenes))(*[s._h.value for s in self.scenes])
-        cfg = _ServerConfig(framebuffer_bytes, max_groups, traversal, use_graph, int(sequential))
+        cfg = _ServerConfig(framebuffer_bytes, max_groups, traversal, use_graph, int(sequential), blocks_per_sm,
+                            refill_mode)
         out = ctypes.c_void_p()
         _check(lib().cvx_server_create(arr, len(self.scenes), ctypes.byref(cfg), ctypes.byref(out)))
         self._h = out

@@ -1,0 +1,94 @@
+"""Autotuner for the render path: times candidate kernel organisations on the
+actual scene and frame size and keeps the fastest.
+
+Candidates (all give the same image for a given RNG order and traversal; the
+single-ray and packet traversals can differ only on t-ties and grazing rays):
+the fused megakernel at several block sizes, and the wavefront form with
+CUDA-graph replay at several persistent grid sizes and ray-refill modes, each
+with the single-ray and the 8-ray packet traversal. The traversal stack holds
+128 entries; a scene needs BVH depth + 2 (checked at scene creation), so stack
+depth is not a tuning knob: untouched entries cost nothing.
+
+Results are cached per (scene size, BVH depth, frame size, RNG order) in a
+JSON file (CONVECTOR_AUTOTUNE_CACHE, default ~/.cache/convector_gb300/autotune.json).
+"""
+
+import json
+import os
+
+from . import (MODE_MEGAKERNEL, MODE_WAVEFRONT, REFILL_AFTER_CAMERA, REFILL_ALL, REFILL_NONE, RNG_GROUP,
+               TRAVERSE_PACKET, TRAVERSE_SINGLE, Renderer)
+
+
+def _cache_path():
+    return os.environ.get("CONVECTOR_AUTOTUNE_CACHE",
+                          os.path.join(os.path.expanduser("~"), ".cache", "convector_gb300", "autotune.json"))
+
+
+def candidates(rng_order=RNG_GROUP, allow_packet=True):
+    """Render configurations (keyword dicts for Renderer) to try."""
+    out = []
+    travs = [TRAVERSE_SINGLE, TRAVERSE_PACKET] if allow_packet else [TRAVERSE_SINGLE]
+    for trav in travs:
+        for block in (64, 128, 256):
+            out.append(dict(rng_order=rng_order, traversal=trav, mode=MODE_MEGAKERNEL, block_size=block))
+    if rng_order == RNG_GROUP:
+        for bps in (8, 12, 16):
+            for refill in (REFILL_AFTER_CAMERA, REFILL_ALL, REFILL_NONE):
+                out.append(dict(rng_order=rng_order, traversal=TRAVERSE_SINGLE, mode=MODE_WAVEFRONT, use_graph=1,
+                                blocks_per_sm=bps, refill_mode=refill))
+            if allow_packet:
+                out.append(dict(rng_order=rng_order, traversal=TRAVERSE_PACKET, mode=MODE_WAVEFRONT, use_graph=1,
+                                blocks_per_sm=bps))
+    return out
+
+
+def measure(scene, width, height, config, frames=5, warmup=2, first_frame=1000):
+    """Median device milliseconds per frame of one configuration."""
+    r = Renderer(scene, width, height, **config)
+    for f in range(warmup):
+        r.render_frame_u8(first_frame + f, gbuffer=False)
+    ms = []
+    for f in range(frames):
+        r.render_frame_u8(first_frame + warmup + f, gbuffer=False)
+        ms.append(r.stats()[1])
+    ms.sort()
+    return ms[len(ms) // 2]
+
+
+def tune(scene, width, height, rng_order=RNG_GROUP, allow_packet=True, frames=5, use_cache=True):
+    """Returns (best config dict, {config key: ms}) for this scene and frame size."""
+    b = scene.bvh
+    key = "tris=%d nodes=%d depth=%d %dx%d rng=%d packet=%d" % (
+        b.triangles.shape[0], b.nodes.shape[0], b.depth, width, height, rng_order, int(allow_packet))
+    path = _cache_path()
+    cache = {}
+    if use_cache and os.path.exists(path):
+        try:
+            with open(path) as f:
+                cache = json.load(f)
+        except (OSError, ValueError):
+            cache = {}
+    if use_cache and key in cache:
+        return cache[key]["best"], cache[key]["table"]
+    table = {}
+    best, best_ms = None, None
+    for cfg in candidates(rng_order, allow_packet):
+        ms = measure(scene, width, height, cfg, frames=frames)
+        table[json.dumps(cfg, sort_keys=True)] = ms
+        if best_ms is None or ms < best_ms:
+            best, best_ms = cfg, ms
+    if use_cache:
+        cache[key] = {"best": best, "table": table}
+        try:
+            os.makedirs(os.path.dirname(path), exist_ok=True)
+            with open(path, "w") as f:
+                json.dump(cache, f, indent=1, sort_keys=True)
+        except OSError:
+            pass
+    return best, table
+
+
+def autotuned_renderer(scene, width, height, rng_order=RNG_GROUP, allow_packet=True):
+    best, _ = tune(scene, width, height, rng_order=rng_order, allow_packet=allow_packet)
+    return Renderer(scene, width, height, **best)

@@ -175,6 +175,8 @@ extern "C" {
 int32_t cvx_scene_create(const cvx_triangle* tris, uint32_t n_tris, const cvx_bvh_node* nodes, uint32_t n_nodes,
                          cvx_scene** out) {
     if (!tris || !nodes || !out || n_tris == 0) return set_error(CVX_ERR_INVALID, "null argument or empty scene");
+    if (n_tris >= (1u << 27) || n_nodes >= (1u << 27))
+        return set_error(CVX_ERR_INVALID, "scenes are limited to 2^27 triangles and 2^27 nodes");
     uint32_t depth = 0;
     int32_t st = validate_tree(nodes, n_nodes, n_tris, &depth);
     if (st) return st;
@@ -313,7 +315,8 @@ int32_t cvx_renderer_create(cvx_scene* scene, uint32_t w, uint32_t h, const cvx_
         return set_error(CVX_ERR_INVALID, "rendering needs at least one direct-sample triangle (scene.rs:143-161)");
     cvx_render_config c{};
     if (cfg) c = *cfg;
-    if (c.rng_order > 1 || c.traversal > 1 || c.mode > 1 || (c.block_size % 32) || c.block_size > 1024)
+    if (c.rng_order > 1 || c.traversal > 1 || c.mode > 1 || (c.block_size % 32) || c.block_size > 1024 ||
+        c.refill_mode > 2 || c.blocks_per_sm > 64)
         return set_error(CVX_ERR_INVALID, "bad render configuration");
     if (c.mode == CVX_MODE_WAVEFRONT && c.rng_order != CVX_RNG_GROUP)
         return set_error(CVX_ERR_INVALID,
@@ -343,7 +346,7 @@ int32_t cvx_renderer_create(cvx_scene* scene, uint32_t w, uint32_t h, const cvx_
     if (c.mode == CVX_MODE_WAVEFRONT) {
         r->engine.reset(new WaveEngine());
         if ((st = r->engine->init(groups_of(w, h), 1, c.traversal == CVX_TRAVERSE_PACKET, c.use_graph != 0,
-                                  c.block_size / 32)))
+                                  c.blocks_per_sm, refill_from(c.refill_mode))))
             return st;
         cvx_scene* sc[1] = {scene};
         if ((st = r->engine->set_scenes(sc, 1))) return st;

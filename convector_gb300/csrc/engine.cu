@@ -57,7 +57,8 @@ WaveEngine::~WaveEngine() {
 }
 
 int32_t WaveEngine::init(uint32_t max_groups, uint32_t max_jobs, bool packet, bool use_graph,
-                         uint32_t blocks_per_sm) {
+                         uint32_t blocks_per_sm, uint32_t refill_from) {
+    refill_from_ = refill_from;
     max_groups_ = max_groups;
     max_jobs_ = max_jobs;
     packet_ = packet;
@@ -112,7 +113,7 @@ static bool same_out(const WaveOutputs& a, const WaveOutputs& b) { return std::m
 
 int32_t WaveEngine::launch(const WaveOutputs& out, cudaStream_t stream) {
     if (!use_graph_) {
-        ECK(launch_wave(d_jobs_, d_hdr_, d_scenes_, st_, out, packet_, blocks_per_sm_, stream), "wave launch");
+        ECK(launch_wave(d_jobs_, d_hdr_, d_scenes_, st_, out, packet_, blocks_per_sm_, refill_from_, stream), "wave launch");
         return CVX_OK;
     }
     for (auto& g : graphs_)
@@ -122,7 +123,7 @@ int32_t WaveEngine::launch(const WaveOutputs& out, cudaStream_t stream) {
         }
     cudaGraph_t graph;
     ECK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal), "begin capture");
-    cudaError_t e = launch_wave(d_jobs_, d_hdr_, d_scenes_, st_, out, packet_, blocks_per_sm_, stream);
+    cudaError_t e = launch_wave(d_jobs_, d_hdr_, d_scenes_, st_, out, packet_, blocks_per_sm_, refill_from_, stream);
     cudaError_t e2 = cudaStreamEndCapture(stream, &graph);
     if (e != cudaSuccess) return cuda_err(e, "capture wave");
     if (e2 != cudaSuccess) return cuda_err(e2, "end capture");
@@ -223,7 +224,7 @@ extern "C" int32_t cvx_batch_create(cvx_scene* const* scenes, uint32_t n_scenes,
     b->max_pixels = max_pixels;
     ECK(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking), "cudaStreamCreate");
     int32_t st = b->engine.init(max_groups, 4096, c.traversal == CVX_TRAVERSE_PACKET, c.use_graph != 0,
-                                c.block_size /* blocks per SM for the wave kernels */);
+                                c.blocks_per_sm, refill_from(c.refill_mode));
     if (st) return st;
     if ((st = b->engine.set_scenes(scenes, n_scenes))) return st;
     std::vector<void*> owned;
@@ -536,7 +537,8 @@ extern "C" int32_t cvx_server_create(cvx_scene* const* scenes, uint32_t n_scenes
     s->scenes.assign(scenes, scenes + n_scenes);
     s->cfg = *cfg;
     ECK(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking), "cudaStreamCreate");
-    int32_t st = s->engine.init(cfg->max_groups, 1024, cfg->traversal == CVX_TRAVERSE_PACKET, cfg->use_graph != 0, 0);
+    int32_t st = s->engine.init(cfg->max_groups, 1024, cfg->traversal == CVX_TRAVERSE_PACKET, cfg->use_graph != 0,
+                                cfg->blocks_per_sm, refill_from(cfg->refill_mode));
     if (st) return st;
     if ((st = s->engine.set_scenes(scenes, n_scenes))) return st;
     s->pool_px = cfg->framebuffer_bytes / 16;  // 12 B accumulator + 4 B RGBA per pixel

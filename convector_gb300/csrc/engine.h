@@ -14,12 +14,15 @@ DeviceScene scene_view(const cvx_scene* s);
 cudaStream_t scene_stream(const cvx_scene* s);
 uint32_t scene_num_lights(const cvx_scene* s);
 uint32_t groups_of(uint32_t w, uint32_t h);
+// First bounce traversed with ray refill for a CVX_REFILL_* mode.
+inline uint32_t refill_from(uint32_t refill_mode) { return refill_mode == 1 ? 0u : refill_mode == 2 ? 5u : 1u; }
 
 class WaveEngine {
    public:
     ~WaveEngine();
     // max_groups: ray-queue capacity (8-pixel groups) of one wave.
-    int32_t init(uint32_t max_groups, uint32_t max_jobs, bool packet, bool use_graph, uint32_t blocks_per_sm);
+    int32_t init(uint32_t max_groups, uint32_t max_jobs, bool packet, bool use_graph, uint32_t blocks_per_sm,
+                 uint32_t refill_from = 1);
     int32_t set_scenes(cvx_scene* const* scenes, uint32_t n);
     // Runs one wave synchronously on `stream`; group_base / n_groups of the
     // jobs are filled in here. rays, job_rays and ms may be null.
@@ -43,7 +46,7 @@ class WaveEngine {
     unsigned long long* d_rays_ = nullptr;
     unsigned long long* d_job_rays_ = nullptr;
     uint32_t* d_err_ = nullptr;
-    uint32_t n_scenes_ = 0, scene_cap_ = 0, max_groups_ = 0, max_jobs_ = 0, blocks_per_sm_ = 0;
+    uint32_t n_scenes_ = 0, scene_cap_ = 0, max_groups_ = 0, max_jobs_ = 0, blocks_per_sm_ = 0, refill_from_ = 1;
     bool packet_ = false, use_graph_ = false;
     std::vector<void*> owned_;
     std::vector<Graph> graphs_;

@@ -20,8 +20,11 @@ cudaError_t launch_render(const DeviceScene& s, const DeviceCamera& cam, uint32_
                           bool packet, bool patch_order, uint32_t* rgba, uint32_t* gbuf, float* color, float* accum,
                           unsigned long long* rays, uint32_t* err, uint32_t block, cudaStream_t st);
 cudaError_t launch_resolve(const float* accum, uint32_t npx, float factor, uint32_t* rgba, cudaStream_t st);
+// refill_from: first bounce whose single-ray traversal uses ray refill (the
+// earlier ones traverse one octet per group); packet traversal ignores it.
 cudaError_t launch_wave(const Job* jobs, const WaveHeader* hdr, const DeviceScene* scenes, const WaveState& st,
-                        const WaveOutputs& out, bool packet, uint32_t blocks_per_sm, cudaStream_t stream);
+                        const WaveOutputs& out, bool packet, uint32_t blocks_per_sm, uint32_t refill_from,
+                        cudaStream_t stream);
 cudaError_t launch_resolve_multi(const ResolveItem* items, uint32_t n_items, const float* accum, uint32_t* rgba,
                                  cudaStream_t stream);
 

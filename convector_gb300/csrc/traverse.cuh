@@ -138,12 +138,24 @@ __device__ __forceinline__ bool traverse(const DeviceScene& s, F3 o, F3 d, bool 
     return ok;
 }
 
+// Stack entry of the refill traversal: a packed node reference and the box's
+// entry distance, 8 bytes. ref = (index << 5) | len: len 0 is an internal node
+// (index = its first child), len 1..30 a leaf of len triangles at index; len
+// 31 escapes larger leaves (index = the node's own id, its (index, len) are
+// read from the node pair). Indices are below 2^27 (checked at scene creation).
+__device__ __forceinline__ uint32_t node_ref(uint32_t node_id, uint32_t index, uint32_t len) {
+    return len < 31u ? (index << 5) | len : (node_id << 5) | 31u;
+}
+
 // Persistent single-ray traversal with ray refill over rays 0..n-1 of `src`.
-// Every iteration each lane pops one stack entry and processes it (a node
-// pair or a leaf); a lane whose ray is finished takes the next unclaimed ray
-// (one warp-aggregated atomic on `next_ray`), so warps stay full while rays of
-// different lengths finish. Per-ray decisions are exactly those of
-// traverse<false>. The whole warp must call this. `src` provides
+// Every iteration each lane processes one node pair or one leaf; a lane whose
+// ray is finished takes the next unclaimed ray (one warp-aggregated atomic on
+// `next_ray`), so warps stay full while rays of different lengths finish.
+// Decisions and their order are exactly those of traverse<false>: after a
+// pair test the child the reference would pop next is processed at once
+// (its cull test sees the same hit distance the pop would), the other one is
+// pushed, and culled entries are popped within the same iteration.
+// The whole warp must call this. `src` provides
 //   bool load(r, F3& o, F3& d, float& far, const float4*& nodes, const float4*& geom)
 //        (false: nothing to trace for r; load then stores r's result itself)
 //   void store(r, const Hit&, uint32_t boxes, uint32_t triangles)
@@ -151,15 +163,15 @@ __device__ __forceinline__ bool traverse(const DeviceScene& s, F3 o, F3 d, bool 
 template <class Src>
 __device__ __forceinline__ bool traverse_refill(const Src& src, uint32_t n, uint32_t* next_ray,
                                                 const ApproxTables& tab) {
+    const int lane = threadIdx.x & 31;
     const float4* nodes = nullptr;
     const float4* geom = nullptr;
-    const int lane = threadIdx.x & 31;
-    uint32_t st_idx[kStackDepth];
-    uint32_t st_len[kStackDepth];
-    float st_t[kStackDepth];
+    uint2 stack[kStackDepth];  // (ref, entry distance bits)
     int sp = 0;
-    uint32_t ray = 0, na = 0, nt = 0, pair = 0;
-    bool have = false, done = false, overflow = false, pending_pair = false;
+    uint32_t ray = 0, na = 0, nt = 0;
+    uint32_t cur = 0;  // ref of the node to process; kNone: pop
+    const uint32_t kNone = 0xffffffffu;
+    bool have = false, done = false, overflow = false;
     F3 o = f3(0, 0, 0), d = f3(0, 0, 0), inv = f3(0, 0, 0);
     Hit h{0.0f, 0.0f, 0.0f, -1};
     for (;;) {
@@ -181,8 +193,7 @@ __device__ __forceinline__ bool traverse_refill(const Src& src, uint32_t n, uint
                         sp = 0;
                         na = 2;
                         nt = 0;
-                        pair = 0;
-                        pending_pair = true;
+                        cur = 0;  // the root pair: internal ref with index 0
                         have = true;
                     }
                 } else {
@@ -192,45 +203,56 @@ __device__ __forceinline__ bool traverse_refill(const Src& src, uint32_t n, uint
         }
         if (__all_sync(0xffffffffu, done)) break;
         if (!have) continue;
-        if (!pending_pair) {
-            if (sp == 0) {
+        if (cur == kNone) {
+            // Pop until an entry survives the cull test (aabb.rs:171-177).
+            while (sp > 0) {
+                uint2 e = stack[--sp];
+                if (!geq(__uint_as_float(e.y), h.t)) {
+                    cur = e.x;
+                    break;
+                }
+            }
+            if (cur == kNone) {
                 src.store(ray, h, na, nt);
                 have = false;
                 continue;
             }
-            sp--;
-            uint32_t idx = st_idx[sp], len = st_len[sp];
-            if (geq(st_t[sp], h.t)) continue;
-            if (len != 0u) {
-                for (uint32_t i = idx; i < idx + len; i++) tri_test(geom, i, o, d, true, h);
-                nt += len;
-                continue;
-            }
-            na += 2;
-            pair = idx >> 1;
         }
-        pending_pair = false;
-        const float4* np = nodes + 4 * pair;
+        uint32_t len = cur & 31u, idx = cur >> 5;
+        if (len == 31u) {  // escaped leaf: read its (index, len) from the node pair
+            uint32_t id = idx;
+            float4 q3 = __ldg(nodes + 4 * (id >> 1) + 3);
+            idx = __float_as_uint((id & 1u) ? q3.z : q3.x);
+            len = __float_as_uint((id & 1u) ? q3.w : q3.y);
+        }
+        if (len != 0u) {
+            for (uint32_t i = idx; i < idx + len; i++) tri_test(geom, i, o, d, true, h);
+            nt += len;
+            cur = kNone;
+            continue;
+        }
+        if (cur != 0u) na += 2;  // every pair but the root pair (bvh.rs:604-634)
+        const float4* np = nodes + 4 * (idx >> 1);
         float4 q0 = __ldg(np), q1 = __ldg(np + 1), q2 = __ldg(np + 2), q3 = __ldg(np + 3);
         BoxT b0 = box_test(q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, o, inv);
         BoxT b1 = box_test(q1.z, q1.w, q2.x, q2.y, q2.z, q2.w, o, inv);
         bool first0 = !sneg(b0.tmin - b1.tmin);
         bool hit0 = b0.mask & !sneg(b0.tmax);
         bool hit1 = b1.mask & !sneg(b1.tmax);
-        if (sp + (int)hit0 + (int)hit1 > kStackDepth) {
+        uint32_t r0 = node_ref(idx, __float_as_uint(q3.x), __float_as_uint(q3.y));
+        uint32_t r1 = node_ref(idx + 1u, __float_as_uint(q3.z), __float_as_uint(q3.w));
+        // The reference pushes `first` then `second` and pops `second` first.
+        bool hit_first = first0 ? hit0 : hit1, hit_second = first0 ? hit1 : hit0;
+        uint32_t ref_first = first0 ? r0 : r1, ref_second = first0 ? r1 : r0;
+        float t_first = first0 ? b0.tmin : b1.tmin, t_second = first0 ? b1.tmin : b0.tmin;
+        if (sp + (int)hit_first + (int)hit_second > kStackDepth) {
             overflow = true;
             sp = 0;
+            cur = kNone;
             continue;
         }
-        uint32_t i0 = __float_as_uint(q3.x), l0 = __float_as_uint(q3.y);
-        uint32_t i1 = __float_as_uint(q3.z), l1 = __float_as_uint(q3.w);
-        if (first0) {
-            if (hit0) { st_idx[sp] = i0; st_len[sp] = l0; st_t[sp] = b0.tmin; sp++; }
-            if (hit1) { st_idx[sp] = i1; st_len[sp] = l1; st_t[sp] = b1.tmin; sp++; }
-        } else {
-            if (hit1) { st_idx[sp] = i1; st_len[sp] = l1; st_t[sp] = b1.tmin; sp++; }
-            if (hit0) { st_idx[sp] = i0; st_len[sp] = l0; st_t[sp] = b0.tmin; sp++; }
-        }
+        if (hit_first) stack[sp++] = make_uint2(ref_first, __float_as_uint(t_first));
+        cur = (hit_second && !geq(t_second, h.t)) ? ref_second : kNone;
     }
     return !overflow;
 }

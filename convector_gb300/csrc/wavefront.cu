@@ -119,10 +119,13 @@ __global__ void __launch_bounds__(128) k_wf_raygen(const Job* __restrict__ jobs,
     }
 }
 
-// Packet traversal: one octet per queued group, decisions over the octet.
-__global__ void __launch_bounds__(128) k_wf_traverse_packet(const Job* __restrict__ jobs,
-                                                            const DeviceScene* __restrict__ scenes, WaveState st,
-                                                            int bounce, WaveOutputs out) {
+// One octet per queued group: decisions over the octet (PACKET) or each lane
+// over its own ray (single, without refill: suits the coherent camera rays,
+// whose adjacent pixels share a warp).
+template <bool PACKET>
+__global__ void __launch_bounds__(128) k_wf_traverse_octet(const Job* __restrict__ jobs,
+                                                           const DeviceScene* __restrict__ scenes, WaveState st,
+                                                           int bounce, WaveOutputs out) {
     __shared__ ApproxTables tab;
     load_tables_wf(tab);
     const int k = threadIdx.x & 7;
@@ -138,7 +141,7 @@ __global__ void __launch_bounds__(128) k_wf_traverse_packet(const Job* __restric
         bool active = (st.flags[l] & 1u) != 0u;
         F3 o = f3(st.ox[l], st.oy[l], st.oz[l]), d = f3(st.dx[l], st.dy[l], st.dz[l]);
         Hit h{1.0e5f, 0.0f, 0.0f, -1};
-        ok &= traverse<true>(s, o, d, active, omask, h, tab, nullptr);
+        if (PACKET || active) ok &= traverse<PACKET>(s, o, d, active, omask, h, tab, nullptr);
         st.ht[l] = h.t;
         st.hu[l] = h.u;
         st.hv[l] = h.v;
@@ -321,7 +324,8 @@ static int sms() {
 }
 
 cudaError_t launch_wave(const Job* jobs, const WaveHeader* hdr, const DeviceScene* scenes, const WaveState& st,
-                        const WaveOutputs& out, bool packet, uint32_t blocks_per_sm, cudaStream_t stream) {
+                        const WaveOutputs& out, bool packet, uint32_t blocks_per_sm, uint32_t refill_from,
+                        cudaStream_t stream) {
     if (blocks_per_sm == 0) blocks_per_sm = 12;
     uint32_t grid = (uint32_t)sms() * blocks_per_sm;
     // counts[0..5]: queue lengths per bounce; counts[6..10]: ray counters of
@@ -330,7 +334,8 @@ cudaError_t launch_wave(const Job* jobs, const WaveHeader* hdr, const DeviceScen
     if (e != cudaSuccess) return e;
     k_wf_raygen<<<grid, 128, 0, stream>>>(jobs, hdr, st);
     for (int b = 0; b < 5; b++) {
-        if (packet) k_wf_traverse_packet<<<grid, 128, 0, stream>>>(jobs, scenes, st, b, out);
+        if (packet) k_wf_traverse_octet<true><<<grid, 128, 0, stream>>>(jobs, scenes, st, b, out);
+        else if ((uint32_t)b < refill_from) k_wf_traverse_octet<false><<<grid, 128, 0, stream>>>(jobs, scenes, st, b, out);
         else k_wf_traverse_single<<<grid, 128, 0, stream>>>(jobs, scenes, st, b, out);
         k_wf_shade<<<grid, 128, 0, stream>>>(jobs, scenes, st, b, out);
     }

@@ -167,12 +167,19 @@ enum { CVX_RNG_PATCH = 0, CVX_RNG_GROUP = 1 };
  * queues with compaction), optionally replayed as a CUDA graph. */
 enum { CVX_MODE_MEGAKERNEL = 0, CVX_MODE_WAVEFRONT = 1 };
 
+/* Wavefront single-ray traversal: which bounces fetch rays with refill
+ * (persistent lanes take the next ray when theirs finishes) rather than one
+ * octet per group (coherent camera rays share warps with their neighbours). */
+enum { CVX_REFILL_AFTER_CAMERA = 0, CVX_REFILL_ALL = 1, CVX_REFILL_NONE = 2 };
+
 typedef struct cvx_render_config {
-    uint32_t rng_order;   /* CVX_RNG_* */
-    uint32_t traversal;   /* CVX_TRAVERSE_* */
-    uint32_t mode;        /* CVX_MODE_* */
-    uint32_t block_size;  /* threads per block, multiple of 32 (0: default) */
-    uint32_t use_graph;   /* wavefront mode: capture the bounce loop in a CUDA graph */
+    uint32_t rng_order;     /* CVX_RNG_* */
+    uint32_t traversal;     /* CVX_TRAVERSE_* */
+    uint32_t mode;          /* CVX_MODE_* */
+    uint32_t block_size;    /* megakernel: threads per block, multiple of 32 (0: 128) */
+    uint32_t use_graph;     /* wavefront: capture the bounce loop in a CUDA graph */
+    uint32_t blocks_per_sm; /* wavefront: persistent blocks per SM (0: 12) */
+    uint32_t refill_mode;   /* wavefront: CVX_REFILL_* */
 } cvx_render_config;
 
 /* Renderer::new (renderer.rs:121-130). Any width and height are accepted;
@@ -239,6 +246,8 @@ typedef struct cvx_server_config {
     uint32_t traversal;         /* CVX_TRAVERSE_* */
     uint32_t use_graph;
     uint32_t sequential;        /* 1: one request at a time (the plain path, for comparison) */
+    uint32_t blocks_per_sm;     /* persistent blocks per SM (0: 12) */
+    uint32_t refill_mode;       /* CVX_REFILL_* */
 } cvx_server_config;
 
 typedef struct cvx_request {

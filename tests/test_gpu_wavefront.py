@@ -27,13 +27,13 @@ def two_scenes(gpu, orc):
     return out
 
 
-@pytest.mark.parametrize("traversal", [0, 1])
+@pytest.mark.parametrize("traversal,refill_mode", [(0, 0), (1, 0), (1, 1), (1, 2)])
 @pytest.mark.parametrize("use_graph", [0, 1])
-def test_wavefront_frame_bitexact(two_scenes, gpu, orc, traversal, use_graph):
+def test_wavefront_frame_bitexact(two_scenes, gpu, orc, traversal, refill_mode, use_graph):
     bvh, scene, osc = two_scenes[0]
     w, h = 200, 120
     r = gpu.Renderer(scene, w, h, rng_order=gpu.RNG_GROUP, traversal=traversal, mode=gpu.MODE_WAVEFRONT,
-                     use_graph=use_graph)
+                     use_graph=use_graph, refill_mode=refill_mode, blocks_per_sm=4 + 4 * refill_mode)
     for frame in (42, 43):
         rgba, gb = r.render_frame_u8(frame)
         col = r.read_frame_f32()
