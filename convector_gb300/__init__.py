@@ -22,7 +22,7 @@ import numpy as np
 
 from . import _build
 
-__all__ = ["SMaterial", "Mesh", "Bvh", "Scene", "Camera", "Renderer", "RenderConfig", "Batch", "View", "Server",
+__all__ = ["SMaterial", "Mesh", "Bvh", "Scene", "Camera", "Renderer", "RenderConfig", "Batch", "View", "Server", "Display",
            "CvxError", "lib", "TRIANGLE_DTYPE_WORDS", "NODE_DTYPE_WORDS"]
 
 TRIANGLE_DTYPE_WORDS = 16  # cvx_triangle: v0 v1 v2 (9 f32), uv0..2 (6 f32), material (u32)
@@ -131,6 +131,10 @@ def lib(build=False):
         "cvx_server_cancel": (I32, [P, ctypes.c_uint64]),
         "cvx_server_stats": (I32, [P, P, P, P, P]),
         "cvx_server_destroy": (None, [P]),
+        "cvx_renderer_set_debug_view": (I32, [P, U32]),
+        "cvx_display_create": (I32, [U32, U32, P, P, U32, U32, P]),
+        "cvx_display_frame": (I32, [P, P, P, U32, U32, P]),
+        "cvx_display_destroy": (None, [P]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -383,6 +387,11 @@ class Renderer:
     def set_camera(self, camera):
         _check(lib().cvx_renderer_set_camera(self._h, ctypes.byref(camera._c)))
 
+    def toggle_debug_view(self, enable=None):
+        """Renderer::toggle_debug_view (renderer.rs:150-152); with an argument, sets it."""
+        self.debug_view = (not getattr(self, "debug_view", False)) if enable is None else bool(enable)
+        _check(lib().cvx_renderer_set_debug_view(self._h, int(self.debug_view)))
+
     def render_frame_u8(self, frame_number, gbuffer=True):
         rgba = np.empty((self.height, self.width), dtype=np.uint32)
         gb = np.empty((self.height, self.width), dtype=np.uint32) if gbuffer else None
@@ -420,6 +429,36 @@ class Renderer:
     def __del__(self):
         if getattr(self, "_h", None) and self._h.value and _LIB is not None:
             _LIB.cvx_renderer_destroy(self._h)
+            self._h = None
+
+
+class Display:
+    """Window::display_buffer (ui.rs:313-364) on headless device buffers: the
+    gbuffer texture composite, the 8-frame blend and the XYZ median filter of
+    src/gpu/*.glsl, restated as CUDA kernels. tex1/tex2: (h, w, 3) uint8 sRGB."""
+
+    def __init__(self, width, height, tex1, tex2):
+        self.width, self.height = width, height
+        self._t1 = np.ascontiguousarray(tex1, dtype=np.uint8)
+        self._t2 = np.ascontiguousarray(tex2, dtype=np.uint8)
+        assert self._t1.shape == self._t2.shape and self._t1.shape[2] == 3
+        out = ctypes.c_void_p()
+        _check(lib().cvx_display_create(width, height, _ptr(self._t1), _ptr(self._t2), self._t1.shape[1],
+                                        self._t1.shape[0], ctypes.byref(out)))
+        self._h = out
+        self.enable_blend, self.enable_median = True, True
+
+    def display_buffer(self, rgba, gbuffer):
+        out = np.empty((self.height, self.width), dtype=np.uint32)
+        a = np.ascontiguousarray(rgba, dtype=np.uint32)
+        g = np.ascontiguousarray(gbuffer, dtype=np.uint32)
+        _check(lib().cvx_display_frame(self._h, _ptr(a), _ptr(g), int(self.enable_blend), int(self.enable_median),
+                                       _ptr(out)))
+        return out
+
+    def __del__(self):
+        if getattr(self, "_h", None) and self._h.value and _LIB is not None:
+            _LIB.cvx_display_destroy(self._h)
             self._h = None
 
 

@@ -30,7 +30,7 @@ def candidates(rng_order=RNG_GROUP, allow_packet=True):
     out = []
     travs = [TRAVERSE_SINGLE, TRAVERSE_PACKET] if allow_packet else [TRAVERSE_SINGLE]
     for trav in travs:
-        for block in (64, 128, 256):
+        for block in (64, 128):  # the fused kernels are compiled for at most 128 threads per block
             out.append(dict(rng_order=rng_order, traversal=trav, mode=MODE_MEGAKERNEL, block_size=block))
     if rng_order == RNG_GROUP:
         for bps in (8, 12, 16):

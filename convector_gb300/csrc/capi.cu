@@ -132,6 +132,7 @@ struct cvx_renderer {
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     uint64_t last_rays = 0;
     float last_ms = 0.0f;
+    bool debug = false;
     ~cvx_renderer() {
         cudaFree(d_rgba);
         cudaFree(d_gbuf);
@@ -315,7 +316,7 @@ int32_t cvx_renderer_create(cvx_scene* scene, uint32_t w, uint32_t h, const cvx_
         return set_error(CVX_ERR_INVALID, "rendering needs at least one direct-sample triangle (scene.rs:143-161)");
     cvx_render_config c{};
     if (cfg) c = *cfg;
-    if (c.rng_order > 1 || c.traversal > 1 || c.mode > 1 || (c.block_size % 32) || c.block_size > 1024 ||
+    if (c.rng_order > 1 || c.traversal > 1 || c.mode > 1 || (c.block_size % 32) || c.block_size > 128 ||
         c.refill_mode > 2 || c.blocks_per_sm > 64)
         return set_error(CVX_ERR_INVALID, "bad render configuration");
     if (c.mode == CVX_MODE_WAVEFRONT && c.rng_order != CVX_RNG_GROUP)
@@ -392,14 +393,15 @@ static int32_t run_frame_wavefront(cvx_renderer* r, uint32_t frame, bool accumul
 }
 
 static int32_t run_frame(cvx_renderer* r, uint32_t frame, bool accumulate, uint32_t* rgba, uint32_t* gbuf) {
-    if (r->engine) return run_frame_wavefront(r, frame, accumulate, rgba, gbuf);
+    if (r->engine && !r->debug) return run_frame_wavefront(r, frame, accumulate, rgba, gbuf);
     size_t npx = (size_t)r->w * r->h;
     CK(cudaMemsetAsync(r->d_rays, 0, 8, r->stream), "reset counters");
     CK(cudaMemsetAsync(r->d_err, 0, 4, r->stream), "reset status");
     CK(cudaEventRecord(r->e0, r->stream), "event");
     CK(launch_render(r->scene->view(), r->cam, r->w, r->h, frame, r->cfg.traversal == CVX_TRAVERSE_PACKET,
                      r->cfg.rng_order == CVX_RNG_PATCH, accumulate ? nullptr : r->d_rgba, r->d_gbuf, r->d_color,
-                     accumulate ? r->d_accum : nullptr, r->d_rays, r->d_err, r->cfg.block_size, r->stream),
+                     accumulate ? r->d_accum : nullptr, r->d_rays, r->d_err, r->cfg.block_size, r->debug,
+                     r->stream),
        "render launch");
     CK(cudaEventRecord(r->e1, r->stream), "event");
     if (rgba) CK(cudaMemcpyAsync(rgba, r->d_rgba, npx * 4, cudaMemcpyDeviceToHost, r->stream), "copy colour");
@@ -412,6 +414,12 @@ static int32_t run_frame(cvx_renderer* r, uint32_t frame, bool accumulate, uint3
     cudaEventElapsedTime(&r->last_ms, r->e0, r->e1);
     r->last_rays = rays;
     if (err) return set_error(CVX_ERR_DEVICE, "traversal stack overflow reported by the kernel");
+    return CVX_OK;
+}
+
+int32_t cvx_renderer_set_debug_view(cvx_renderer* r, uint32_t enable) {
+    if (!r) return set_error(CVX_ERR_INVALID, "null renderer");
+    r->debug = enable != 0;
     return CVX_OK;
 }
 

@@ -148,6 +148,7 @@ struct FrameArgs {
     float* accum;
     unsigned long long* rays;
     uint32_t* err;
+    uint32_t debug;  // Renderer::toggle_debug_view (renderer.rs:150-152)
 };
 
 // Screen x (or y) of lane k of group g of the 16x4 block at (xb, yb), before
@@ -215,7 +216,8 @@ __global__ void __launch_bounds__(128) k_render_group(FrameArgs a) {
         x = fmaf(unit_from(rng.next()), scale, x);
         y = fmaf(unit_from(rng.next()), scale, y);
         PixelOut p;
-        ok &= render_pixels<PACKET>(a.s, a.cam, x, y, rng, omask, tab, p, rays);
+        if (a.debug) ok &= render_pixels_debug<PACKET>(a.s, a.cam, x, y, omask, tab, p, rays);
+        else ok &= render_pixels<PACKET>(a.s, a.cam, x, y, rng, omask, tab, p, rays);
         store_pixel(a, gx + (uint32_t)(k & 3), gy + (uint32_t)(k >> 2), p);
     }
     if (!ok) atomicOr(a.err, kErrStackOverflow);
@@ -249,7 +251,8 @@ __global__ void __launch_bounds__(128) k_render_patch(FrameArgs a) {
                     x = fmaf(jx[g], scale, x);
                     y = fmaf(jy[g], scale, y);
                     PixelOut p;
-                    ok &= render_pixels<PACKET>(a.s, a.cam, x, y, rng, omask, tab, p, rays);
+                    if (a.debug) ok &= render_pixels_debug<PACKET>(a.s, a.cam, x, y, omask, tab, p, rays);
+                    else ok &= render_pixels<PACKET>(a.s, a.cam, x, y, rng, omask, tab, p, rays);
                     store_pixel(a, xb + 4u * (uint32_t)(g >> 1) + (uint32_t)(k & 3),
                                 yb + 2u * (uint32_t)(g & 1) + (uint32_t)(k >> 2), p);
                 }
@@ -336,8 +339,8 @@ cudaError_t launch_intersect(const DeviceScene& s, const float* rays, uint32_t n
 
 cudaError_t launch_render(const DeviceScene& s, const DeviceCamera& cam, uint32_t w, uint32_t h, uint32_t frame,
                           bool packet, bool patch_order, uint32_t* rgba, uint32_t* gbuf, float* color, float* accum,
-                          unsigned long long* rays, uint32_t* err, uint32_t block, cudaStream_t st) {
-    FrameArgs a{s, cam, w, h, frame, rgba, gbuf, color, accum, rays, err};
+                          unsigned long long* rays, uint32_t* err, uint32_t block, bool debug, cudaStream_t st) {
+    FrameArgs a{s, cam, w, h, frame, rgba, gbuf, color, accum, rays, err, debug ? 1u : 0u};
     if (block == 0) block = 128;
     if (patch_order) {
         uint32_t units = ((w + 31) / 32) * ((h + 31) / 32);

@@ -277,6 +277,27 @@ __device__ __forceinline__ bool render_pixels(const DeviceScene& s, const Device
     return ok;
 }
 
+// renderer.rs:470-486: the debug view of one lane. The time is 0 (no random
+// draw); green and blue are log2 of the boxes and triangles the packet (or the
+// ray, SINGLE) tested, times 0.1. log2 is taken in double and rounded to
+// float, which equals a correctly rounded f32 log2.
+template <bool PACKET>
+__device__ __forceinline__ bool render_pixels_debug(const DeviceScene& s, const DeviceCamera& cam, float x, float y,
+                                                    unsigned omask, const ApproxTables& tab, PixelOut& out,
+                                                    uint32_t& rays) {
+    F3 o, d;
+    camera_ray(cam, x, y, 0.0f, tab, o, d);
+    Hit h{1.0e5f, 0.0f, 0.0f, -1};
+    Counters c{0u, 0u};
+    bool ok = traverse<PACKET>(s, o, d, true, omask, h, tab, &c);
+    rays += 1u;
+    float g = (float)log2((double)c.aabb) * 0.1f, b = (float)log2((double)c.tri) * 0.1f;
+    out.color = f3(0.0f, g, b);
+    out.tex = 0;
+    out.tu = out.tv = out.fresnel = 0.0f;
+    return ok;
+}
+
 __device__ __forceinline__ uint32_t pack_color(F3 c) {  // renderer.rs:239-256
     float r = xmin(1.0f, c.x * 2.0f) * 255.0f, g = xmin(1.0f, c.y * 2.0f) * 255.0f,
           b = xmin(1.0f, c.z * 2.0f) * 255.0f;

@@ -176,7 +176,7 @@ typedef struct cvx_render_config {
     uint32_t rng_order;     /* CVX_RNG_* */
     uint32_t traversal;     /* CVX_TRAVERSE_* */
     uint32_t mode;          /* CVX_MODE_* */
-    uint32_t block_size;    /* megakernel: threads per block, multiple of 32 (0: 128) */
+    uint32_t block_size;    /* megakernel: threads per block, 32, 64, 96 or 128 (0: 128) */
     uint32_t use_graph;     /* wavefront: capture the bounce loop in a CUDA graph */
     uint32_t blocks_per_sm; /* wavefront: persistent blocks per SM (0: 12) */
     uint32_t refill_mode;   /* wavefront: CVX_REFILL_* */
@@ -189,6 +189,10 @@ int32_t cvx_renderer_create(cvx_scene* scene, uint32_t width, uint32_t height, c
 void cvx_renderer_destroy(cvx_renderer* r);
 /* The scene's camera (scene.rs:103 `pub camera`). */
 int32_t cvx_renderer_set_camera(cvx_renderer* r, const cvx_camera* cam);
+/* Renderer::toggle_debug_view (renderer.rs:150-152): frames show log2 of the
+ * boxes (green) and triangles (blue) tested per packet, times 0.1
+ * (renderer.rs:470-486). The debug view always runs the fused kernel. */
+int32_t cvx_renderer_set_debug_view(cvx_renderer* r, uint32_t enable);
 /* Renderer::render_patch_u8 (renderer.rs:306-327) over every patch of the
  * frame: RGBA8 colour and gbuffer words, row-major, row 0 at the bottom
  * (renderer.rs:210-235 stores rows bottom-up). Either output may be NULL. */
@@ -276,6 +280,23 @@ int32_t cvx_server_cancel(cvx_server* s, uint64_t id);
 /* The server clock (seconds), waves run, rays traced and device busy time. */
 int32_t cvx_server_stats(cvx_server* s, double* now_s, uint64_t* waves, uint64_t* rays, double* busy_s);
 void cvx_server_destroy(cvx_server* s);
+
+/* ---- device: display post-process ----------------------------------------
+ * Window::display_buffer (ui.rs:313-364) and the shaders it runs
+ * (src/gpu/gbuffer.glsl, blend.glsl, median.glsl, id.glsl), restated as CUDA
+ * kernels over device buffers instead of OpenGL textures: the gbuffer
+ * composite of the material textures into a ring of 8 frames, the mean of the
+ * ring (or the newest frame), the 5-tap median in CIE XYZ (or the identity),
+ * and the sRGB encode of the window's framebuffer. Textures are RGB8 sRGB,
+ * tex_w x tex_h, for texture indices 1 and 2. */
+typedef struct cvx_display cvx_display;
+int32_t cvx_display_create(uint32_t width, uint32_t height, const uint8_t* texture1_rgb, const uint8_t* texture2_rgb,
+                           uint32_t tex_w, uint32_t tex_h, cvx_display** out);
+/* One displayed frame from a rendered frame and its gbuffer (host buffers);
+ * out_srgb receives sRGB RGBA8, row-major, row 0 at the bottom. */
+int32_t cvx_display_frame(cvx_display* d, const uint32_t* rgba, const uint32_t* gbuffer, uint32_t enable_blend,
+                          uint32_t enable_median, uint32_t* out_srgb);
+void cvx_display_destroy(cvx_display* d);
 
 #ifdef __cplusplus
 }

@@ -581,6 +581,38 @@ void render_pixels(const Scene& s, const Camera& cam, const float xs[8], const f
     }
 }
 
+// renderer.rs:470-486 for one 8-pixel group: time 0 (no random draw), colour
+// (0, log2(boxes) * 0.1, log2(triangles) * 0.1) from the packet's counters
+// (or each ray's, single-ray traversal). log2 in double rounded to float.
+void render_pixels_debug(const Scene& s, const Camera& cam, const float xs[8], const float ys[8], bool single,
+                         PixelOut out[8], uint64_t* rays) {
+    Ray ray[8];
+    bool active[8];
+    Isect is[8];
+    for (int j = 0; j < 8; j++) {
+        ray[j] = camera_ray(cam, xs[j], ys[j], 0.0f);
+        active[j] = true;
+        is[j] = far_isect(ray[j], 1.0e5f);
+    }
+    uint32_t na[8], nt[8];
+    if (!single) {
+        uint32_t a = 0, b = 0;
+        packet_traverse(s, ray, active, is, &a, &b);
+        for (int j = 0; j < 8; j++) {
+            na[j] = a;
+            nt[j] = b;
+        }
+    } else {
+        for (int j = 0; j < 8; j++) single_traverse(s, ray[j], is[j], &na[j], &nt[j]);
+    }
+    *rays += 8;
+    for (int j = 0; j < 8; j++) {
+        out[j].color = v3(0.0f, (float)std::log2((double)na[j]) * 0.1f, (float)std::log2((double)nt[j]) * 0.1f);
+        out[j].tex = 0;
+        out[j].tu = out[j].tv = out[j].fresnel = 0.0f;
+    }
+}
+
 // renderer.rs:239-256 for one pixel
 inline uint32_t pack_color(V3 c) {
     V3 r = v3(xmin(1.0f, c.x * 2.0f) * 255.0f, xmin(1.0f, c.y * 2.0f) * 255.0f, xmin(1.0f, c.z * 2.0f) * 255.0f);
@@ -605,6 +637,7 @@ struct Frame {
     uint32_t* gbuf;
     float* color;  // w*h*3, written (not accumulated) when non-null
     float* accum;  // w*h*3, accumulated when non-null
+    bool debug;    // Renderer::toggle_debug_view
 };
 
 // The pixel coordinates of group g (0..7) of the 16x4 block at (xb, yb), in
@@ -666,7 +699,8 @@ uint64_t render_patch(const Frame& f, uint32_t x, uint32_t y) {
                 }
             for (int g = 0; g < 8; g++) {
                 PixelOut out[8];
-                render_pixels(*f.s, f.cam, xs[g], ys[g], rng, f.single, out, &rays);
+                if (f.debug) render_pixels_debug(*f.s, f.cam, xs[g], ys[g], f.single, out, &rays);
+                else render_pixels(*f.s, f.cam, xs[g], ys[g], rng, f.single, out, &rays);
                 store_group(f, xb + 4 * (uint32_t)(g >> 1), yb + 2 * (uint32_t)(g & 1), out);
             }
         }
@@ -692,7 +726,8 @@ uint64_t render_group_pg(const Frame& f, uint32_t gx, uint32_t gy) {
     }
     PixelOut out[8];
     uint64_t rays = 0;
-    render_pixels(*f.s, f.cam, gxs, gys, rng, f.single, out, &rays);
+    if (f.debug) render_pixels_debug(*f.s, f.cam, gxs, gys, f.single, out, &rays);
+    else render_pixels(*f.s, f.cam, gxs, gys, rng, f.single, out, &rays);
     store_group(f, gx, gy, out);
     return rays;
 }
@@ -732,6 +767,72 @@ uint64_t render_frame(const Frame& f, int rng_order, int nthreads) {
         });
     }
     return rays.load();
+}
+
+// ---- display post-process (src/gpu/*.glsl via ui.rs:313-364), restated with
+// the same fixed choices as the GPU kernels: unorm8 reads byte/255, render
+// targets store round(clamp(x)*255), textures are sRGB-decoded and sampled
+// bilinearly with repeat wrapping, the median's neighbours clamp at the edge,
+// sRGB decode/encode through tables computed in double.
+struct OrcDisplay {
+    uint32_t w, h, tw, th, slot = 0;
+    std::vector<uint8_t> t1, t2;
+    std::vector<uint32_t> ring;
+    float dec[256], enc[255];
+};
+static inline float unorm8(uint32_t w, int c) { return (float)((w >> (8 * c)) & 0xffu) * (1.0f / 255.0f); }
+static inline uint32_t quant8(float x) {
+    x = x < 0.0f ? 0.0f : (x > 1.0f ? 1.0f : x);
+    return (uint32_t)(int32_t)std::nearbyint(x * 255.0f);
+}
+static inline uint32_t pack4f(const float c[4]) {
+    return quant8(c[0]) | (quant8(c[1]) << 8) | (quant8(c[2]) << 16) | (quant8(c[3]) << 24);
+}
+static void tex_sample(const OrcDisplay& d, const std::vector<uint8_t>& t, float u, float v, float out[4]) {
+    float x = u * (float)d.tw - 0.5f, y = v * (float)d.th - 0.5f;
+    float fx = std::floor(x), fy = std::floor(y);
+    float ax = x - fx, ay = y - fy;
+    int x0 = (int)fx, y0 = (int)fy, W = (int)d.tw, H = (int)d.th;
+    int xs[2] = {((x0 % W) + W) % W, (((x0 + 1) % W) + W) % W};
+    int ys[2] = {((y0 % H) + H) % H, (((y0 + 1) % H) + H) % H};
+    for (int c = 0; c < 3; c++) {
+        float p00 = d.dec[t[3 * ((size_t)ys[0] * d.tw + xs[0]) + c]];
+        float p10 = d.dec[t[3 * ((size_t)ys[0] * d.tw + xs[1]) + c]];
+        float p01 = d.dec[t[3 * ((size_t)ys[1] * d.tw + xs[0]) + c]];
+        float p11 = d.dec[t[3 * ((size_t)ys[1] * d.tw + xs[1]) + c]];
+        float top = p00 * (1.0f - ax) + p10 * ax, bot = p01 * (1.0f - ax) + p11 * ax;
+        out[c] = top * (1.0f - ay) + bot * ay;
+    }
+    out[3] = 1.0f;
+}
+static void to_xyz(float c[4]) {  // median.glsl:35-41
+    const float k = 1.0f / 0.17697f;
+    float m[9] = {0.49f * k, 0.17697f * k, 0.0f * k, 0.31f * k, 0.81240f * k, 0.01f * k, 0.20f * k, 0.01063f * k,
+                  0.99f * k};
+    float r = c[0], g = c[1], b = c[2];
+    c[0] = m[0] * r + m[3] * g + m[6] * b;
+    c[1] = m[1] * r + m[4] * g + m[7] * b;
+    c[2] = m[2] * r + m[5] * g + m[8] * b;
+}
+static void to_rgb(float c[4]) {  // median.glsl:43-49
+    float m[9] = {0.41847f, -0.091169f, 0.00092090f, -0.15866f, 0.25243f, -0.0025498f, -0.082835f, 0.015708f,
+                  0.17860f};
+    float x = c[0], y = c[1], z = c[2];
+    c[0] = m[0] * x + m[3] * y + m[6] * z;
+    c[1] = m[1] * x + m[4] * y + m[7] * z;
+    c[2] = m[2] * x + m[5] * y + m[8] * z;
+}
+static void sort2v(float a[4], float b[4]) {
+    for (int c = 0; c < 4; c++) {
+        float lo = std::fmin(a[c], b[c]), hi = std::fmax(a[c], b[c]);
+        a[c] = lo;
+        b[c] = hi;
+    }
+}
+static uint32_t srgb_of(const OrcDisplay& d, float x) {
+    uint32_t n = 0;
+    while (n < 255 && d.enc[n] <= x) n++;
+    return n;
 }
 
 }  // namespace orc
@@ -807,7 +908,8 @@ void orc_intersect(void* sp, const float* ox, const float* oy, const float* oz, 
 // rng_order 0 = patch-sequential (reference), 1 = per-group.
 // traversal 0 = packet (reference), 1 = single-ray.
 uint64_t orc_render(void* sp, const float* cam, uint32_t w, uint32_t h, uint32_t frame, int rng_order,
-                    int traversal, uint32_t* rgba, uint32_t* gbuf, float* color, float* accum, int nthreads) {
+                    int traversal, uint32_t* rgba, uint32_t* gbuf, float* color, float* accum, int nthreads,
+                    int debug) {
     Frame f;
     f.s = (const Scene*)sp;
     f.cam.pos = v3(cam[0], cam[1], cam[2]);
@@ -823,7 +925,90 @@ uint64_t orc_render(void* sp, const float* cam, uint32_t w, uint32_t h, uint32_t
     f.gbuf = gbuf;
     f.color = color;
     f.accum = accum;
+    f.debug = debug != 0;
     return render_frame(f, rng_order, nthreads);
+}
+
+void* orc_display_new(uint32_t w, uint32_t h, const uint8_t* t1, const uint8_t* t2, uint32_t tw, uint32_t th) {
+    OrcDisplay* d = new OrcDisplay();
+    d->w = w;
+    d->h = h;
+    d->tw = tw;
+    d->th = th;
+    d->t1.assign(t1, t1 + (size_t)tw * th * 3);
+    d->t2.assign(t2, t2 + (size_t)tw * th * 3);
+    d->ring.assign((size_t)w * h * 8, 0u);
+    for (int i = 0; i < 256; i++) {
+        double sv = i / 255.0;
+        d->dec[i] = (float)(sv <= 0.04045 ? sv / 12.92 : std::pow((sv + 0.055) / 1.055, 2.4));
+    }
+    for (int k = 1; k <= 255; k++) {
+        double sv = (k - 0.5) / 255.0;
+        d->enc[k - 1] = (float)(sv <= 0.04045 ? sv / 12.92 : std::pow((sv + 0.055) / 1.055, 2.4));
+    }
+    return d;
+}
+void orc_display_free(void* d) { delete (OrcDisplay*)d; }
+
+void orc_display_frame(void* dp, const uint32_t* rgba, const uint32_t* gbuf, int enable_blend, int enable_median,
+                       uint32_t* out) {
+    OrcDisplay& d = *(OrcDisplay*)dp;
+    size_t npx = (size_t)d.w * d.h;
+    d.slot = (d.slot + 1) % 8;
+    uint32_t* slot = &d.ring[d.slot * npx];
+    for (size_t i = 0; i < npx; i++) {  // gbuffer.glsl:18-42
+        float color[4], data[4];
+        for (int c = 0; c < 4; c++) {
+            color[c] = unorm8(rgba[i], c);
+            data[c] = unorm8(gbuf[i], c);
+        }
+        float fresnel = data[2];
+        for (int k = 1; k <= 2; k++)
+            if (data[3] == (float)k / 255.0f) {
+                float tex[4];
+                tex_sample(d, k == 1 ? d.t1 : d.t2, data[0], data[1], tex);
+                for (int c = 0; c < 4; c++) color[c] = color[c] * (1.0f * fresnel + tex[c] * (1.0f - fresnel));
+            }
+        slot[i] = pack4f(color);
+    }
+    std::vector<uint32_t> scratch(npx);
+    for (size_t i = 0; i < npx; i++) {  // blend.glsl:22-34
+        float sum[4] = {0, 0, 0, 0};
+        for (int f = 0; f < 8; f++) {
+            uint32_t w = d.ring[(size_t)(enable_blend ? f : (int)d.slot) * npx + i];
+            for (int c = 0; c < 4; c++) sum[c] = f == 0 ? unorm8(w, c) : sum[c] + unorm8(w, c);
+        }
+        float o[4] = {sum[0] * 0.125f, sum[1] * 0.125f, sum[2] * 0.125f, 1.0f};
+        scratch[i] = pack4f(o);
+    }
+    for (size_t i = 0; i < npx; i++) {  // median.glsl:51-75 / id.glsl, then the sRGB framebuffer
+        int x = (int)(i % d.w), y = (int)(i / d.w);
+        float res[4];
+        if (!enable_median) {
+            for (int c = 0; c < 4; c++) res[c] = unorm8(scratch[i], c);
+        } else {
+            const int dx[5] = {0, 1, 0, -1, 0}, dy[5] = {0, 0, 1, 0, -1};
+            float c5[5][4];
+            for (int t = 0; t < 5; t++) {
+                int xx = std::min(std::max(x + dx[t], 0), (int)d.w - 1);
+                int yy = std::min(std::max(y + dy[t], 0), (int)d.h - 1);
+                for (int c = 0; c < 4; c++) c5[t][c] = unorm8(scratch[(size_t)yy * d.w + xx], c);
+                to_xyz(c5[t]);
+            }
+            sort2v(c5[0], c5[1]);
+            sort2v(c5[3], c5[4]);
+            sort2v(c5[0], c5[2]);
+            sort2v(c5[1], c5[2]);
+            sort2v(c5[0], c5[3]);
+            sort2v(c5[2], c5[3]);
+            sort2v(c5[1], c5[4]);
+            sort2v(c5[1], c5[2]);
+            sort2v(c5[3], c5[4]);
+            for (int c = 0; c < 4; c++) res[c] = c5[2][c] * 0.667f + c5[1][c] * 0.1666f + c5[3][c] * 0.1666f;
+            to_rgb(res);
+        }
+        out[i] = srgb_of(d, res[0]) | (srgb_of(d, res[1]) << 8) | (srgb_of(d, res[2]) << 16) | (quant8(res[3]) << 24);
+    }
 }
 
 // renderer.rs:378-410 on a row-major w*h*3 accumulation buffer.
@@ -833,6 +1018,7 @@ void orc_resolve(const float* accum, uint32_t w, uint32_t h, uint32_t n, uint32_
         rgba[i] = pack_color(v3(accum[3 * i] * factor, accum[3 * i + 1] * factor, accum[3 * i + 2] * factor));
 }
 
+// renderer.rs:378-410 on a row-major w*h*3 accumulation buffer.
 // ---- element functions for the ported unit tests ----
 float orc_rcp(float x) { return rcp(x); }
 float orc_rsqrt(float x) { return rsqrt(x); }

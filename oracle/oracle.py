@@ -29,7 +29,11 @@ def lib():
             "orc_scene_new": (P, [P, U32, P, U32, P, U32, ctypes.c_int]),
             "orc_scene_free": (None, [P]),
             "orc_intersect": (None, [P, P, P, P, P, P, P, U32, F32, ctypes.c_int, P, P, P, P, P, P, ctypes.c_int]),
-            "orc_render": (U64, [P, P, U32, U32, U32, ctypes.c_int, ctypes.c_int, P, P, P, P, ctypes.c_int]),
+            "orc_render": (U64, [P, P, U32, U32, U32, ctypes.c_int, ctypes.c_int, P, P, P, P, ctypes.c_int,
+                                 ctypes.c_int]),
+            "orc_display_new": (P, [U32, U32, P, P, U32, U32]),
+            "orc_display_free": (None, [P]),
+            "orc_display_frame": (None, [P, P, P, ctypes.c_int, ctypes.c_int, P]),
             "orc_resolve": (None, [P, U32, U32, U32, P]),
             "orc_rcp": (F32, [F32]), "orc_rsqrt": (F32, [F32]), "orc_recip_precise": (F32, [F32]),
             "orc_sin": (F32, [F32]), "orc_cos": (F32, [F32]), "orc_acos": (F32, [F32]),
@@ -98,13 +102,13 @@ class OracleScene:
         return t, tri
 
     def render(self, camera, width, height, frame, rng_order=RNG_GROUP, traversal=TRAVERSE_PACKET, nthreads=None,
-               color=True, accum=None):
+               color=True, accum=None, debug=False):
         cam = np.ascontiguousarray(camera, dtype=np.float32)
         rgba = np.zeros((height, width), np.uint32)
         gbuf = np.zeros((height, width), np.uint32)
         col = np.zeros((height, width, 3), np.float32) if color else None
         rays = lib().orc_render(self._h, _p(cam), width, height, frame, rng_order, traversal, _p(rgba), _p(gbuf),
-                                _p(col), _p(accum), nthreads or default_threads())
+                                _p(col), _p(accum), nthreads or default_threads(), int(debug))
         return rgba, gbuf, col, rays
 
     def __del__(self):
@@ -118,3 +122,26 @@ def resolve(accum, n):
     rgba = np.zeros((h, w), np.uint32)
     lib().orc_resolve(_p(np.ascontiguousarray(accum, dtype=np.float32)), w, h, n, _p(rgba))
     return rgba
+
+
+class OracleDisplay:
+    """The display post-process restatement (ring of 8 frames kept inside)."""
+
+    def __init__(self, width, height, tex1, tex2):
+        self.w, self.h = width, height
+        self.t1 = np.ascontiguousarray(tex1, dtype=np.uint8)
+        self.t2 = np.ascontiguousarray(tex2, dtype=np.uint8)
+        th, tw = self.t1.shape[:2]
+        self._h = lib().orc_display_new(width, height, _p(self.t1), _p(self.t2), tw, th)
+
+    def frame(self, rgba, gbuf, blend=True, median=True):
+        out = np.zeros((self.h, self.w), np.uint32)
+        a = np.ascontiguousarray(rgba, dtype=np.uint32)
+        g = np.ascontiguousarray(gbuf, dtype=np.uint32)
+        lib().orc_display_frame(self._h, _p(a), _p(g), int(blend), int(median), _p(out))
+        return out
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _L is not None:
+            _L.orc_display_free(self._h)
+            self._h = None
