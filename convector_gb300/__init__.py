@@ -31,7 +31,7 @@ NODE_DTYPE_WORDS = 8       # cvx_bvh_node: origin far_ (6 f32), index, len (u32)
 TRAVERSE_PACKET, TRAVERSE_SINGLE = 0, 1
 REFILL_AFTER_CAMERA, REFILL_ALL, REFILL_NONE = 0, 1, 2
 RNG_PATCH, RNG_GROUP = 0, 1
-MODE_MEGAKERNEL, MODE_WAVEFRONT = 0, 1
+MODE_MEGAKERNEL, MODE_WAVEFRONT, MODE_AUTO = 0, 1, 2
 
 _LIB = None
 
@@ -56,7 +56,8 @@ class _View(ctypes.Structure):
 class _ServerConfig(ctypes.Structure):
     _fields_ = [("framebuffer_bytes", ctypes.c_uint64), ("max_groups", ctypes.c_uint32),
                 ("traversal", ctypes.c_uint32), ("use_graph", ctypes.c_uint32), ("sequential", ctypes.c_uint32),
-                ("blocks_per_sm", ctypes.c_uint32), ("refill_mode", ctypes.c_uint32)]
+                ("blocks_per_sm", ctypes.c_uint32), ("refill_mode", ctypes.c_uint32),
+                ("kernel_mode", ctypes.c_uint32)]
 
 
 class _Request(ctypes.Structure):
@@ -125,6 +126,8 @@ def lib(build=False):
         "cvx_batch_create": (I32, [P, U32, U32, ctypes.c_uint64, P, P]),
         "cvx_batch_render": (I32, [P, P, U32, P, P, P]),
         "cvx_batch_destroy": (None, [P]),
+        "cvx_batch_set_scene_mode": (I32, [P, U32, U32]),
+        "cvx_server_set_scene_mode": (I32, [P, U32, U32]),
         "cvx_server_create": (I32, [P, U32, P, P]),
         "cvx_server_submit": (I32, [P, P, P, P]),
         "cvx_server_wait": (I32, [P, ctypes.c_uint64, U32, P]),
@@ -477,10 +480,10 @@ class Batch:
     """Many views of many resident scenes rendered in shared wavefronts."""
 
     def __init__(self, scenes, max_groups=1 << 20, max_pixels=1 << 24, traversal=TRAVERSE_SINGLE, use_graph=1,
-                 blocks_per_sm=0, refill_mode=REFILL_AFTER_CAMERA):
+                 blocks_per_sm=0, refill_mode=REFILL_AFTER_CAMERA, mode=MODE_AUTO):
         self.scenes = list(scenes)
         arr = (ctypes.c_void_p * len(self.scenes))(*[s._h.value for s in self.scenes])
-        cfg = RenderConfig(RNG_GROUP, traversal, MODE_WAVEFRONT, 0, use_graph, blocks_per_sm, refill_mode)
+        cfg = RenderConfig(RNG_GROUP, traversal, mode, 0, use_graph, blocks_per_sm, refill_mode)
         out = ctypes.c_void_p()
         _check(lib().cvx_batch_create(arr, len(self.scenes), max_groups, max_pixels, ctypes.byref(cfg),
                                       ctypes.byref(out)))
@@ -504,11 +507,11 @@ class Server:
     """Continuously batched request server over resident scenes."""
 
     def __init__(self, scenes, framebuffer_bytes=4 << 30, max_groups=1 << 21, traversal=TRAVERSE_SINGLE,
-                 use_graph=1, sequential=False, blocks_per_sm=0, refill_mode=REFILL_AFTER_CAMERA):
+                 use_graph=1, sequential=False, blocks_per_sm=0, refill_mode=REFILL_AFTER_CAMERA, kernel_mode=0):
         self.scenes = list(scenes)
         arr = (ctypes.c_void_p * len(self.scenes))(*[s._h.value for s in self.scenes])
         cfg = _ServerConfig(framebuffer_bytes, max_groups, traversal, use_graph, int(sequential), blocks_per_sm,
-                            refill_mode)
+                            refill_mode, kernel_mode)
         out = ctypes.c_void_p()
         _check(lib().cvx_server_create(arr, len(self.scenes), ctypes.byref(cfg), ctypes.byref(out)))
         self._h = out

@@ -114,6 +114,7 @@ struct cvx_scene {
 
 DeviceScene cvx::scene_view(const cvx_scene* s) { return s->view(); }
 cudaStream_t cvx::scene_stream(const cvx_scene* s) { return s->stream; }
+uint32_t cvx::scene_depth(const cvx_scene* s) { return s->depth; }
 uint32_t cvx::scene_num_lights(const cvx_scene* s) { return s->n_lights; }
 
 struct cvx_renderer {

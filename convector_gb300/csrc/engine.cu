@@ -52,32 +52,37 @@ WaveEngine::~WaveEngine() {
     for (void* p : owned_) cudaFree(p);
     if (h_jobs_) cudaFreeHost(h_jobs_);
     if (h_hdr_) cudaFreeHost(h_hdr_);
+    if (h_read_) cudaFreeHost(h_read_);
+    if (h_job_rays_) cudaFreeHost(h_job_rays_);
     if (e0_) cudaEventDestroy(e0_);
     if (e1_) cudaEventDestroy(e1_);
 }
 
 int32_t WaveEngine::init(uint32_t max_groups, uint32_t max_jobs, bool packet, bool use_graph,
-                         uint32_t blocks_per_sm, uint32_t refill_from) {
+                         uint32_t blocks_per_sm, uint32_t refill_from, bool fused) {
     refill_from_ = refill_from;
     max_groups_ = max_groups;
     max_jobs_ = max_jobs;
     packet_ = packet;
     use_graph_ = use_graph;
     blocks_per_sm_ = blocks_per_sm;
-    size_t L = (size_t)max_groups * 8;
+    fused_ = fused;
     int32_t st = 0;
-    float** f[] = {&st_.ox, &st_.oy, &st_.oz, &st_.dx, &st_.dy, &st_.dz, &st_.cr, &st_.cg, &st_.cb,
-                   &st_.ht, &st_.hu, &st_.hv};
-    for (float** p : f)
-        if ((st = alloc(p, L, owned_))) return st;
-    if ((st = alloc(&st_.rng, L, owned_))) return st;
-    if ((st = alloc(&st_.gbuf, L, owned_))) return st;
-    if ((st = alloc(&st_.flags, L, owned_))) return st;
-    if ((st = alloc(&st_.htri, L, owned_))) return st;
-    if ((st = alloc(&st_.group_job, max_groups, owned_))) return st;
-    if ((st = alloc(&st_.queue[0], max_groups, owned_))) return st;
-    if ((st = alloc(&st_.queue[1], max_groups, owned_))) return st;
-    if ((st = alloc(&st_.counts, 16, owned_))) return st;
+    if (!fused) {  // the fused kernel keeps a path's state in registers: no ray queues
+        size_t L = (size_t)max_groups * 8;
+        float** f[] = {&st_.ox, &st_.oy, &st_.oz, &st_.dx, &st_.dy, &st_.dz, &st_.cr, &st_.cg, &st_.cb,
+                       &st_.ht, &st_.hu, &st_.hv};
+        for (float** p : f)
+            if ((st = alloc(p, L, owned_))) return st;
+        if ((st = alloc(&st_.rng, L, owned_))) return st;
+        if ((st = alloc(&st_.gbuf, L, owned_))) return st;
+        if ((st = alloc(&st_.flags, L, owned_))) return st;
+        if ((st = alloc(&st_.htri, L, owned_))) return st;
+        if ((st = alloc(&st_.group_job, max_groups, owned_))) return st;
+        if ((st = alloc(&st_.queue[0], max_groups, owned_))) return st;
+        if ((st = alloc(&st_.queue[1], max_groups, owned_))) return st;
+        if ((st = alloc(&st_.counts, 16, owned_))) return st;
+    }
     if ((st = alloc(&d_jobs_, max_jobs, owned_))) return st;
     if ((st = alloc(&d_hdr_, 1, owned_))) return st;
     if ((st = alloc(&d_rays_, 1, owned_))) return st;
@@ -85,6 +90,8 @@ int32_t WaveEngine::init(uint32_t max_groups, uint32_t max_jobs, bool packet, bo
     if ((st = alloc(&d_err_, 1, owned_))) return st;
     ECK(cudaMallocHost((void**)&h_jobs_, max_jobs * sizeof(Job)), "pinned job staging");
     ECK(cudaMallocHost((void**)&h_hdr_, sizeof(WaveHeader)), "pinned job staging");
+    ECK(cudaMallocHost((void**)&h_read_, sizeof(Readback)), "pinned readback");
+    ECK(cudaMallocHost((void**)&h_job_rays_, max_jobs * sizeof(unsigned long long)), "pinned readback");
     ECK(cudaEventCreate(&e0_), "cudaEventCreate");
     ECK(cudaEventCreate(&e1_), "cudaEventCreate");
     return CVX_OK;
@@ -111,9 +118,17 @@ int32_t WaveEngine::set_scenes(cvx_scene* const* scenes, uint32_t n) {
 
 static bool same_out(const WaveOutputs& a, const WaveOutputs& b) { return std::memcmp(&a, &b, sizeof a) == 0; }
 
+static cudaError_t launch_any(bool fused, const Job* jobs, const WaveHeader* hdr, const DeviceScene* scenes,
+                              const WaveState& st, const WaveOutputs& out, bool packet, uint32_t bps,
+                              uint32_t refill_from, cudaStream_t stream) {
+    return fused ? launch_wave_fused(jobs, hdr, scenes, out, packet, bps, stream)
+                 : launch_wave(jobs, hdr, scenes, st, out, packet, bps, refill_from, stream);
+}
+
 int32_t WaveEngine::launch(const WaveOutputs& out, cudaStream_t stream) {
     if (!use_graph_) {
-        ECK(launch_wave(d_jobs_, d_hdr_, d_scenes_, st_, out, packet_, blocks_per_sm_, refill_from_, stream), "wave launch");
+        ECK(launch_any(fused_, d_jobs_, d_hdr_, d_scenes_, st_, out, packet_, blocks_per_sm_, refill_from_, stream),
+            "wave launch");
         return CVX_OK;
     }
     for (auto& g : graphs_)
@@ -123,7 +138,8 @@ int32_t WaveEngine::launch(const WaveOutputs& out, cudaStream_t stream) {
         }
     cudaGraph_t graph;
     ECK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal), "begin capture");
-    cudaError_t e = launch_wave(d_jobs_, d_hdr_, d_scenes_, st_, out, packet_, blocks_per_sm_, refill_from_, stream);
+    cudaError_t e =
+        launch_any(fused_, d_jobs_, d_hdr_, d_scenes_, st_, out, packet_, blocks_per_sm_, refill_from_, stream);
     cudaError_t e2 = cudaStreamEndCapture(stream, &graph);
     if (e != cudaSuccess) return cuda_err(e, "capture wave");
     if (e2 != cudaSuccess) return cuda_err(e2, "end capture");
@@ -140,8 +156,10 @@ int32_t WaveEngine::launch(const WaveOutputs& out, cudaStream_t stream) {
     return CVX_OK;
 }
 
-int32_t WaveEngine::run(const std::vector<Job>& jobs_in, WaveOutputs out, cudaStream_t stream, uint64_t* rays,
-                        std::vector<uint64_t>* job_rays, float* ms) {
+int32_t WaveEngine::submit(const std::vector<Job>& jobs_in, WaveOutputs out, cudaStream_t stream,
+                           bool want_job_rays) {
+    last_jobs_ = 0;
+    last_want_ = want_job_rays;
     if (jobs_in.size() > max_jobs_) return set_error(CVX_ERR_CAPACITY, "too many jobs for one wave");
     uint32_t groups = 0;
     for (size_t i = 0; i < jobs_in.size(); i++) {
@@ -155,35 +173,51 @@ int32_t WaveEngine::run(const std::vector<Job>& jobs_in, WaveOutputs out, cudaSt
     h_hdr_->n_jobs = (uint32_t)jobs_in.size();
     h_hdr_->n_groups = groups;
     if (jobs_in.empty()) return CVX_OK;
+    last_jobs_ = (uint32_t)jobs_in.size();
     out.rays = d_rays_;
-    out.job_rays = job_rays ? d_job_rays_ : nullptr;
+    out.job_rays = want_job_rays ? d_job_rays_ : nullptr;
     out.err = d_err_;
     ECK(cudaMemcpyAsync(d_jobs_, h_jobs_, jobs_in.size() * sizeof(Job), cudaMemcpyHostToDevice, stream),
         "upload jobs");
     ECK(cudaMemcpyAsync(d_hdr_, h_hdr_, sizeof(WaveHeader), cudaMemcpyHostToDevice, stream), "upload jobs");
     ECK(cudaMemsetAsync(d_rays_, 0, 8, stream), "reset counters");
     ECK(cudaMemsetAsync(d_err_, 0, 4, stream), "reset status");
-    if (job_rays) ECK(cudaMemsetAsync(d_job_rays_, 0, jobs_in.size() * 8, stream), "reset counters");
+    if (want_job_rays) ECK(cudaMemsetAsync(d_job_rays_, 0, jobs_in.size() * 8, stream), "reset counters");
     ECK(cudaEventRecord(e0_, stream), "event");
     int32_t st = launch(out, stream);
     if (st) return st;
     ECK(cudaEventRecord(e1_, stream), "event");
-    unsigned long long r = 0;
-    uint32_t err = 0;
-    ECK(cudaMemcpyAsync(&r, d_rays_, 8, cudaMemcpyDeviceToHost, stream), "read counters");
-    ECK(cudaMemcpyAsync(&err, d_err_, 4, cudaMemcpyDeviceToHost, stream), "read status");
-    if (job_rays) {
-        job_rays->assign(jobs_in.size(), 0);
-        ECK(cudaMemcpyAsync(job_rays->data(), d_job_rays_, jobs_in.size() * 8, cudaMemcpyDeviceToHost, stream),
+    ECK(cudaMemcpyAsync(&h_read_->rays, d_rays_, 8, cudaMemcpyDeviceToHost, stream), "read counters");
+    ECK(cudaMemcpyAsync(&h_read_->err, d_err_, 4, cudaMemcpyDeviceToHost, stream), "read status");
+    if (want_job_rays)
+        ECK(cudaMemcpyAsync(h_job_rays_, d_job_rays_, jobs_in.size() * 8, cudaMemcpyDeviceToHost, stream),
             "read counters");
+    return CVX_OK;
+}
+
+int32_t WaveEngine::collect(cudaStream_t stream, uint64_t* rays, std::vector<uint64_t>* job_rays, float* ms) {
+    if (last_jobs_ == 0) {
+        if (rays) *rays = 0;
+        if (ms) *ms = 0.0f;
+        if (job_rays) job_rays->clear();
+        return CVX_OK;
     }
     ECK(cudaStreamSynchronize(stream), "wave");
     float t = 0.0f;
     cudaEventElapsedTime(&t, e0_, e1_);
     if (ms) *ms = t;
-    if (rays) *rays = r;
-    if (err) return set_error(CVX_ERR_DEVICE, "traversal stack overflow reported by the kernel");
+    if (rays) *rays = h_read_->rays;
+    if (job_rays) job_rays->assign(h_job_rays_, h_job_rays_ + (last_want_ ? last_jobs_ : 0));
+    if (job_rays && !last_want_) job_rays->assign(last_jobs_, 0);
+    if (h_read_->err) return set_error(CVX_ERR_DEVICE, "traversal stack overflow reported by the kernel");
     return CVX_OK;
+}
+
+int32_t WaveEngine::run(const std::vector<Job>& jobs, WaveOutputs out, cudaStream_t stream, uint64_t* rays,
+                        std::vector<uint64_t>* job_rays, float* ms) {
+    int32_t st = submit(jobs, out, stream, job_rays != nullptr);
+    if (st) return st;
+    return collect(stream, rays, job_rays, ms);
 }
 
 }  // namespace cvx
@@ -193,9 +227,20 @@ using namespace cvx;
 // ---------------------------------------------------------------------------
 // Batch API
 
+// Kernel organisation of a scene in batches and in the server: the fused
+// kernel for shallow BVHs, the wavefront form (ray refill) for deep or large
+// ones, where long traversals benefit most from refill.
+static uint32_t default_scene_mode(const cvx_scene* s) {
+    DeviceScene v = scene_view(s);
+    return (scene_depth(s) > 40 || v.n_tris > 200000) ? 1u : 0u;
+}
+
 struct cvx_batch {
     std::vector<cvx_scene*> scenes;
-    WaveEngine engine;
+    std::vector<uint32_t> mode;  // per scene: 0 fused, 1 wavefront
+    WaveEngine engine;           // wavefront
+    WaveEngine fused;
+    cudaStream_t stream2 = nullptr;
     uint64_t max_pixels = 0;
     float* d_accum = nullptr;
     uint32_t* d_rgba = nullptr;
@@ -207,6 +252,7 @@ struct cvx_batch {
         cudaFree(d_rgba);
         cudaFree(d_items);
         if (stream) cudaStreamDestroy(stream);
+        if (stream2) cudaStreamDestroy(stream2);
     }
 };
 
@@ -223,10 +269,17 @@ extern "C" int32_t cvx_batch_create(cvx_scene* const* scenes, uint32_t n_scenes,
     b->scenes.assign(scenes, scenes + n_scenes);
     b->max_pixels = max_pixels;
     ECK(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking), "cudaStreamCreate");
+    ECK(cudaStreamCreateWithFlags(&b->stream2, cudaStreamNonBlocking), "cudaStreamCreate");
     int32_t st = b->engine.init(max_groups, 4096, c.traversal == CVX_TRAVERSE_PACKET, c.use_graph != 0,
                                 c.blocks_per_sm, refill_from(c.refill_mode));
     if (st) return st;
+    if ((st = b->fused.init(0xffffffffu, 4096, c.traversal == CVX_TRAVERSE_PACKET, c.use_graph != 0, 0, 1, true)))
+        return st;
     if ((st = b->engine.set_scenes(scenes, n_scenes))) return st;
+    if ((st = b->fused.set_scenes(scenes, n_scenes))) return st;
+    for (uint32_t i = 0; i < n_scenes; i++)
+        b->mode.push_back(c.mode == CVX_MODE_WAVEFRONT ? 1u : c.mode == CVX_MODE_MEGAKERNEL ? 0u
+                                                                                         : default_scene_mode(scenes[i]));
     std::vector<void*> owned;
     if ((st = alloc(&b->d_accum, max_pixels * 3, owned))) return st;
     if ((st = alloc(&b->d_rgba, max_pixels, owned))) return st;
@@ -247,7 +300,7 @@ extern "C" int32_t cvx_batch_render(cvx_batch* b, const cvx_view* views, uint32_
         const cvx_view& v = views[i];
         if (v.scene >= b->scenes.size() || v.width == 0 || v.height == 0 || v.spp == 0)
             return set_error(CVX_ERR_INVALID, "bad view");
-        if (groups_of(v.width, v.height) > b->engine.max_groups())
+        if (b->mode[v.scene] == 1 && groups_of(v.width, v.height) > b->engine.max_groups())
             return set_error(CVX_ERR_CAPACITY, "a view is larger than the ray-queue capacity");
         offset[i] = total;
         total += (uint64_t)v.width * v.height;
@@ -259,24 +312,33 @@ extern "C" int32_t cvx_batch_render(cvx_batch* b, const cvx_view* views, uint32_
     float ms = 0.0f;
     WaveOutputs out{};
     out.accum = b->d_accum;
+    // Sample s of every view goes into wave s; a wave's jobs are split by
+    // their scene's kernel organisation, and the two halves run concurrently
+    // (disjoint pixels) on two streams. A wave larger than the ray-queue
+    // capacity is split into several.
     for (uint32_t s = 0; s < max_spp; s++) {
-        std::vector<Job> jobs;
+        std::vector<Job> jobs[2];
         uint32_t groups = 0;
         auto flush = [&]() -> int32_t {
-            uint64_t r = 0;
-            float t = 0.0f;
-            int32_t st = b->engine.run(jobs, out, b->stream, &r, nullptr, &t);
-            rays += r;
-            ms += t;
-            jobs.clear();
+            uint64_t r[2] = {0, 0};
+            float t[2] = {0.0f, 0.0f};
+            int32_t st = b->fused.submit(jobs[0], out, b->stream2, false);
+            if (!st) st = b->engine.submit(jobs[1], out, b->stream, false);
+            int32_t st0 = b->fused.collect(b->stream2, &r[0], nullptr, &t[0]);
+            int32_t st1 = b->engine.collect(b->stream, &r[1], nullptr, &t[1]);
+            rays += r[0] + r[1];
+            ms += t[0] > t[1] ? t[0] : t[1];
+            jobs[0].clear();
+            jobs[1].clear();
             groups = 0;
-            return st;
+            return st ? st : (st0 ? st0 : st1);
         };
         for (uint32_t i = 0; i < n; i++) {
             const cvx_view& v = views[i];
             if (v.spp <= s) continue;
+            uint32_t m = b->mode[v.scene];
             uint32_t g = groups_of(v.width, v.height);
-            if (groups + g > b->engine.max_groups() || jobs.size() == b->engine.max_jobs()) {
+            if ((m == 1 && groups + g > b->engine.max_groups()) || jobs[m].size() == b->engine.max_jobs()) {
                 int32_t st = flush();
                 if (st) return st;
             }
@@ -287,10 +349,10 @@ extern "C" int32_t cvx_batch_render(cvx_batch* b, const cvx_view* views, uint32_
             j.h = v.height;
             j.frame = v.frame_base + s;
             j.out_offset = offset[i];
-            jobs.push_back(j);
-            groups += g;
+            jobs[m].push_back(j);
+            if (m == 1) groups += g;
         }
-        if (!jobs.empty()) {
+        if (!jobs[0].empty() || !jobs[1].empty()) {
             int32_t st = flush();
             if (st) return st;
         }
@@ -310,6 +372,12 @@ extern "C" int32_t cvx_batch_render(cvx_batch* b, const cvx_view* views, uint32_
     ECK(cudaStreamSynchronize(b->stream), "batch");
     if (rays_out) *rays_out = rays;
     if (ms_out) *ms_out = ms;
+    return CVX_OK;
+}
+
+extern "C" int32_t cvx_batch_set_scene_mode(cvx_batch* b, uint32_t scene, uint32_t mode) {
+    if (!b || scene >= b->scenes.size() || mode > 1) return set_error(CVX_ERR_INVALID, "bad scene mode");
+    b->mode[scene] = mode;
     return CVX_OK;
 }
 
@@ -370,8 +438,11 @@ struct RangeAlloc {
 
 struct cvx_server {
     std::vector<cvx_scene*> scenes;
+    std::vector<uint32_t> mode;  // per scene: 0 fused, 1 wavefront
     cvx_server_config cfg{};
-    WaveEngine engine;
+    WaveEngine engine;  // wavefront
+    WaveEngine fused;
+    cudaStream_t stream2 = nullptr;
     float* d_accum = nullptr;
     uint32_t* d_rgba = nullptr;
     ResolveItem* d_items = nullptr;
@@ -415,18 +486,21 @@ struct cvx_server {
                 std::unique_lock<std::mutex> lk(mu);
                 cv.wait(lk, [&] { return stop || !pending.empty() || !admitted.empty(); });
                 if (stop) return;
-                // Admission, FIFO: stop at the first request that does not fit.
+                // Admission, FIFO: stop at the first request that does not fit
+                // (framebuffer pool; ray queues of wavefront-mode scenes).
                 while (!pending.empty()) {
                     auto& q = pending.front();
                     if (cfg.sequential && !admitted.empty()) break;
                     uint64_t off = 0;
-                    if (admitted_groups + q->groups > engine.max_groups() || admitted.size() >= engine.max_jobs() ||
+                    uint32_t qg = mode[q->r.scene] ? q->groups : 0u;
+                    if (admitted_groups + qg > engine.max_groups() || admitted.size() >= engine.max_jobs() ||
                         !pool.take(q->npx, &off))
                         break;
                     q->offset = off;
                     q->admitted = true;
                     q->res.start_s = now();
-                    admitted_groups += q->groups;
+                    q->groups = qg;
+                    admitted_groups += qg;
                     admitted.push_back(q);
                     pending.pop_front();
                 }
@@ -442,8 +516,10 @@ struct cvx_server {
                 wave = admitted;
             }
             if (wave.empty()) continue;
-            jobs.clear();
-            for (auto& q : wave) {
+            std::vector<Job> sub[2];
+            std::vector<size_t> where[2];
+            for (size_t i = 0; i < wave.size(); i++) {
+                auto& q = wave[i];
                 Job j{};
                 std::memcpy(&j.cam, &q->r.camera, sizeof(cvx_camera));
                 j.scene = q->r.scene;
@@ -451,16 +527,29 @@ struct cvx_server {
                 j.h = q->r.height;
                 j.frame = q->r.frame_base + q->next_sample;
                 j.out_offset = q->offset;
-                jobs.push_back(j);
+                uint32_t m = mode[q->r.scene];
+                sub[m].push_back(j);
+                where[m].push_back(i);
             }
             // A request's accumulator starts at zero with its first sample.
             for (auto& q : wave)
-                if (q->next_sample == 0) cudaMemsetAsync(d_accum + 3 * q->offset, 0, q->npx * 12, stream);
+                if (q->next_sample == 0)
+                    cudaMemsetAsync(d_accum + 3 * q->offset, 0, q->npx * 12, mode[q->r.scene] ? stream : stream2);
             WaveOutputs out{};
             out.accum = d_accum;
-            uint64_t r = 0;
-            float ms = 0.0f;
-            int32_t st = engine.run(jobs, out, stream, &r, &job_rays, &ms);
+            uint64_t r = 0, r0 = 0, r1 = 0;
+            float ms = 0.0f, ms0 = 0.0f, ms1 = 0.0f;
+            std::vector<uint64_t> jr[2];
+            int32_t st = fused.submit(sub[0], out, stream2, true);
+            if (!st) st = engine.submit(sub[1], out, stream, true);
+            int32_t st0 = fused.collect(stream2, &r0, &jr[0], &ms0);
+            int32_t st1 = engine.collect(stream, &r1, &jr[1], &ms1);
+            if (!st) st = st0 ? st0 : st1;
+            r = r0 + r1;
+            ms = ms0 > ms1 ? ms0 : ms1;
+            job_rays.assign(wave.size(), 0);
+            for (int m = 0; m < 2; m++)
+                for (size_t k = 0; k < where[m].size() && k < jr[m].size(); k++) job_rays[where[m][k]] = jr[m][k];
             std::vector<std::shared_ptr<Request>> done;
             std::vector<ResolveItem> items;
             {
@@ -523,6 +612,7 @@ struct cvx_server {
         cudaFree(d_rgba);
         cudaFree(d_items);
         if (stream) cudaStreamDestroy(stream);
+        if (stream2) cudaStreamDestroy(stream2);
     }
 };
 
@@ -537,10 +627,17 @@ extern "C" int32_t cvx_server_create(cvx_scene* const* scenes, uint32_t n_scenes
     s->scenes.assign(scenes, scenes + n_scenes);
     s->cfg = *cfg;
     ECK(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking), "cudaStreamCreate");
+    ECK(cudaStreamCreateWithFlags(&s->stream2, cudaStreamNonBlocking), "cudaStreamCreate");
     int32_t st = s->engine.init(cfg->max_groups, 1024, cfg->traversal == CVX_TRAVERSE_PACKET, cfg->use_graph != 0,
                                 cfg->blocks_per_sm, refill_from(cfg->refill_mode));
     if (st) return st;
+    if ((st = s->fused.init(0xffffffffu, 1024, cfg->traversal == CVX_TRAVERSE_PACKET, cfg->use_graph != 0, 0, 1,
+                            true)))
+        return st;
     if ((st = s->engine.set_scenes(scenes, n_scenes))) return st;
+    if ((st = s->fused.set_scenes(scenes, n_scenes))) return st;
+    for (uint32_t i = 0; i < n_scenes; i++)
+        s->mode.push_back(cfg->kernel_mode == 1 ? 0u : cfg->kernel_mode == 2 ? 1u : default_scene_mode(scenes[i]));
     s->pool_px = cfg->framebuffer_bytes / 16;  // 12 B accumulator + 4 B RGBA per pixel
     std::vector<void*> owned;
     if ((st = alloc(&s->d_accum, s->pool_px * 3, owned))) return st;
@@ -561,7 +658,7 @@ extern "C" int32_t cvx_server_submit(cvx_server* s, const cvx_request* req, uint
     q->host_rgba = rgba;
     q->npx = (uint64_t)req->width * req->height;
     q->groups = groups_of(req->width, req->height);
-    if (q->npx > s->pool_px || q->groups > s->engine.max_groups())
+    if (q->npx > s->pool_px || (s->mode[req->scene] == 1 && q->groups > s->engine.max_groups()))
         return set_error(CVX_ERR_CAPACITY, "request larger than the server's framebuffer or ray-queue budget");
     {
         std::lock_guard<std::mutex> lk(s->mu);
@@ -614,6 +711,15 @@ extern "C" int32_t cvx_server_stats(cvx_server* s, double* now_s, uint64_t* wave
     if (waves) *waves = s->waves;
     if (rays) *rays = s->rays;
     if (busy_s) *busy_s = s->busy_s;
+    return CVX_OK;
+}
+
+extern "C" int32_t cvx_server_set_scene_mode(cvx_server* s, uint32_t scene, uint32_t mode) {
+    if (!s || scene >= s->scenes.size() || mode > 1) return set_error(CVX_ERR_INVALID, "bad scene mode");
+    std::lock_guard<std::mutex> lk(s->mu);
+    if (!s->admitted.empty() || !s->pending.empty())
+        return set_error(CVX_ERR_INVALID, "scene modes can change only while the server is idle");
+    s->mode[scene] = mode;
     return CVX_OK;
 }
 

@@ -12,6 +12,7 @@ namespace cvx {
 
 DeviceScene scene_view(const cvx_scene* s);
 cudaStream_t scene_stream(const cvx_scene* s);
+uint32_t scene_depth(const cvx_scene* s);
 uint32_t scene_num_lights(const cvx_scene* s);
 uint32_t groups_of(uint32_t w, uint32_t h);
 // First bounce traversed with ray refill for a CVX_REFILL_* mode.
@@ -20,19 +21,33 @@ inline uint32_t refill_from(uint32_t refill_mode) { return refill_mode == 1 ? 0u
 class WaveEngine {
    public:
     ~WaveEngine();
-    // max_groups: ray-queue capacity (8-pixel groups) of one wave.
+    // max_groups: ray-queue capacity (8-pixel groups) of one wave. fused: run
+    // waves as one persistent fused kernel (no ray queues) instead of the
+    // wavefront kernels.
     int32_t init(uint32_t max_groups, uint32_t max_jobs, bool packet, bool use_graph, uint32_t blocks_per_sm,
-                 uint32_t refill_from = 1);
+                 uint32_t refill_from = 1, bool fused = false);
     int32_t set_scenes(cvx_scene* const* scenes, uint32_t n);
-    // Runs one wave synchronously on `stream`; group_base / n_groups of the
-    // jobs are filled in here. rays, job_rays and ms may be null.
+    // Queues one wave on `stream` (asynchronous); group_base / n_groups of the
+    // jobs are filled in here. collect() waits for it and reads its counters.
+    int32_t submit(const std::vector<Job>& jobs, WaveOutputs out, cudaStream_t stream, bool want_job_rays);
+    int32_t collect(cudaStream_t stream, uint64_t* rays, std::vector<uint64_t>* job_rays, float* ms);
+    // submit + collect. rays, job_rays and ms may be null.
     int32_t run(const std::vector<Job>& jobs, WaveOutputs out, cudaStream_t stream, uint64_t* rays,
                 std::vector<uint64_t>* job_rays, float* ms);
     uint32_t max_groups() const { return max_groups_; }
     uint32_t max_jobs() const { return max_jobs_; }
+    bool fused() const { return fused_; }
 
    private:
     int32_t launch(const WaveOutputs& out, cudaStream_t stream);
+    struct Readback {
+        unsigned long long rays;
+        uint32_t err;
+    };
+    Readback* h_read_ = nullptr;
+    unsigned long long* h_job_rays_ = nullptr;
+    uint32_t last_jobs_ = 0;
+    bool last_want_ = false, fused_ = false;
     struct Graph {
         WaveOutputs out;
         cudaGraphExec_t exec;

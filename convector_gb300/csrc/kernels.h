@@ -25,6 +25,9 @@ cudaError_t launch_resolve(const float* accum, uint32_t npx, float factor, uint3
 cudaError_t launch_wave(const Job* jobs, const WaveHeader* hdr, const DeviceScene* scenes, const WaveState& st,
                         const WaveOutputs& out, bool packet, uint32_t blocks_per_sm, uint32_t refill_from,
                         cudaStream_t stream);
+// The fused (megakernel) form of a wave: one persistent launch.
+cudaError_t launch_wave_fused(const Job* jobs, const WaveHeader* hdr, const DeviceScene* scenes,
+                              const WaveOutputs& out, bool packet, uint32_t blocks_per_sm, cudaStream_t stream);
 cudaError_t launch_resolve_multi(const ResolveItem* items, uint32_t n_items, const float* accum, uint32_t* rgba,
                                  cudaStream_t stream);
 

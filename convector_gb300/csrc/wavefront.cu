@@ -292,6 +292,87 @@ __global__ void __launch_bounds__(128) k_wf_shade(const Job* __restrict__ jobs, 
     if ((threadIdx.x & 31u) == 0u && v) atomicAdd(out.rays, v);
 }
 
+static int g_sms_wf = 0;
+static int sms() {
+    if (!g_sms_wf) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&g_sms_wf, cudaDevAttrMultiProcessorCount, dev);
+        if (g_sms_wf <= 0) g_sms_wf = 1;
+    }
+    return g_sms_wf;
+}
+
+// The fused form over a wave: every octet renders whole groups of any job
+// (camera ray, bounce loop and shading in registers), walking the wave's
+// groups with a grid-stride loop. Same per-group RNG order and outputs as the
+// wavefront kernels.
+template <bool PACKET>
+__global__ void __launch_bounds__(128) k_wave_fused(const Job* __restrict__ jobs, const WaveHeader* __restrict__ hdr,
+                                                    const DeviceScene* __restrict__ scenes, WaveOutputs out) {
+    __shared__ ApproxTables tab;
+    load_tables_wf(tab);
+    const int k = threadIdx.x & 7;
+    const unsigned omask = 0xffu << (threadIdx.x & 24u);
+    const uint32_t n_groups = hdr->n_groups, n_jobs = hdr->n_jobs;
+    const uint32_t octets = (gridDim.x * blockDim.x) >> 3;
+    uint32_t rays = 0;
+    bool ok = true;
+    for (uint32_t gi = (blockIdx.x * blockDim.x + threadIdx.x) >> 3; gi < n_groups; gi += octets) {
+        uint32_t ji = find_job(jobs, n_jobs, gi);
+        const Job& j = jobs[ji];
+        uint32_t xb, yb, gx, gy;
+        int g;
+        group_origin(j, gi - j.group_base, &xb, &yb, &g, &gx, &gy);
+        if (gx >= j.w || gy >= j.h) continue;  // whole group outside the frame (octet-uniform)
+        const DeviceScene s = scenes[j.scene];
+        float x, y, scale;
+        block_coord_wf(j.w, j.h, xb, yb, g, k, &x, &y, &scale);
+        LaneRng rng;
+        rng.seed(gx, gy, j.frame, k);
+        x = fmaf(unit_from(rng.next()), scale, x);
+        y = fmaf(unit_from(rng.next()), scale, y);
+        PixelOut p;
+        uint32_t r = 0;
+        ok &= render_pixels<PACKET>(s, j.cam, x, y, rng, omask, tab, p, r);
+        rays += r;
+        if (out.job_rays) {
+            uint32_t tot = r;
+            for (int off = 4; off > 0; off >>= 1) tot += __shfl_down_sync(omask, tot, off, 8);
+            if (k == 0 && tot) atomicAdd(&out.job_rays[ji], (unsigned long long)tot);
+        }
+        uint32_t px = gx + (uint32_t)(k & 3), py = gy + (uint32_t)(k >> 2);
+        if (px < j.w && py < j.h) {
+            size_t idx = (size_t)j.out_offset + (size_t)py * j.w + px;
+            if (out.rgba) out.rgba[idx] = pack_color(p.color);
+            if (out.gbuf) out.gbuf[idx] = pack_gbuffer(p);
+            if (out.color) {
+                out.color[3 * idx] = p.color.x;
+                out.color[3 * idx + 1] = p.color.y;
+                out.color[3 * idx + 2] = p.color.z;
+            }
+            if (out.accum) {
+                out.accum[3 * idx] += p.color.x;
+                out.accum[3 * idx + 1] += p.color.y;
+                out.accum[3 * idx + 2] += p.color.z;
+            }
+        }
+    }
+    if (!ok) atomicOr(out.err, kErrStackOverflow);
+    unsigned long long v = rays;
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+    if ((threadIdx.x & 31u) == 0u && v) atomicAdd(out.rays, v);
+}
+
+cudaError_t launch_wave_fused(const Job* jobs, const WaveHeader* hdr, const DeviceScene* scenes,
+                              const WaveOutputs& out, bool packet, uint32_t blocks_per_sm, cudaStream_t stream) {
+    if (blocks_per_sm == 0) blocks_per_sm = 16;
+    uint32_t grid = (uint32_t)sms() * blocks_per_sm;
+    if (packet) k_wave_fused<true><<<grid, 128, 0, stream>>>(jobs, hdr, scenes, out);
+    else k_wave_fused<false><<<grid, 128, 0, stream>>>(jobs, hdr, scenes, out);
+    return cudaGetLastError();
+}
+
 __global__ void k_resolve_multi(const ResolveItem* __restrict__ items, uint32_t n_items, const float* __restrict__ accum,
                                 uint32_t* __restrict__ rgba) {
     for (uint32_t it = blockIdx.y; it < n_items; it += gridDim.y) {
@@ -310,17 +391,6 @@ cudaError_t launch_resolve_multi(const ResolveItem* items, uint32_t n_items, con
     dim3 grid(64, n_items < 1024 ? n_items : 1024);
     k_resolve_multi<<<grid, 256, 0, stream>>>(items, n_items, accum, rgba);
     return cudaGetLastError();
-}
-
-static int g_sms_wf = 0;
-static int sms() {
-    if (!g_sms_wf) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&g_sms_wf, cudaDevAttrMultiProcessorCount, dev);
-        if (g_sms_wf <= 0) g_sms_wf = 1;
-    }
-    return g_sms_wf;
 }
 
 cudaError_t launch_wave(const Job* jobs, const WaveHeader* hdr, const DeviceScene* scenes, const WaveState& st,

@@ -165,7 +165,7 @@ enum { CVX_RNG_PATCH = 0, CVX_RNG_GROUP = 1 };
 /* Kernel organisation: one fused kernel per frame, or the wavefront form
  * (ray generation, traversal, shading and accumulation kernels over SoA ray
  * queues with compaction), optionally replayed as a CUDA graph. */
-enum { CVX_MODE_MEGAKERNEL = 0, CVX_MODE_WAVEFRONT = 1 };
+enum { CVX_MODE_MEGAKERNEL = 0, CVX_MODE_WAVEFRONT = 1, CVX_MODE_AUTO = 2 };
 
 /* Wavefront single-ray traversal: which bounces fetch rays with refill
  * (persistent lanes take the next ray when theirs finishes) rather than one
@@ -229,13 +229,19 @@ typedef struct cvx_view {
 
 typedef struct cvx_batch cvx_batch;
 /* max_groups bounds the 8-pixel groups of one wave (ray-queue capacity);
- * max_pixels bounds the pixels of all views of one call. */
+ * max_pixels bounds the pixels of all views of one call. config->mode picks
+ * the kernel organisation of every scene: CVX_MODE_MEGAKERNEL (fused),
+ * CVX_MODE_WAVEFRONT, or CVX_MODE_AUTO (wavefront for BVHs deeper than 40
+ * levels or above 200k triangles, fused otherwise). A wave's fused and
+ * wavefront jobs run concurrently on two streams. */
 int32_t cvx_batch_create(cvx_scene* const* scenes, uint32_t n_scenes, uint32_t max_groups, uint64_t max_pixels,
                          const cvx_render_config* config, cvx_batch** out);
 /* Renders every view; rgba[i] (host, width*height words, may be NULL)
  * receives view i. rays and ms (may be NULL) receive the totals. */
 int32_t cvx_batch_render(cvx_batch* b, const cvx_view* views, uint32_t n_views, uint32_t* const* rgba,
                          uint64_t* rays, float* ms);
+/* Overrides one scene's kernel organisation (0 fused, 1 wavefront). */
+int32_t cvx_batch_set_scene_mode(cvx_batch* b, uint32_t scene, uint32_t mode);
 void cvx_batch_destroy(cvx_batch* b);
 
 /* ---- device: request server ----------------------------------------------
@@ -252,6 +258,7 @@ typedef struct cvx_server_config {
     uint32_t sequential;        /* 1: one request at a time (the plain path, for comparison) */
     uint32_t blocks_per_sm;     /* persistent blocks per SM (0: 12) */
     uint32_t refill_mode;       /* CVX_REFILL_* */
+    uint32_t kernel_mode;       /* 0: per scene as CVX_MODE_AUTO; 1: all fused; 2: all wavefront */
 } cvx_server_config;
 
 typedef struct cvx_request {
@@ -277,6 +284,9 @@ int32_t cvx_server_wait(cvx_server* s, uint64_t id, uint32_t timeout_ms, cvx_req
 /* Cancels a queued or running request (its result status becomes
  * CVX_ERR_CANCELLED). */
 int32_t cvx_server_cancel(cvx_server* s, uint64_t id);
+/* Overrides one scene's kernel organisation (0 fused, 1 wavefront); only
+ * while the server has no queued or admitted request. */
+int32_t cvx_server_set_scene_mode(cvx_server* s, uint32_t scene, uint32_t mode);
 /* The server clock (seconds), waves run, rays traced and device busy time. */
 int32_t cvx_server_stats(cvx_server* s, double* now_s, uint64_t* waves, uint64_t* rays, double* busy_s);
 void cvx_server_destroy(cvx_server* s);

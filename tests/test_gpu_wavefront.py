@@ -67,14 +67,18 @@ def _alone(gpu, scene, view):
     return r.resolve_u8(view.spp)
 
 
-def test_batch_images_equal_alone(two_scenes, gpu, orc):
+@pytest.mark.parametrize("mode", ["fused", "wavefront", "mixed"])
+def test_batch_images_equal_alone(two_scenes, gpu, orc, mode):
     scs = [s for _, s, _ in two_scenes]
     views = []
     for i, (w, h, spp) in enumerate([(160, 96, 2), (33, 17, 3), (96, 64, 1), (320, 184, 4)]):
         cam = gpu.Camera()
         scenes.default_camera(cam, eye=(0.3 * i, 1.2, 1.6))
         views.append(gpu.View(i % 2, w, h, spp, 100 * i, cam))
-    batch = gpu.Batch(scs, max_groups=1 << 16, max_pixels=1 << 20)
+    m = {"fused": gpu.MODE_MEGAKERNEL, "wavefront": gpu.MODE_WAVEFRONT, "mixed": gpu.MODE_MEGAKERNEL}[mode]
+    batch = gpu.Batch(scs, max_groups=1 << 16, max_pixels=1 << 20, mode=m)
+    if mode == "mixed":  # scene 1 through the wavefront kernels, scene 0 fused, in the same waves
+        gpu.lib().cvx_batch_set_scene_mode(batch._h, 1, 1)
     imgs, rays, ms = batch.render(views)
     assert rays > 0
     for v, img in zip(views, imgs):
@@ -98,7 +102,8 @@ def test_batch_splits_waves_when_queue_is_small(two_scenes, gpu):
         assert (a == b).all()
 
 
-def test_server_mix_equals_alone(two_scenes, gpu):
+@pytest.mark.parametrize("kernel_mode", [1, 2])
+def test_server_mix_equals_alone(two_scenes, gpu, kernel_mode):
     scs = [s for _, s, _ in two_scenes]
     rng = np.random.default_rng(4)
     reqs = []
@@ -108,7 +113,8 @@ def test_server_mix_equals_alone(two_scenes, gpu):
         reqs.append((int(k % 2), int(rng.choice([64, 100, 160])), int(rng.choice([32, 50, 96])),
                      int(rng.integers(1, 5)), cam))
     for sequential in (False, True):
-        srv = gpu.Server(scs, framebuffer_bytes=64 << 20, max_groups=1 << 14, sequential=sequential)
+        srv = gpu.Server(scs, framebuffer_bytes=64 << 20, max_groups=1 << 14, sequential=sequential,
+                         kernel_mode=kernel_mode)
         ids = []
         for i, (sc, w, h, spp, cam) in enumerate(reqs):
             ids.append(srv.submit(sc, w, h, spp, cam, frame_base=10 * i))
@@ -125,7 +131,7 @@ def test_server_mix_equals_alone(two_scenes, gpu):
 def test_server_admission_cancel_timeout(two_scenes, gpu):
     scs = [s for _, s, _ in two_scenes]
     cam = scenes.default_camera(gpu.Camera())
-    srv = gpu.Server(scs, framebuffer_bytes=64 * 64 * 16 * 2, max_groups=2048)
+    srv = gpu.Server(scs, framebuffer_bytes=64 * 64 * 16 * 2, max_groups=2048, kernel_mode=2)
     with pytest.raises(gpu.CvxError) as e:  # can never fit the framebuffer budget
         srv.submit(0, 1280, 736, 1, cam)
     assert e.value.status == 7
