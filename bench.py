@@ -110,6 +110,23 @@ class ClockSampler:
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def reduce_max(value, dist=None, device=None):
+    """Max of a per-rank float over all ranks (replicas: the job takes as long
+    as its slowest rank). Works with the nccl (device tensor) and gloo (CPU)
+    backends; without an initialised process group returns `value`."""
+    if dist is None or not dist.is_available() or not dist.is_initialized() or dist.get_world_size() == 1:
+        return float(value)
+    import torch
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device or "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_value(rays_per_rank, world, seconds):
+    """Whole-job Mrays/s of `world` replicas that each traced rays_per_rank."""
+    return world * rays_per_rank / seconds / 1e6
+
+
 def build_c1():
     import convector_gb300 as cg
     from convector_gb300 import scenes
@@ -218,9 +235,10 @@ def run_ours(args):
     def step(trav):
         scene.intersect_nearest_device(rays, t_out, tri_out, traversal=trav, stream=stream)
 
-    # Pick the faster traversal variant on a short untimed trial.
+    # Pick the faster traversal variant and launch shape on a short untimed trial.
     trial = {}
-    for trav in (0, 1):
+    for trav, bps in ((0, 0), (1, 8), (1, 10), (1, 12)):
+        scene.set_query_launch(bps)
         for _ in range(2):
             step(trav)
         torch.cuda.synchronize()
@@ -230,8 +248,10 @@ def run_ours(args):
             step(trav)
         e1.record()
         torch.cuda.synchronize()
-        trial[trav] = e0.elapsed_time(e1) / 3
-    trav = min(trial, key=trial.get)
+        trial["%s/%d" % ("packet8" if trav == 0 else "single", bps)] = e0.elapsed_time(e1) / 3
+    best = min(trial, key=trial.get)
+    trav = 0 if best.startswith("packet8") else 1
+    scene.set_query_launch(int(best.split("/")[1]))
 
     for _ in range(args.warmup):
         flush.zero_()
@@ -251,14 +271,11 @@ def run_ours(args):
         torch.cuda.synchronize()
         wall = time.perf_counter() - wall0
     step_ms = [e0.elapsed_time(e1) for e0, e1 in evs]
-    total_ms = sum(step_ms)
+    total_ms = reduce_max(sum(step_ms), dist if world > 1 else None, "cuda")
     if world > 1:
-        tt = torch.tensor([total_ms], device="cuda", dtype=torch.float64)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        total_ms = float(tt.item())
         dist.barrier()
     ms_per_step = total_ms / args.steps
-    value = world * n * args.steps / (total_ms * 1e-3) / 1e6
+    value = replica_value(n * args.steps, world, total_ms * 1e-3)
 
     # End to end through the C-ABI with host buffers: copies in and out every step.
     pin = [torch.from_numpy(np.ascontiguousarray(a)).pin_memory() for a in
@@ -283,12 +300,8 @@ def run_ours(args):
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
         e2e_call()
-    e2e_s = time.perf_counter() - t0
-    if world > 1:
-        tt = torch.tensor([e2e_s], device="cuda", dtype=torch.float64)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        e2e_s = float(tt.item())
-    e2e_value = world * n * e2e_steps / e2e_s / 1e6
+    e2e_s = reduce_max(time.perf_counter() - t0, dist if world > 1 else None, "cuda")
+    e2e_value = replica_value(n * e2e_steps, world, e2e_s)
 
     render = batched = served = large = None
     if rank == 0 and not args.no_render:
@@ -315,7 +328,7 @@ def run_ours(args):
             "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": WORKLOAD, "rays_per_step": n, "triangles": int(bvh.triangles.shape[0]),
-                       "traversal": "packet8" if trav == 0 else "single", "trial_ms": trial,
+                       "traversal": "packet8" if trav == 0 else "single", "launch": best, "trial_ms": trial,
                        "l2": "flushed between timed steps (256 MB write)", "parallelism": "replicas"},
             "e2e": {"value": e2e_value, "unit": "Mrays/s", "h2d_bytes_per_step": 24 * n, "d2h_bytes_per_step": 8 * n},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,

@@ -109,6 +109,7 @@ def lib(build=False):
         "cvx_scene_from_bvh": (I32, [P, P]),
         "cvx_scene_num_direct_samples": (U32, [P]),
         "cvx_scene_set_light_pick": (I32, [P, U32]),
+        "cvx_scene_set_query_launch": (I32, [P, U32]),
         "cvx_scene_destroy": (None, [P]),
         "cvx_intersect_nearest": (I32, [P, P, P, P, P, P, P, U32, F32, U32, P, P]),
         "cvx_intersect_nearest_device": (I32, [P, P, U32, F32, U32, P, P, P, P]),
@@ -332,6 +333,10 @@ class Scene:
     @staticmethod
     def from_meshes(meshes, light_pick=1):
         return Scene(Bvh.from_meshes(meshes), light_pick=light_pick)
+
+    def set_query_launch(self, blocks_per_sm):
+        """Resident blocks per SM of the nearest-hit kernel (0: default)."""
+        _check(lib().cvx_scene_set_query_launch(self._h, blocks_per_sm))
 
     def direct_sample_num(self):
         return lib().cvx_scene_num_direct_samples(self._h)

@@ -80,6 +80,7 @@ struct cvx_scene {
     uint32_t* d_err = nullptr;
     uint32_t n_nodes = 0, n_tris = 0, n_lights = 0, depth = 0;
     uint32_t general_pick = 1;
+    uint32_t blocks_per_sm = 0;  // launch shape of the nearest-hit query (0: default)
     // scratch for the host-buffer query
     float* d_rays = nullptr;
     float* d_t = nullptr;
@@ -257,6 +258,12 @@ int32_t cvx_scene_set_light_pick(cvx_scene* s, uint32_t light_pick) {
     return CVX_OK;
 }
 
+int32_t cvx_scene_set_query_launch(cvx_scene* s, uint32_t blocks_per_sm) {
+    if (!s || blocks_per_sm > 32) return set_error(CVX_ERR_INVALID, "bad launch shape");
+    s->blocks_per_sm = blocks_per_sm;
+    return CVX_OK;
+}
+
 void cvx_scene_destroy(cvx_scene* s) { delete s; }
 
 int32_t cvx_intersect_nearest_device(cvx_scene* s, const float* rays, uint32_t n, float far_dist, uint32_t traversal,
@@ -266,7 +273,7 @@ int32_t cvx_intersect_nearest_device(cvx_scene* s, const float* rays, uint32_t n
     if (n == 0) return CVX_OK;
     cudaStream_t st = (cudaStream_t)stream;
     CK(launch_intersect(s->view(), rays, n, far_dist, traversal == CVX_TRAVERSE_PACKET, t_out, tri_out, counters,
-                        s->d_err, 0, 0, st),
+                        s->d_err, 0, s->blocks_per_sm, st),
        "intersect launch");
     return CVX_OK;
 }
@@ -298,7 +305,7 @@ int32_t cvx_intersect_nearest(cvx_scene* s, const float* ox, const float* oy, co
            "copy rays");
     CK(cudaMemsetAsync(s->d_err, 0, 4, s->stream), "reset status");
     CK(launch_intersect(s->view(), s->d_rays, n, far_dist, traversal == CVX_TRAVERSE_PACKET, s->d_t, s->d_tri,
-                        nullptr, s->d_err, 0, 0, s->stream),
+                        nullptr, s->d_err, 0, s->blocks_per_sm, s->stream),
        "intersect launch");
     CK(cudaMemcpyAsync(t_out, s->d_t, (size_t)n * 4, cudaMemcpyDeviceToHost, s->stream), "copy distances");
     CK(cudaMemcpyAsync(tri_out, s->d_tri, (size_t)n * 4, cudaMemcpyDeviceToHost, s->stream), "copy indices");

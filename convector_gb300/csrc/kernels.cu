@@ -127,8 +127,11 @@ struct SoaRays {
     }
 };
 
-__global__ void __launch_bounds__(128) k_intersect_refill(SoaRays src, uint32_t* __restrict__ next_ray,
-                                                          uint32_t* __restrict__ err) {
+// MINB: resident blocks per SM the register allocation must allow (8: the
+// compiler's choice, 56 registers; 10 and 12 cap registers for occupancy).
+template <int MINB>
+__global__ void __launch_bounds__(128, MINB) k_intersect_refill(SoaRays src, uint32_t* __restrict__ next_ray,
+                                                                uint32_t* __restrict__ err) {
     __shared__ ApproxTables tab;
     load_tables(tab);
     if (!traverse_refill(src, src.n, next_ray, tab)) atomicOr(err, kErrStackOverflow);
@@ -322,7 +325,9 @@ cudaError_t launch_intersect(const DeviceScene& s, const float* rays, uint32_t n
         uint32_t need = (n + 127u) / 128u;
         if (blocks > need) blocks = need;
         SoaRays src{s.nodes, s.geom, rays, n, far_dist, t_out, tri_out, counters};
-        k_intersect_refill<<<blocks, 128, 0, st>>>(src, err + 1, err);
+        if (bps >= 12) k_intersect_refill<12><<<blocks, 128, 0, st>>>(src, err + 1, err);
+        else if (bps >= 10) k_intersect_refill<10><<<blocks, 128, 0, st>>>(src, err + 1, err);
+        else k_intersect_refill<8><<<blocks, 128, 0, st>>>(src, err + 1, err);
         return cudaGetLastError();
     }
     if (block == 0) block = 128;
