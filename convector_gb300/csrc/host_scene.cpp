@@ -5,14 +5,18 @@
 // -ffp-contract=off so that every float operation rounds where the Rust
 // original rounds.
 #include <algorithm>
+#include <charconv>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <fstream>
 #include <future>
 #include <memory>
 #include <sstream>
 #include <string>
+#include <string_view>
+#include <thread>
 #include <vector>
 
 #include "internal.h"
@@ -55,17 +59,37 @@ static inline float coord(S3 v, int axis) { return axis == 0 ? v.x : axis == 1 ?
 // ---------------------------------------------------------------------------
 // OBJ loading (wavefront.rs:83-152)
 
-static bool parse_f32(const std::string& tok, float* out) {
-    if (tok.empty()) return false;
-    if (tok.find("0x") != std::string::npos || tok.find("0X") != std::string::npos) return false;
+// Tokens are views into the OBJ text; nothing is allocated per token.
+using Tok = std::string_view;
+
+// Rust's f32::from_str: decimal or exponent notation, inf / nan, correctly
+// rounded; strtof also takes hexadecimal floats, which are refused here.
+static bool parse_f32(Tok tok, float* out) {
+    if (tok.empty() || tok.size() >= 128) return false;
+    // Plain decimal tokens in range: std::from_chars, correctly rounded like
+    // strtof and several times faster. Everything else goes through strtof.
+    if (tok[0] != '+') {
+        float v;
+        auto r = std::from_chars(tok.data(), tok.data() + tok.size(), v, std::chars_format::general);
+        bool plain = true;
+        for (char c : tok) plain = plain && ((c >= '0' && c <= '9') || c == '.' || c == '-' || c == 'e' || c == 'E');
+        if (plain && r.ec == std::errc() && r.ptr == tok.data() + tok.size()) {
+            *out = v;
+            return true;
+        }
+    }
+    if (tok.find("0x") != Tok::npos || tok.find("0X") != Tok::npos) return false;
+    char buf[128];
+    std::memcpy(buf, tok.data(), tok.size());
+    buf[tok.size()] = 0;
     char* end = nullptr;
-    float v = std::strtof(tok.c_str(), &end);
-    if (end != tok.c_str() + tok.size()) return false;
+    float v = std::strtof(buf, &end);
+    if (end != buf + tok.size()) return false;
     *out = v;
     return true;
 }
 
-static bool parse_u32(const std::string& tok, uint32_t* out) {
+static bool parse_u32(Tok tok, uint32_t* out) {
     size_t i = 0;
     if (i < tok.size() && tok[i] == '+') i++;
     if (i == tok.size()) return false;
@@ -80,70 +104,76 @@ static bool parse_u32(const std::string& tok, uint32_t* out) {
 }
 
 // wavefront.rs:49-55: "v" or "v/t" (further parts parsed and ignored).
-static bool parse_vertex_index(const std::string& tok, uint32_t* v, int64_t* t) {
-    std::vector<std::string> parts;
-    size_t start = 0;
-    for (;;) {
+static bool parse_vertex_index(Tok tok, uint32_t* v, int64_t* t) {
+    uint32_t vi = 0, ti = 0;
+    size_t start = 0, part = 0;
+    for (;; part++) {
         size_t p = tok.find('/', start);
-        parts.push_back(tok.substr(start, p == std::string::npos ? std::string::npos : p - start));
-        if (p == std::string::npos) break;
+        Tok s = tok.substr(start, p == Tok::npos ? Tok::npos : p - start);
+        uint32_t x;
+        if (!parse_u32(s, &x) || x == 0) return false;
+        if (part == 0) vi = x;
+        if (part == 1) ti = x;
+        if (p == Tok::npos) break;
         start = p + 1;
     }
-    uint32_t vi = 0, ti = 0;
-    for (size_t k = 0; k < parts.size(); k++) {
-        uint32_t x;
-        if (!parse_u32(parts[k], &x) || x == 0) return false;
-        if (k == 0) vi = x;
-        if (k == 1) ti = x;
-    }
     *v = vi - 1;
-    *t = parts.size() >= 2 ? (int64_t)ti - 1 : -1;
+    *t = part >= 1 ? (int64_t)ti - 1 : -1;
     return true;
 }
 
-static int32_t parse_obj(const char* text, size_t len, const char* const* names, const uint32_t* materials,
-                         uint32_t n_materials, cvx_mesh** out) {
+// ASCII white space: space and \t \n \v \f \r.
+static inline bool is_ws(char c) { return c == ' ' || (c >= '\t' && c <= '\r'); }
+
+// Splits [pos, end) at ASCII white space.
+static void tokenize(const char* text, size_t pos, size_t end, std::vector<Tok>& toks) {
+    toks.clear();
+    for (size_t i = pos; i < end;) {
+        while (i < end && is_ws(text[i])) i++;
+        size_t j = i;
+        while (j < end && !is_ws(text[j])) j++;
+        if (j > i) toks.emplace_back(text + i, j - i);
+        i = j;
+    }
+}
+
+static int32_t parse_obj_sequential(const char* text, size_t len, const char* const* names,
+                                    const uint32_t* materials, uint32_t n_materials, cvx_mesh** out) {
     std::unique_ptr<cvx_mesh> mesh(new cvx_mesh());
     uint32_t material = 0x00ffffffu;  // SMaterial::white() (material.rs:93-95)
     size_t pos = 0;
     uint32_t line_nr = 0;
-    std::vector<std::string> toks;
+    std::vector<Tok> toks;
+    std::vector<uint32_t> vi;
+    std::vector<int64_t> ti;
     while (pos < len) {
         size_t eol = pos;
         while (eol < len && text[eol] != '\n') eol++;
         size_t end = eol;
         if (end > pos && text[end - 1] == '\r') end--;
         line_nr++;
-        toks.clear();
-        size_t i = pos;
-        while (i < end) {
-            while (i < end && std::isspace((unsigned char)text[i])) i++;
-            size_t j = i;
-            while (j < end && !std::isspace((unsigned char)text[j])) j++;
-            if (j > i) toks.emplace_back(text + i, j - i);
-            i = j;
-        }
+        tokenize(text, pos, end, toks);
         pos = eol + 1;
         if (toks.empty()) continue;
-        const std::string& kw = toks[0];
-        char where[64];
-        std::snprintf(where, sizeof where, " (line %u)", line_nr);
+        Tok kw = toks[0];
+        // the location suffix of an error message, made only on error
+        auto where = [line_nr] { return " (line " + std::to_string(line_nr) + ")"; };
         if (kw == "v") {
             float c[3];
-            if (toks.size() < 4) return set_error(CVX_ERR_PARSE, std::string("missing vertex coordinate") + where);
+            if (toks.size() < 4) return set_error(CVX_ERR_PARSE, std::string("missing vertex coordinate") + where());
             for (int k = 0; k < 3; k++)
                 if (!parse_f32(toks[1 + k], &c[k]))
-                    return set_error(CVX_ERR_PARSE, std::string("bad vertex coordinate") + where);
+                    return set_error(CVX_ERR_PARSE, std::string("bad vertex coordinate") + where());
             mesh->vertices.insert(mesh->vertices.end(), c, c + 3);
         } else if (kw == "vt") {
             float c[2];
-            if (toks.size() < 3) return set_error(CVX_ERR_PARSE, std::string("missing texture coordinate") + where);
+            if (toks.size() < 3) return set_error(CVX_ERR_PARSE, std::string("missing texture coordinate") + where());
             for (int k = 0; k < 2; k++)
                 if (!parse_f32(toks[1 + k], &c[k]))
-                    return set_error(CVX_ERR_PARSE, std::string("bad texture coordinate") + where);
+                    return set_error(CVX_ERR_PARSE, std::string("bad texture coordinate") + where());
             mesh->tex_coords.insert(mesh->tex_coords.end(), c, c + 2);
         } else if (kw == "usemtl") {
-            if (toks.size() < 2) return set_error(CVX_ERR_PARSE, std::string("missing material name") + where);
+            if (toks.size() < 2) return set_error(CVX_ERR_PARSE, std::string("missing material name") + where());
             bool found = false;
             for (uint32_t k = 0; k < n_materials; k++)
                 if (toks[1] == names[k]) {
@@ -151,26 +181,26 @@ static int32_t parse_obj(const char* text, size_t len, const char* const* names,
                     found = true;
                 }
             if (!found)
-                return set_error(CVX_ERR_PARSE, "material '" + toks[1] + "' not present in material dictionary" + where);
+                return set_error(CVX_ERR_PARSE, "material '" + std::string(toks[1]) + "' not present in material dictionary" + where());
         } else if (kw == "f") {
-            if (toks.size() < 4) return set_error(CVX_ERR_PARSE, std::string("missing triangle index") + where);
-            std::vector<uint32_t> vi(toks.size() - 1);
-            std::vector<int64_t> ti(toks.size() - 1);
+            if (toks.size() < 4) return set_error(CVX_ERR_PARSE, std::string("missing triangle index") + where());
+            vi.resize(toks.size() - 1);
+            ti.resize(toks.size() - 1);
             for (size_t k = 1; k < toks.size(); k++)
                 if (!parse_vertex_index(toks[k], &vi[k - 1], &ti[k - 1]))
-                    return set_error(CVX_ERR_PARSE, "bad face index '" + toks[k] + "'" + where);
+                    return set_error(CVX_ERR_PARSE, "bad face index '" + std::string(toks[k]) + "'" + where());
             size_t nv = mesh->vertices.size() / 3;
             // Fan triangulation of convex n-gons (wavefront.rs:132-139).
             for (size_t k = 2; k < vi.size(); k++) {
                 uint32_t a = vi[0], b = vi[k - 1], c = vi[k];
                 if (a >= nv || b >= nv || c >= nv)
-                    return set_error(CVX_ERR_PARSE, std::string("vertex index out of range") + where);
+                    return set_error(CVX_ERR_PARSE, std::string("vertex index out of range") + where());
                 // wavefront.rs:30-46
                 S3 v0 = s3(&mesh->vertices[3 * a]), v1 = s3(&mesh->vertices[3 * b]), v2 = s3(&mesh->vertices[3 * c]);
                 S3 e1 = v0 - v2, e2 = v1 - v0;
                 S3 cr = scross(e1, e2);
                 if (sdot(cr, cr) == 0.0f)
-                    return set_error(CVX_ERR_DEGENERATE, std::string("encountered degenerate triangle") + where);
+                    return set_error(CVX_ERR_DEGENERATE, std::string("encountered degenerate triangle") + where());
                 MeshTri t;
                 t.v[0] = a;
                 t.v[1] = b;
@@ -184,6 +214,217 @@ static int32_t parse_obj(const char* text, size_t len, const char* const* names,
             }
         }
     }
+    *out = mesh.release();
+    return CVX_OK;
+}
+
+// Parallel form of the same parser for large inputs. The text is cut into
+// chunks at line starts; every chunk is tokenised concurrently into vertices,
+// texture coordinates and an ordered list of records (material switches and
+// faces, with the vertex and texture counts seen before them in the chunk).
+// Prefix sums give every record its file-global counts and active material,
+// then faces are checked (index range, degeneracy) and fan-triangulated
+// concurrently. The result, and the first error in file order, equal the
+// sequential parser's.
+struct ChunkFace {
+    uint32_t line;             // line number within the chunk (1-based)
+    uint32_t v_before, t_before;  // vertices / texture coords earlier in the chunk
+    int32_t mat_record;        // index of the last material switch in the chunk, -1: none
+    uint32_t first, count;     // the face's corners in Chunk::vi / Chunk::ti
+};
+struct Chunk {
+    size_t begin, end;
+    uint32_t lines = 0;
+    std::vector<float> v, vt;
+    std::vector<uint32_t> mats;  // material values of the chunk's switches, in order
+    std::vector<ChunkFace> faces;
+    std::vector<uint32_t> vi;
+    std::vector<int64_t> ti;
+    int32_t err = CVX_OK;
+    uint32_t err_line = 0;
+    std::string err_msg;
+};
+
+static void parse_chunk(const char* text, Chunk& c, const char* const* names, const uint32_t* materials,
+                        uint32_t n_materials) {
+    std::vector<Tok> toks;
+    size_t pos = c.begin;
+    while (pos < c.end) {
+        size_t eol = pos;
+        while (eol < c.end && text[eol] != '\n') eol++;
+        size_t end = eol;
+        if (end > pos && text[end - 1] == '\r') end--;
+        c.lines++;
+        tokenize(text, pos, end, toks);
+        pos = eol + 1;
+        if (toks.empty()) continue;
+        auto fail = [&](int32_t st, const std::string& m) {
+            c.err = st;
+            c.err_line = c.lines;
+            c.err_msg = m;
+        };
+        Tok kw = toks[0];
+        if (kw == "v") {
+            float f[3];
+            if (toks.size() < 4) return fail(CVX_ERR_PARSE, "missing vertex coordinate");
+            for (int k = 0; k < 3; k++)
+                if (!parse_f32(toks[1 + k], &f[k])) return fail(CVX_ERR_PARSE, "bad vertex coordinate");
+            c.v.insert(c.v.end(), f, f + 3);
+        } else if (kw == "vt") {
+            float f[2];
+            if (toks.size() < 3) return fail(CVX_ERR_PARSE, "missing texture coordinate");
+            for (int k = 0; k < 2; k++)
+                if (!parse_f32(toks[1 + k], &f[k])) return fail(CVX_ERR_PARSE, "bad texture coordinate");
+            c.vt.insert(c.vt.end(), f, f + 2);
+        } else if (kw == "usemtl") {
+            if (toks.size() < 2) return fail(CVX_ERR_PARSE, "missing material name");
+            bool found = false;
+            uint32_t m = 0;
+            for (uint32_t k = 0; k < n_materials; k++)
+                if (toks[1] == names[k]) {
+                    m = materials[k];
+                    found = true;
+                }
+            if (!found) return fail(CVX_ERR_PARSE, "material '" + std::string(toks[1]) + "' not present in material dictionary");
+            c.mats.push_back(m);
+        } else if (kw == "f") {
+            if (toks.size() < 4) return fail(CVX_ERR_PARSE, "missing triangle index");
+            ChunkFace f;
+            f.line = c.lines;
+            f.v_before = (uint32_t)(c.v.size() / 3);
+            f.t_before = (uint32_t)(c.vt.size() / 2);
+            f.mat_record = (int32_t)c.mats.size() - 1;
+            f.first = (uint32_t)c.vi.size();
+            f.count = (uint32_t)(toks.size() - 1);
+            for (size_t k = 1; k < toks.size(); k++) {
+                uint32_t v;
+                int64_t t;
+                if (!parse_vertex_index(toks[k], &v, &t)) return fail(CVX_ERR_PARSE, "bad face index '" + std::string(toks[k]) + "'");
+                c.vi.push_back(v);
+                c.ti.push_back(t);
+            }
+            c.faces.push_back(f);
+        }
+    }
+}
+
+static int32_t parse_obj(const char* text, size_t len, const char* const* names, const uint32_t* materials,
+                         uint32_t n_materials, cvx_mesh** out) {
+    // CONVECTOR_OBJ_THREADS=n fixes the number of chunks (1: the sequential
+    // parser) whatever the input size; by default inputs under 1 MiB are
+    // parsed sequentially and larger ones on every hardware thread.
+    unsigned hw = std::thread::hardware_concurrency();
+    size_t nchunks = std::min<size_t>(hw ? hw : 1, 64);
+    bool forced = false;
+    if (const char* env = std::getenv("CONVECTOR_OBJ_THREADS")) {
+        long n = std::strtol(env, nullptr, 10);
+        if (n >= 1) {
+            nchunks = (size_t)std::min<long>(n, 256);
+            forced = true;
+        }
+    }
+    if ((!forced && len < (1u << 20)) || nchunks < 2 || len == 0)
+        return parse_obj_sequential(text, len, names, materials, n_materials, out);
+    // Cut at line starts.
+    std::vector<Chunk> ch(nchunks);
+    size_t at = 0;
+    for (size_t k = 0; k < nchunks; k++) {
+        ch[k].begin = at;
+        size_t e = k + 1 == nchunks ? len : std::max(at, len * (k + 1) / nchunks);
+        while (e > 0 && e < len && text[e - 1] != '\n') e++;
+        ch[k].end = e;
+        at = e;
+    }
+    {
+        std::vector<std::thread> pool;
+        for (auto& c : ch) pool.emplace_back([&, cp = &c] { parse_chunk(text, *cp, names, materials, n_materials); });
+        for (auto& t : pool) t.join();
+    }
+    // Global counts before each chunk; the first tokenising error in file order.
+    std::vector<uint32_t> line0(nchunks), v0(nchunks), t0(nchunks), mat0(nchunks);
+    uint32_t lines = 0, nv = 0, nt = 0, mat = 0x00ffffffu;  // SMaterial::white()
+    for (size_t k = 0; k < nchunks; k++) {
+        line0[k] = lines;
+        v0[k] = nv;
+        t0[k] = nt;
+        mat0[k] = mat;
+        if (ch[k].err) {
+            char where[64];
+            std::snprintf(where, sizeof where, " (line %u)", lines + ch[k].err_line);
+            // a face error earlier in the file must win over this one
+            ch[k].err_line += lines;
+            ch[k].err_msg += where;
+        }
+        lines += ch[k].lines;
+        nv += (uint32_t)(ch[k].v.size() / 3);
+        nt += (uint32_t)(ch[k].vt.size() / 2);
+        if (!ch[k].mats.empty()) mat = ch[k].mats.back();
+    }
+    std::unique_ptr<cvx_mesh> mesh(new cvx_mesh());
+    mesh->vertices.reserve((size_t)nv * 3);
+    mesh->tex_coords.reserve((size_t)nt * 2);
+    for (auto& c : ch) {
+        mesh->vertices.insert(mesh->vertices.end(), c.v.begin(), c.v.end());
+        mesh->tex_coords.insert(mesh->tex_coords.end(), c.vt.begin(), c.vt.end());
+    }
+    // Faces: range and degeneracy checks and fan triangulation, per chunk.
+    std::vector<std::vector<MeshTri>> tris(nchunks);
+    std::vector<uint32_t> face_err_line(nchunks, 0);
+    std::vector<int32_t> face_err(nchunks, CVX_OK);
+    std::vector<std::string> face_msg(nchunks);
+    {
+        std::vector<std::thread> pool;
+        for (size_t k = 0; k < nchunks; k++)
+            pool.emplace_back([&, k] {
+                for (const ChunkFace& f : ch[k].faces) {
+                    const uint32_t* vi = &ch[k].vi[f.first];
+                    const int64_t* ti = &ch[k].ti[f.first];
+                    uint32_t visible = v0[k] + f.v_before;  // vertices defined before this line
+                    uint32_t material = f.mat_record >= 0 ? ch[k].mats[f.mat_record] : mat0[k];
+                    auto where = [&] { return " (line " + std::to_string(line0[k] + f.line) + ")"; };
+                    for (size_t j = 2; j < f.count; j++) {
+                        uint32_t a = vi[0], b = vi[j - 1], c = vi[j];
+                        if (a >= visible || b >= visible || c >= visible) {
+                            face_err[k] = CVX_ERR_PARSE;
+                            face_err_line[k] = line0[k] + f.line;
+                            face_msg[k] = std::string("vertex index out of range") + where();
+                            return;
+                        }
+                        S3 va = s3(&mesh->vertices[3 * (size_t)a]), vb = s3(&mesh->vertices[3 * (size_t)b]),
+                           vc = s3(&mesh->vertices[3 * (size_t)c]);
+                        S3 cr = scross(va - vc, vb - va);
+                        if (sdot(cr, cr) == 0.0f) {
+                            face_err[k] = CVX_ERR_DEGENERATE;
+                            face_err_line[k] = line0[k] + f.line;
+                            face_msg[k] = std::string("encountered degenerate triangle") + where();
+                            return;
+                        }
+                        MeshTri t;
+                        t.v[0] = a;
+                        t.v[1] = b;
+                        t.v[2] = c;
+                        bool has_t = ti[0] >= 0 && ti[j - 1] >= 0 && ti[j] >= 0;
+                        t.t[0] = has_t ? ti[0] : -1;
+                        t.t[1] = has_t ? ti[j - 1] : -1;
+                        t.t[2] = has_t ? ti[j] : -1;
+                        t.material = material;
+                        tris[k].push_back(t);
+                    }
+                }
+            });
+        for (auto& t : pool) t.join();
+    }
+    // The first error in file order: a chunk's tokenising error stops that
+    // chunk, so its face errors can only come from lines before it.
+    for (size_t k = 0; k < nchunks; k++) {
+        bool fe = face_err[k] != CVX_OK, te = ch[k].err != CVX_OK;
+        if (fe && (!te || face_err_line[k] < ch[k].err_line)) return set_error(face_err[k], face_msg[k]);
+        if (te) return set_error(ch[k].err, ch[k].err_msg);
+    }
+    size_t total = 0;
+    for (auto& t : tris) total += t.size();
+    mesh->triangles.reserve(total);
+    for (auto& t : tris) mesh->triangles.insert(mesh->triangles.end(), t.begin(), t.end());
     *out = mesh.release();
     return CVX_OK;
 }

@@ -9,6 +9,8 @@ import re
 import numpy as np
 import pytest
 
+from convector_gb300 import scenes
+
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 REFERENCE = os.environ.get("CONVECTOR_REFERENCE", "/root/reference")
 
@@ -199,3 +201,84 @@ def test_scene_triangle_arrays_equal_loaded_obj(cvx, gen):
     a = cvx.Bvh.from_meshes([cvx.Mesh.parse(text, mats)])
     b = cvx.Bvh.build(tris)
     assert (a.triangles == b.triangles).all() and (a.nodes == b.nodes).all()
+
+
+def _parse_with_threads(cvx, monkeypatch, text, mats, threads):
+    monkeypatch.setenv("CONVECTOR_OBJ_THREADS", str(threads))
+    try:
+        m = cvx.Mesh.parse(text, mats)
+    except cvx.CvxError as e:
+        return ("error", e.status, str(e))
+    b = cvx.Bvh.from_meshes([m])
+    return ("ok", m.num_triangles, b.triangles.tobytes(), b.nodes.tobytes(), b.source_index.tobytes())
+
+
+@pytest.mark.parametrize("threads", [2, 3, 7, 16, 61])
+def test_parallel_obj_parse_equals_sequential(cvx, monkeypatch, threads):
+    """The chunked parser gives the sequential parser's mesh (materials carried
+    across chunk boundaries, vertex indices checked against the vertices
+    defined before each face) on a mixed scene with quads and tex coords."""
+    text, mats = scenes.room_sphere()
+    extra = "".join("vt %d 0.5\n" % k for k in range(5)) + "usemtl wall\n" + "f 1/1 2/2 3/3 4/4\n" * 3
+    text = text + extra
+    seq = _parse_with_threads(cvx, monkeypatch, text, mats, 1)
+    assert seq[0] == "ok"
+    assert _parse_with_threads(cvx, monkeypatch, text, mats, threads) == seq
+
+
+@pytest.mark.parametrize("threads", [2, 5, 13])
+def test_parallel_obj_parse_reports_the_first_error(cvx, monkeypatch, threads):
+    """Whichever chunk holds it, the first error in file order is the one
+    reported, with the sequential parser's status, message and line."""
+    text, mats = scenes.room_sphere()
+    lines = text.splitlines(keepends=True)
+    n = len(lines)
+    cases = []
+    for frac in (0.1, 0.5, 0.9):
+        at = int(n * frac)
+        # a face before its vertices exist, then a tokenising error later
+        cases.append(lines[:at] + ["f 1 2 999999\n"] + lines[at:at + 40] + ["v 0 zz 0\n"] + lines[at + 40:])
+        # a tokenising error first, then a degenerate face
+        cases.append(lines[:at] + ["usemtl nosuch\n"] + lines[at:] + ["v 9 9 9\nf 1 1 2\n"])
+        # degenerate face only
+        cases.append(lines[:at] + ["f 1 1 2\n"] + lines[at:])
+    for c in cases:
+        t = "".join(c)
+        seq = _parse_with_threads(cvx, monkeypatch, t, mats, 1)
+        assert seq[0] == "error"
+        assert _parse_with_threads(cvx, monkeypatch, t, mats, threads) == seq
+
+
+def test_parallel_obj_parse_edge_inputs(cvx, monkeypatch):
+    def count(text, threads):
+        monkeypatch.setenv("CONVECTOR_OBJ_THREADS", str(threads))
+        return cvx.Mesh.parse(text).num_triangles
+
+    for text, n in [("", 0), ("\n\n", 0), ("v 0 0 0", 0), ("# only a comment\r\n", 0),
+                    ("v 0 0 0\nv 1 0 0\nv 0 1 0\nf 1 2 3", 1), ("v 0 0 0\r\nv 1 0 0\r\nv 0 1 0\r\nf 1 2 3\r\n", 1)]:
+        for threads in (1, 2, 8, 64):
+            assert count(text, threads) == n, (text, threads)
+
+
+@pytest.mark.parametrize("tok", ["1.", ".5", "+1.5", "-0", "1e-50", "2.5e+1", "7E-1", "0.1", "1234567.891",
+                                 "0.30000001192092896", "16777217", "1e-40"])
+def test_obj_vertex_coordinates_round_like_rust(cvx, tok):
+    """Coordinates are parsed as f32::from_str does: correctly rounded, with a
+    leading '+', a bare fraction or exponent, and subnormal results."""
+    quad = "v 50 0 0\nv 51 0 0\nv 51 1 0\nv 50 1 0\nf 4 5 6 7\n"
+    m = cvx.Mesh.parse("v %s 0 0\nv 1 1 0\nv 0 1 1\nf 1 2 3\n" % tok + quad)
+    b = cvx.Bvh.from_meshes([m])
+    t = b.triangles_f32[list(b.source_index).index(0)]
+    assert t[0] == np.float32(float(tok))
+
+
+@pytest.mark.parametrize("tok,ok", [("1e50", True), ("inf", True), ("-inf", True), ("NaN", True),
+                                    ("0x1p3", False), ("1.0f", False), ("--1", False), ("+-1", False),
+                                    ("1e", False), (".", False), ("e5", False)])
+def test_obj_vertex_coordinate_syntax(cvx, tok, ok):
+    text = "v %s 0 0\n" % tok
+    if ok:
+        assert cvx.Mesh.parse(text).num_triangles == 0
+    else:
+        with pytest.raises(cvx.CvxError, match="bad vertex coordinate"):
+            cvx.Mesh.parse(text)
