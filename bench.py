@@ -303,19 +303,20 @@ def run_ours(args):
     e2e_s = reduce_max(time.perf_counter() - t0, dist if world > 1 else None, "cuda")
     e2e_value = replica_value(n * e2e_steps, world, e2e_s)
 
-    render = batched = served = large = None
+    render = batched = served = large = bvh_build = None
     if rank == 0 and not args.no_render:
         render = _guard(bench_render, cg)
     if rank == 0 and not args.no_extra:
         large = _guard(bench_large, cg)
         batched = _guard(bench_batched, cg)
         served = _guard(bench_served, cg)
+        bvh_build = _guard(bench_bvh_build, cg)
 
     if rank == 0:
         peak, peak_kind = _peaks()
         bytes_launch = algo[trav]["bytes"]
         achieved = bytes_launch / (ms_per_step * 1e-3) / 1e9
-        kname = "k_intersect_packet" if trav == 0 else "k_intersect_single"
+        kname = "k_intersect_packet" if trav == 0 else "k_intersect_refill"
         cpu = None
         if world == 1:
             from oracle import oracle as orc
@@ -345,6 +346,7 @@ def run_ours(args):
             "large_accumulate": large,
             "batched": batched,
             "served": served,
+            "bvh_build": bvh_build,
         }
         print(json.dumps(line))
     if world > 1:
@@ -497,17 +499,58 @@ def _served_run(cg, scs, reqs, sequential):
             "waves": st["waves"], "device_busy_s": st["busy_s"]}
 
 
+def _plain_renderer_run(cg, scs, bvhs, reqs):
+    """The plain method: the drop-in Renderer API, one request at a time in
+    arrival order. Each request gets a Renderer at its resolution, spp
+    accumulate_frame_f32 calls and a resolve_u8 read back to the host; the
+    scene's kernel form is the server's default rule (wavefront for BVHs
+    deeper than 40 or above 200k triangles, else the single-launch form)."""
+    modes = [cg.MODE_WAVEFRONT if (b.depth > 40 or b.triangles.shape[0] > 200000) else cg.MODE_MEGAKERNEL
+             for b in bvhs]
+
+    def run(sc, w, h, spp, cam, base):
+        r = cg.Renderer(scs[sc], w, h, rng_order=cg.RNG_GROUP, traversal=cg.TRAVERSE_SINGLE, mode=modes[sc],
+                        use_graph=1 if modes[sc] == cg.MODE_WAVEFRONT else 0)
+        r.set_camera(cam)
+        n = 0
+        for s in range(spp):
+            r.accumulate_frame_f32(base + s)
+            n += r.stats()[0]  # rays of the last frame
+        r.resolve_u8(spp)
+        return n
+
+    for k in range(len(scs)):  # warm-up: one small request per scene
+        run(k, 64, 64, 1, reqs[0][5], 0)
+    lat, rays = [], 0
+    t0 = time.perf_counter()
+    first = last = None
+    for i, (at, sc, w, h, spp, cam) in enumerate(reqs):
+        dt = t0 + at - time.perf_counter()
+        if dt > 0:
+            time.sleep(dt)
+        start = time.perf_counter()
+        first = start if first is None else first
+        rays += run(sc, w, h, spp, cam, i * 16)
+        last = time.perf_counter()
+        lat.append((last - (t0 + at)) * 1e3)
+    span = last - min(t0 + reqs[0][0], first)
+    lat = np.array(lat)
+    return {"requests": len(reqs), "latency_ms_p50": float(np.percentile(lat, 50)),
+            "latency_ms_p99": float(np.percentile(lat, 99)), "mrays_per_s": rays / span / 1e6, "span_s": span}
+
+
 def bench_served(cg, duration=2.0, rate=200.0, seed=4):
     """Poisson arrivals (200 req/s) over 3 resident scenes (room+sphere,
     displaced icosphere, random-walk tube); camera on a radius-3 sphere around
     the room centre, resolution log-uniform 320x184..1920x1080, 1..16 spp.
     Continuously batched server against the one-request-at-a-time path."""
     from convector_gb300 import scenes
-    scs = []
+    scs, bvhs = [], []
     for gen in (scenes.room_sphere, lambda obj: scenes.displaced_icosphere(obj=obj, light=True),
                 scenes.random_walk_tube):
         tris, _ = gen(obj=False)
-        scs.append(cg.Scene(cg.Bvh.build(tris)))
+        bvhs.append(cg.Bvh.build(tris))
+        scs.append(cg.Scene(bvhs[-1]))
     rng = np.random.default_rng(seed)
     center = np.array([0.0, 1.25, -2.0])
     reqs, t = [], 0.0
@@ -523,9 +566,35 @@ def bench_served(cg, duration=2.0, rate=200.0, seed=4):
         h = int(min(1080, max(184, round(w * 184 / 320))))
         reqs.append((t, int(rng.integers(0, 3)), w, h, int(rng.integers(1, 17)), cam))
     served = _served_run(cg, scs, reqs, sequential=False)
-    plain = _served_run(cg, scs, reqs, sequential=True)
-    return {"rate_per_s": rate, "duration_s": duration, "served": served, "plain_sequential": plain,
-            "throughput_ratio": served["mrays_per_s"] / plain["mrays_per_s"]}
+    sequential = _served_run(cg, scs, reqs, sequential=True)
+    plain = _plain_renderer_run(cg, scs, bvhs, reqs)
+    return {"rate_per_s": rate, "duration_s": duration, "served": served, "plain_renderer": plain,
+            "server_one_at_a_time": sequential,
+            "throughput_ratio": served["mrays_per_s"] / plain["mrays_per_s"],
+            "throughput_ratio_vs_server_one_at_a_time": served["mrays_per_s"] / sequential["mrays_per_s"]}
+
+
+def bench_bvh_build(cg):
+    """Host build against the device build (same output) for the ray-cast
+    scene and the ~870k-triangle tube; best of 3 wall-clock runs."""
+    from convector_gb300 import scenes
+    out = {}
+    for name, gen in (("displaced_icosphere", lambda: scenes.displaced_icosphere(obj=False)[0]),
+                      ("random_walk_tube", lambda: scenes.random_walk_tube(obj=False)[0])):
+        tris = gen()
+        cg.Bvh.build_device(tris[:4096])  # context and table warm-up
+        th, td = [], []
+        for _ in range(3):
+            t0 = time.perf_counter()
+            a = cg.Bvh.build(tris)
+            th.append(time.perf_counter() - t0)
+            t0 = time.perf_counter()
+            b = cg.Bvh.build_device(tris)
+            td.append(time.perf_counter() - t0)
+        same = bool(np.array_equal(a.nodes, b.nodes) and np.array_equal(a.source_index, b.source_index))
+        out[name] = {"triangles": int(tris.shape[0]), "host_ms": 1e3 * min(th), "device_ms": 1e3 * min(td),
+                     "host_threads": os.cpu_count(), "identical": same}
+    return out
 
 
 def main():
@@ -536,7 +605,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-render", action="store_true")
     ap.add_argument("--no-extra", action="store_true", help="skip the large, batched and served sections")
-    ap.add_argument("--section", choices=["render", "large", "batched", "served"],
+    ap.add_argument("--section", choices=["render", "large", "batched", "served", "bvh"],
                     help="run one extra section alone and print its JSON (no headline line)")
     args = ap.parse_args()
     if args.warmup < 3:
@@ -544,7 +613,8 @@ def main():
     if args.section:
         import convector_gb300 as cg
         cg.lib(build=True)
-        fn = {"render": bench_render, "large": bench_large, "batched": bench_batched, "served": bench_served}
+        fn = {"render": bench_render, "large": bench_large, "batched": bench_batched, "served": bench_served,
+              "bvh": bench_bvh_build}
         print(json.dumps({args.section: fn[args.section](cg)}))
         return
     if args.impl == "reference":

@@ -95,6 +95,7 @@ def lib(build=False):
         "cvx_mesh_destroy": (None, [P]),
         "cvx_bvh_from_meshes": (I32, [P, U32, P]),
         "cvx_bvh_build": (I32, [P, U32, P]),
+        "cvx_bvh_build_device": (I32, [P, U32, P]),
         "cvx_bvh_num_nodes": (U32, [P]),
         "cvx_bvh_num_triangles": (U32, [P]),
         "cvx_bvh_copy_nodes": (None, [P, P]),
@@ -268,6 +269,14 @@ class Bvh:
         tris = np.ascontiguousarray(triangles).view(np.uint32).reshape(-1, TRIANGLE_DTYPE_WORDS)
         out = ctypes.c_void_p()
         _check(lib().cvx_bvh_build(_ptr(tris), tris.shape[0], ctypes.byref(out)))
+        return Bvh(out.value)
+
+    @staticmethod
+    def build_device(triangles):
+        """Bvh.build on the GPU: identical nodes, triangle order and statistics."""
+        tris = np.ascontiguousarray(triangles).view(np.uint32).reshape(-1, TRIANGLE_DTYPE_WORDS)
+        out = ctypes.c_void_p()
+        _check(lib().cvx_bvh_build_device(_ptr(tris), tris.shape[0], ctypes.byref(out)))
         return Bvh(out.value)
 
     @property

@@ -18,7 +18,7 @@ INCLUDE = os.path.join(os.path.dirname(PKG), "include")
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "lib", "libconvector_gpu.so")
 
-CU_SOURCES = ["kernels.cu", "wavefront.cu", "engine.cu", "capi.cu", "noalloc.cu", "postprocess.cu"]
+CU_SOURCES = ["kernels.cu", "wavefront.cu", "engine.cu", "capi.cu", "noalloc.cu", "postprocess.cu", "bvh_build.cu"]
 CPP_SOURCES = ["host_scene.cpp"]
 HEADERS = ["x86sem.cuh", "layout.cuh", "traverse.cuh", "shade.cuh", "kernels.h", "internal.h",
            "x86_approx_tables.h", "wavefront.cuh", "engine.h"]

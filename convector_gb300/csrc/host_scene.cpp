@@ -13,6 +13,7 @@
 #include <fstream>
 #include <future>
 #include <memory>
+#include <mutex>
 #include <sstream>
 #include <string>
 #include <string_view>
@@ -478,14 +479,22 @@ struct Bin {  // bvh.rs:64-121
     void clear() { tris.clear(); }
 };
 
-// TreeSurfaceAreaHeuristic (bvh.rs:452-474) with the constants of bvh.rs:500-504.
+// TreeSurfaceAreaHeuristic (bvh.rs:452-474) with the constants of bvh.rs:500-504:
+//   aabb_term = 1 + ac_ap * (2p - n p^m) / (p - 2p^2),  m = log2(n)
+//   tri_term  = n p^(m-1) * ac_ap
+// The factors that depend on n alone (tsah_x, tsah_t) are shared with the
+// device build, which reads them from a table made here, so that both builds
+// round every operation alike.
+static const float kTsahP = 0.8f;
+static inline float tsah_x(float n) { return 2.0f * kTsahP - n * std::pow(kTsahP, std::log2(n)); }
+static inline float tsah_t(float n) { return n * std::pow(kTsahP, std::log2(n) - 1.0f); }
+static inline float tsah_y() { return kTsahP - 2.0f * kTsahP * kTsahP; }
 static inline float tsah_aabb_cost(const Aabb& parent, const Aabb& box, size_t num_tris) {
-    const float aabb_cost = 40.0f, tri_cost = 120.0f, p = 0.8f;
+    const float aabb_cost = 40.0f, tri_cost = 120.0f;
     float ac_ap = area(box) / area(parent);
     float n = (float)num_tris;
-    float m = std::log2(n);
-    float aabb_term = 1.0f + ac_ap * (2.0f * p - n * std::pow(p, m)) / (p - 2.0f * p * p);
-    float tri_term = n * std::pow(p, m - 1.0f) * ac_ap;
+    float aabb_term = 1.0f + ac_ap * tsah_x(n) / tsah_y();
+    float tri_term = tsah_t(n) * ac_ap;
     return aabb_term * aabb_cost + tri_term * tri_cost;
 }
 static inline float tsah_tris_cost(size_t n) { return (float)n * 120.0f; }
@@ -656,6 +665,93 @@ static void crystallize(const Interim& n, const std::vector<cvx_triangle>& src, 
             out.source_index.push_back(t.index);
         }
     }
+}
+
+void tsah_tables(uint32_t n, std::vector<float>& x, std::vector<float>& t, float* y) {
+    // Grown on demand and kept: the factors depend on the count alone.
+    static std::mutex mu;
+    static std::vector<float> cx{0.0f}, ct{0.0f};
+    {
+        std::lock_guard<std::mutex> lk(mu);
+        for (uint32_t k = (uint32_t)cx.size(); k <= n; k++) {
+            cx.push_back(tsah_x((float)k));
+            ct.push_back(tsah_t((float)k));
+        }
+        x.assign(cx.begin(), cx.begin() + (size_t)n + 1);
+        t.assign(ct.begin(), ct.begin() + (size_t)n + 1);
+    }
+    *y = tsah_y();
+}
+
+// crystallize (bvh.rs:389-428) and the statistics of bvh.rs:536-545 over an
+// interim tree built elsewhere (the device build): node 0 is the root, a
+// leaf's triangles are order[beg .. beg + cnt) in leaf order.
+static float interim_area(const InterimNode& n) {
+    Aabb a{S3{n.lo[0], n.lo[1], n.lo[2]}, S3{n.hi[0], n.hi[1], n.hi[2]}};
+    return area(a);
+}
+static float interim_summed_area_ratio(const std::vector<InterimNode>& t, uint32_t i) {  // bvh.rs:380-385
+    const InterimNode& n = t[i];
+    if (!n.c0) return 0.0f;
+    float child_contrib = 0.0f;
+    child_contrib += interim_summed_area_ratio(t, n.c0);
+    child_contrib += interim_summed_area_ratio(t, n.c1);
+    float self_area = interim_area(n);
+    float child_sum = 0.0f;
+    child_sum += interim_area(t[n.c0]) / self_area;
+    child_sum += interim_area(t[n.c1]) / self_area;
+    return child_sum + child_contrib;
+}
+static void interim_crystallize(const std::vector<InterimNode>& t, uint32_t i, const std::vector<uint32_t>& order,
+                                const cvx_triangle* src, cvx_bvh& out, size_t into, uint32_t depth, size_t* leaves) {
+    const InterimNode& n = t[i];
+    cvx_bvh_node& nd = out.nodes[into];
+    for (int k = 0; k < 3; k++) {
+        nd.origin[k] = n.lo[k];
+        nd.far_[k] = n.hi[k];
+    }
+    out.depth = std::max(out.depth, depth);
+    if (n.c0) {
+        size_t child = out.nodes.size();
+        out.nodes.push_back(cvx_bvh_node{});
+        out.nodes.push_back(cvx_bvh_node{});
+        interim_crystallize(t, n.c0, order, src, out, child, depth + 1, leaves);
+        interim_crystallize(t, n.c1, order, src, out, child + 1, depth + 1, leaves);
+        out.nodes[into].index = (uint32_t)child;
+        out.nodes[into].len = 0;
+    } else {
+        (*leaves)++;
+        out.nodes[into].index = (uint32_t)out.triangles.size();
+        out.nodes[into].len = n.cnt;
+        for (uint32_t k = 0; k < n.cnt; k++) {
+            uint32_t tri = order[n.beg + k];
+            out.triangles.push_back(src[tri]);
+            out.source_index.push_back(tri);
+        }
+    }
+}
+
+int32_t bvh_from_interim(const std::vector<InterimNode>& t, const std::vector<uint32_t>& order,
+                         const cvx_triangle* src, uint32_t n, cvx_bvh** out) {
+    const InterimNode& root = t[0];
+    if (!root.c0)
+        return set_error(CVX_ERR_INVALID,
+                         "the BVH root did not split: the reference needs at least two root nodes (bvh.rs:509-512)");
+    std::unique_ptr<cvx_bvh> bvh(new cvx_bvh());
+    bvh->nodes.reserve(t.size());
+    bvh->triangles.reserve(n);
+    bvh->source_index.reserve(n);
+    bvh->nodes.push_back(cvx_bvh_node{});
+    bvh->nodes.push_back(cvx_bvh_node{});
+    size_t leaves = 0;
+    interim_crystallize(t, root.c0, order, src, *bvh, 0, 1, &leaves);
+    interim_crystallize(t, root.c1, order, src, *bvh, 1, 1, &leaves);
+    if (bvh->triangles.size() != n) return set_error(CVX_ERR_DEVICE, "device BVH build lost triangles");
+    size_t num_nodes = bvh->nodes.size() + 1;  // the interim nodes: crystallized ones and the root
+    bvh->avg_area_ratio = interim_summed_area_ratio(t, 0) / (float)num_nodes;
+    bvh->avg_tris_per_leaf = (float)n / (float)leaves;
+    *out = bvh.release();
+    return CVX_OK;
 }
 
 static int32_t build(const cvx_triangle* tris, uint32_t n, cvx_bvh** out) {

@@ -10,6 +10,22 @@ namespace cvx {
 
 int32_t set_error(int32_t status, const std::string& msg);
 
+// A node of the interim tree of the device BVH build (bvh.rs:52-62): its
+// exact bounding box, its triangles order[beg .. beg + cnt) and its children
+// (c0 == 0: a leaf; node 0 is the root and never a child).
+struct InterimNode {
+    float lo[3], hi[3];
+    uint32_t beg, cnt;
+    uint32_t c0, c1;
+};
+
+// TSAH factors for triangle counts 0..n (index 0 unused) and the constant
+// denominator, as the host build computes them.
+void tsah_tables(uint32_t n, std::vector<float>& x, std::vector<float>& t, float* y);
+// crystallize and statistics over an interim tree (same results as the host build).
+int32_t bvh_from_interim(const std::vector<InterimNode>& t, const std::vector<uint32_t>& order,
+                         const cvx_triangle* src, uint32_t n, cvx_bvh** out);
+
 struct MeshTri {
     uint32_t v[3];
     int64_t t[3];  // -1: the face has no texture coordinates

@@ -132,9 +132,9 @@ struct SoaRays {
 template <int MINB>
 __global__ void __launch_bounds__(128, MINB) k_intersect_refill(SoaRays src, uint32_t* __restrict__ next_ray,
                                                                 uint32_t* __restrict__ err) {
-    __shared__ ApproxTables tab;
-    load_tables(tab);
-    if (!traverse_refill(src, src.n, next_ray, tab)) atomicOr(err, kErrStackOverflow);
+    // The reciprocal table is read three times per ray: from global memory
+    // (L1-resident), which leaves the shared-memory carve-out to L1.
+    if (!traverse_refill(src, src.n, next_ray, g_tables)) atomicOr(err, kErrStackOverflow);
 }
 
 // ---------------------------------------------------------------------------

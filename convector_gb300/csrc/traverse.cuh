@@ -166,7 +166,12 @@ __device__ __forceinline__ bool traverse_refill(const Src& src, uint32_t n, uint
     const int lane = threadIdx.x & 31;
     const float4* nodes = nullptr;
     const float4* geom = nullptr;
-    uint2 stack[kStackDepth];  // (ref, entry distance bits)
+    // (ref, entry distance bits). The top entry lives in `top`, entries
+    // below it in local memory: a pop takes `top` at once and reloads the
+    // next one from memory, so that load's latency hides behind the work on
+    // the popped node.
+    uint2 stack[kStackDepth];
+    uint2 top = make_uint2(0u, 0u);
     int sp = 0;
     uint32_t ray = 0, na = 0, nt = 0;
     uint32_t cur = 0;  // ref of the node to process; kNone: pop
@@ -206,7 +211,8 @@ __device__ __forceinline__ bool traverse_refill(const Src& src, uint32_t n, uint
         if (cur == kNone) {
             // Pop until an entry survives the cull test (aabb.rs:171-177).
             while (sp > 0) {
-                uint2 e = stack[--sp];
+                uint2 e = top;
+                if (--sp > 0) top = stack[sp - 1];
                 if (!geq(__uint_as_float(e.y), h.t)) {
                     cur = e.x;
                     break;
@@ -251,7 +257,11 @@ __device__ __forceinline__ bool traverse_refill(const Src& src, uint32_t n, uint
             cur = kNone;
             continue;
         }
-        if (hit_first) stack[sp++] = make_uint2(ref_first, __float_as_uint(t_first));
+        if (hit_first) {
+            if (sp > 0) stack[sp - 1] = top;
+            top = make_uint2(ref_first, __float_as_uint(t_first));
+            sp++;
+        }
         cur = (hit_second && !geq(t_second, h.t)) ? ref_second : kNone;
     }
     return !overflow;

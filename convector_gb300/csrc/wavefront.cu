@@ -188,10 +188,8 @@ struct QueueRays {
 __global__ void __launch_bounds__(128) k_wf_traverse_single(const Job* __restrict__ jobs,
                                                             const DeviceScene* __restrict__ scenes, WaveState st,
                                                             int bounce, WaveOutputs out) {
-    __shared__ ApproxTables tab;
-    load_tables_wf(tab);
     QueueRays src{jobs, scenes, st, st.queue[bounce & 1]};
-    if (!traverse_refill(src, st.counts[bounce] * 8u, &st.counts[6 + bounce], tab))
+    if (!traverse_refill(src, st.counts[bounce] * 8u, &st.counts[6 + bounce], g_tables_wf))
         atomicOr(out.err, kErrStackOverflow);
 }
 

@@ -88,6 +88,11 @@ void cvx_mesh_destroy(cvx_mesh* mesh);
  * reference's binned tree-SAH build, node order and triangle order. */
 int32_t cvx_bvh_from_meshes(const cvx_mesh* const* meshes, uint32_t n_meshes, cvx_bvh** out);
 int32_t cvx_bvh_build(const cvx_triangle* triangles, uint32_t n, cvx_bvh** out);
+/* Bvh::build (bvh.rs:488-545) run on the device: the same nodes, triangle
+ * order, source indices and statistics as cvx_bvh_build, for scene admission
+ * in serving. Refuses NaN or infinite vertex coordinates (CVX_ERR_INVALID)
+ * and more than 2^26 triangles (CVX_ERR_CAPACITY). */
+int32_t cvx_bvh_build_device(const cvx_triangle* triangles, uint32_t n, cvx_bvh** out);
 uint32_t cvx_bvh_num_nodes(const cvx_bvh* bvh);
 uint32_t cvx_bvh_num_triangles(const cvx_bvh* bvh);
 /* Copies nodes / triangles (BVH order) / source index of each BVH-order
