@@ -127,14 +127,96 @@ struct SoaRays {
     }
 };
 
+// Staged ray supply of the isolated query: a warp claims 32 consecutive rays
+// at a time and copies them into shared memory with cp.async, one batch ahead
+// of use. A lane that finishes a ray takes the next one from shared memory, so
+// neither the claim's atomic nor the ray's DRAM load stalls the warp.
+__device__ __forceinline__ void cp_async4(void* smem, const void* gmem) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"((uint32_t)__cvta_generic_to_shared(smem)),
+                 "l"(__cvta_generic_to_global(gmem)));
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_one_pending() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
+
+struct StagedSoaClaim {
+    const SoaRays& src;
+    uint32_t* next_ray;
+    float (*buf)[6][32];  // this warp's two batches: [batch][component][slot]
+    uint32_t base_cur, base_nxt, used;
+    int cur;
+
+    __device__ __forceinline__ uint32_t claim32(int lane) {
+        uint32_t b = 0;
+        if (lane == 0) b = atomicAdd(next_ray, 32u);
+        return __shfl_sync(0xffffffffu, b, 0);
+    }
+    __device__ __forceinline__ void issue(int which, uint32_t base, int lane) {
+        uint32_t r = base + (uint32_t)lane;
+        if (r < src.n)
+            for (int c = 0; c < 6; c++) cp_async4(&buf[which][c][lane], src.rays + (size_t)c * src.n + r);
+        cp_async_commit();
+    }
+    __device__ __forceinline__ void init(int lane) {
+        base_cur = claim32(lane);
+        issue(0, base_cur, lane);
+        base_nxt = claim32(lane);
+        issue(1, base_nxt, lane);
+        cp_async_wait_one_pending();
+        __syncwarp();
+        cur = 0;
+        used = 0;
+    }
+    __device__ __forceinline__ int claim(unsigned b, bool want, int lane, uint32_t& r, RayIn& in) {
+        uint32_t k = (uint32_t)__popc(b);
+        if (used + k > 32u) {  // some lanes take from the next batch: it must have landed
+            cp_async_wait_all();
+            __syncwarp();
+        }
+        int res = kClaimNone;
+        if (want) {
+            uint32_t t = used + (uint32_t)__popc(b & ((1u << lane) - 1u));
+            int which = t < 32u ? cur : cur ^ 1;
+            uint32_t slot = t & 31u;
+            r = (t < 32u ? base_cur : base_nxt) + slot;
+            if (r < src.n) {
+                in.o = f3(buf[which][0][slot], buf[which][1][slot], buf[which][2][slot]);
+                in.d = f3(buf[which][3][slot], buf[which][4][slot], buf[which][5][slot]);
+                in.far = src.far_dist;
+                in.nodes = src.nodes;
+                in.geom = src.geom;
+                res = kClaimRay;
+            } else {
+                res = kClaimDone;
+            }
+        }
+        used += k;
+        if (used >= 32u) {  // the current batch is used up: the next one becomes current
+            __syncwarp();    // every read of the old batch is done
+            used -= 32u;
+            cur ^= 1;
+            base_cur = base_nxt;
+            cp_async_wait_all();
+            __syncwarp();
+            base_nxt = claim32(lane);
+            issue(cur ^ 1, base_nxt, lane);
+        }
+        return res;
+    }
+};
+
 // MINB: resident blocks per SM the register allocation must allow (8: the
-// compiler's choice, 56 registers; 10 and 12 cap registers for occupancy).
+// compiler's choice, 64 registers; 10 and 12 cap registers for occupancy).
 template <int MINB>
 __global__ void __launch_bounds__(128, MINB) k_intersect_refill(SoaRays src, uint32_t* __restrict__ next_ray,
                                                                 uint32_t* __restrict__ err) {
     // The reciprocal table is read three times per ray: from global memory
     // (L1-resident), which leaves the shared-memory carve-out to L1.
-    if (!traverse_refill(src, src.n, next_ray, g_tables)) atomicOr(err, kErrStackOverflow);
+    __shared__ float stage[4][2][6][32];
+    StagedSoaClaim claim{src, next_ray, stage[threadIdx.x >> 5], 0u, 0u, 0u, 0};
+    claim.init(threadIdx.x & 31);
+    bool ok = traverse_refill(src, claim, g_tables);
+    if (!ok) atomicOr(err, kErrStackOverflow);
 }
 
 // ---------------------------------------------------------------------------
@@ -320,7 +402,7 @@ cudaError_t launch_intersect(const DeviceScene& s, const float* rays, uint32_t n
         // persistent ray-refill kernel; err[1] is its ray counter
         cudaError_t e = cudaMemsetAsync(err + 1, 0, 4, st);
         if (e != cudaSuccess) return e;
-        uint32_t bps = blocks_per_sm ? blocks_per_sm : 10;
+        uint32_t bps = blocks_per_sm ? blocks_per_sm : 8;
         uint32_t blocks = (uint32_t)num_sms() * bps;
         uint32_t need = (n + 127u) / 128u;
         if (blocks > need) blocks = need;

@@ -147,22 +147,52 @@ __device__ __forceinline__ uint32_t node_ref(uint32_t node_id, uint32_t index, u
     return len < 31u ? (index << 5) | len : (node_id << 5) | 31u;
 }
 
-// Persistent single-ray traversal with ray refill over rays 0..n-1 of `src`.
+// Ray supply of the refill traversal. claim() is called by the whole warp in
+// an iteration in which the lanes of `b` want a ray; for a wanting lane it
+// returns kClaimRay with the ray's data, kClaimDone when the rays are used up,
+// or kClaimNone when the ray it took needs no tracing (the source then stored
+// that ray's result itself).
+enum : int { kClaimNone = 0, kClaimRay = 1, kClaimDone = 2 };
+
+struct RayIn {
+    F3 o, d;
+    float far;
+    const float4* nodes;
+    const float4* geom;
+};
+
+// One warp-aggregated atomic per claiming iteration; the source loads the ray.
+//   bool Src::load(r, F3& o, F3& d, float& far, const float4*& nodes, const float4*& geom)
+template <class Src>
+struct EachClaim {
+    const Src& src;
+    uint32_t n;
+    uint32_t* next_ray;
+    __device__ __forceinline__ int claim(unsigned b, bool want, int lane, uint32_t& r, RayIn& in) {
+        uint32_t base = 0;
+        int first = __ffs(b) - 1;
+        if (lane == first) base = atomicAdd(next_ray, (uint32_t)__popc(b));
+        base = __shfl_sync(0xffffffffu, base, first);
+        if (!want) return kClaimNone;
+        r = base + __popc(b & ((1u << lane) - 1u));
+        if (r >= n) return kClaimDone;
+        return src.load(r, in.o, in.d, in.far, in.nodes, in.geom) ? kClaimRay : kClaimNone;
+    }
+};
+
+// Persistent single-ray traversal with ray refill over the rays of `claim`.
 // Every iteration each lane processes one node pair or one leaf; a lane whose
-// ray is finished takes the next unclaimed ray (one warp-aggregated atomic on
-// `next_ray`), so warps stay full while rays of different lengths finish.
+// ray is finished takes the next unclaimed ray, so warps stay full while rays
+// of different lengths finish.
 // Decisions and their order are exactly those of traverse<false>: after a
 // pair test the child the reference would pop next is processed at once
 // (its cull test sees the same hit distance the pop would), the other one is
 // pushed, and culled entries are popped within the same iteration.
 // The whole warp must call this. `src` provides
-//   bool load(r, F3& o, F3& d, float& far, const float4*& nodes, const float4*& geom)
-//        (false: nothing to trace for r; load then stores r's result itself)
 //   void store(r, const Hit&, uint32_t boxes, uint32_t triangles)
 // Returns false if a ray overflowed the stack (its hit is then incomplete).
-template <class Src>
-__device__ __forceinline__ bool traverse_refill(const Src& src, uint32_t n, uint32_t* next_ray,
-                                                const ApproxTables& tab) {
+template <class Src, class Claim>
+__device__ __forceinline__ bool traverse_refill(const Src& src, Claim& claim, const ApproxTables& tab) {
     const int lane = threadIdx.x & 31;
     const float4* nodes = nullptr;
     const float4* geom = nullptr;
@@ -183,25 +213,24 @@ __device__ __forceinline__ bool traverse_refill(const Src& src, uint32_t n, uint
         bool want = !have && !done;
         unsigned b = __ballot_sync(0xffffffffu, want);
         if (b) {
-            uint32_t base = 0;
-            int first = __ffs(b) - 1;
-            if (lane == first) base = atomicAdd(next_ray, (uint32_t)__popc(b));
-            base = __shfl_sync(0xffffffffu, base, first);
+            uint32_t r = 0;
+            RayIn in;
+            int got = claim.claim(b, want, lane, r, in);
             if (want) {
-                uint32_t r = base + __popc(b & ((1u << lane) - 1u));
-                if (r < n) {
-                    float far;
+                if (got == kClaimRay) {
                     ray = r;
-                    if (src.load(r, o, d, far, nodes, geom)) {
-                        inv = f3(x_rcp(d.x, tab), x_rcp(d.y, tab), x_rcp(d.z, tab));
-                        h = Hit{far, 0.0f, 0.0f, -1};
-                        sp = 0;
-                        na = 2;
-                        nt = 0;
-                        cur = 0;  // the root pair: internal ref with index 0
-                        have = true;
-                    }
-                } else {
+                    o = in.o;
+                    d = in.d;
+                    nodes = in.nodes;
+                    geom = in.geom;
+                    inv = f3(x_rcp(d.x, tab), x_rcp(d.y, tab), x_rcp(d.z, tab));
+                    h = Hit{in.far, 0.0f, 0.0f, -1};
+                    sp = 0;
+                    na = 2;
+                    nt = 0;
+                    cur = 0;  // the root pair: internal ref with index 0
+                    have = true;
+                } else if (got == kClaimDone) {
                     done = true;
                 }
             }

@@ -189,7 +189,8 @@ __global__ void __launch_bounds__(128) k_wf_traverse_single(const Job* __restric
                                                             const DeviceScene* __restrict__ scenes, WaveState st,
                                                             int bounce, WaveOutputs out) {
     QueueRays src{jobs, scenes, st, st.queue[bounce & 1]};
-    if (!traverse_refill(src, st.counts[bounce] * 8u, &st.counts[6 + bounce], g_tables_wf))
+    EachClaim<QueueRays> claim{src, st.counts[bounce] * 8u, &st.counts[6 + bounce]};
+    if (!traverse_refill(src, claim, g_tables_wf))
         atomicOr(out.err, kErrStackOverflow);
 }
 

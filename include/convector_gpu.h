@@ -123,7 +123,7 @@ uint32_t cvx_scene_num_direct_samples(const cvx_scene* scene);
  * triangles); 1 (default): `(bits * n) >> 32`, identical to it when n == 8. */
 int32_t cvx_scene_set_light_pick(cvx_scene* scene, uint32_t light_pick);
 /* Launch shape of this scene's nearest-hit queries: resident 128-thread
- * blocks per SM (0: default 10; the single-ray kernel is built for 8, 10 and
+ * blocks per SM (0: default 8; the single-ray kernel is built for 8, 10 and
  * 12, trading registers for occupancy). Results do not depend on it. */
 int32_t cvx_scene_set_query_launch(cvx_scene* scene, uint32_t blocks_per_sm);
 void cvx_scene_destroy(cvx_scene* scene);

@@ -58,6 +58,22 @@ def test_intersect_bitexact(icosphere, orc, traversal):
     assert (tri >= 0).mean() > 0.5
 
 
+@pytest.mark.parametrize("launch", [8, 10, 12])
+def test_intersect_single_launch_shapes_bitexact(icosphere, orc, launch):
+    """Every launch shape of the single-ray query (occupancy variants of the
+    staged ray supply) returns the oracle's results, ragged tail included."""
+    bvh, scene, osc = icosphere
+    o, d = scenes.random_rays((1 << 17) + 45, seed=19)
+    ot, otri = osc.intersect(o, d, mode=1)
+    scene.set_query_launch(launch)
+    try:
+        t, tri = scene.intersect_nearest(o, d, traversal=1)
+    finally:
+        scene.set_query_launch(0)
+    assert (tri == otri).all(), np.nonzero(tri != otri)[0][:10]
+    assert (t.view(np.uint32) == ot.view(np.uint32)).all()
+
+
 @pytest.mark.parametrize("traversal", [0, 1])
 def test_intersect_counters_match_reference_debug_counts(icosphere, orc, traversal):
     """Box and triangle counts per packet (bvh.rs:604-651, the debug view) or per ray."""
