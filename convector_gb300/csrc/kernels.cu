@@ -131,14 +131,6 @@ struct SoaRays {
 // at a time and copies them into shared memory with cp.async, one batch ahead
 // of use. A lane that finishes a ray takes the next one from shared memory, so
 // neither the claim's atomic nor the ray's DRAM load stalls the warp.
-__device__ __forceinline__ void cp_async4(void* smem, const void* gmem) {
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"((uint32_t)__cvta_generic_to_shared(smem)),
-                 "l"(__cvta_generic_to_global(gmem)));
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;"); }
-__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
-__device__ __forceinline__ void cp_async_wait_one_pending() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
-
 struct StagedSoaClaim {
     const SoaRays& src;
     uint32_t* next_ray;

@@ -147,6 +147,15 @@ __device__ __forceinline__ uint32_t node_ref(uint32_t node_id, uint32_t index, u
     return len < 31u ? (index << 5) | len : (node_id << 5) | 31u;
 }
 
+// Asynchronous global-to-shared copies (cp.async) for staging rays.
+__device__ __forceinline__ void cp_async4(void* smem, const void* gmem) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"((uint32_t)__cvta_generic_to_shared(smem)),
+                 "l"(__cvta_generic_to_global(gmem)));
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_one_pending() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
+
 // Ray supply of the refill traversal. claim() is called by the whole warp in
 // an iteration in which the lanes of `b` want a ray; for a wanting lane it
 // returns kClaimRay with the ray's data, kClaimDone when the rays are used up,

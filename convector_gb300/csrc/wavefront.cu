@@ -151,33 +151,12 @@ __global__ void __launch_bounds__(128) k_wf_traverse_octet(const Job* __restrict
 }
 
 // Single-ray traversal over the lanes of the queued groups, with ray refill
-// (traverse_refill): ray r is lane r % 8 of queue entry r / 8.
-struct QueueRays {
-    const Job* jobs;
-    const DeviceScene* scenes;
+// (traverse_refill): ray r is lane r % 8 of queue entry r / 8. The claim
+// hands the traversal the lane slot l = group * 8 + k as the ray's index, so
+// its result is stored without reading the queue again.
+struct QueueStore {
     WaveState st;
-    const uint32_t* queue;
-    __device__ __forceinline__ bool load(uint32_t r, F3& o, F3& d, float& far, const float4*& nodes,
-                                         const float4*& geom) const {
-        uint32_t gi = queue[r >> 3];
-        size_t l = (size_t)gi * 8 + (r & 7u);
-        if (!(st.flags[l] & 1u)) {
-            st.ht[l] = 1.0e5f;
-            st.hu[l] = 0.0f;
-            st.hv[l] = 0.0f;
-            st.htri[l] = -1;
-            return false;
-        }
-        const DeviceScene* s = scenes + jobs[st.group_job[gi]].scene;
-        nodes = s->nodes;
-        geom = s->geom;
-        o = f3(st.ox[l], st.oy[l], st.oz[l]);
-        d = f3(st.dx[l], st.dy[l], st.dz[l]);
-        far = 1.0e5f;
-        return true;
-    }
-    __device__ __forceinline__ void store(uint32_t r, const Hit& h, uint32_t, uint32_t) const {
-        size_t l = (size_t)queue[r >> 3] * 8 + (r & 7u);
+    __device__ __forceinline__ void store(uint32_t l, const Hit& h, uint32_t, uint32_t) const {
         st.ht[l] = h.t;
         st.hu[l] = h.u;
         st.hv[l] = h.v;
@@ -185,13 +164,47 @@ struct QueueRays {
     }
 };
 
+struct QueueClaim {
+    const Job* jobs;
+    const DeviceScene* scenes;
+    WaveState st;
+    const uint32_t* queue;
+    uint32_t n;
+    uint32_t* next_ray;
+    __device__ __forceinline__ int claim(unsigned b, bool want, int lane, uint32_t& r_out, RayIn& in) {
+        uint32_t base = 0;
+        int first = __ffs(b) - 1;
+        if (lane == first) base = atomicAdd(next_ray, (uint32_t)__popc(b));
+        base = __shfl_sync(0xffffffffu, base, first);
+        if (!want) return kClaimNone;
+        uint32_t r = base + __popc(b & ((1u << lane) - 1u));
+        if (r >= n) return kClaimDone;
+        uint32_t gi = queue[r >> 3];
+        uint32_t l = gi * 8u + (r & 7u);
+        if (!(st.flags[l] & 1u)) {  // inactive lane: its result is the miss
+            st.ht[l] = 1.0e5f;
+            st.hu[l] = 0.0f;
+            st.hv[l] = 0.0f;
+            st.htri[l] = -1;
+            return kClaimNone;
+        }
+        const DeviceScene* s = scenes + jobs[st.group_job[gi]].scene;
+        in.nodes = s->nodes;
+        in.geom = s->geom;
+        in.o = f3(st.ox[l], st.oy[l], st.oz[l]);
+        in.d = f3(st.dx[l], st.dy[l], st.dz[l]);
+        in.far = 1.0e5f;
+        r_out = l;
+        return kClaimRay;
+    }
+};
+
 __global__ void __launch_bounds__(128) k_wf_traverse_single(const Job* __restrict__ jobs,
                                                             const DeviceScene* __restrict__ scenes, WaveState st,
                                                             int bounce, WaveOutputs out) {
-    QueueRays src{jobs, scenes, st, st.queue[bounce & 1]};
-    EachClaim<QueueRays> claim{src, st.counts[bounce] * 8u, &st.counts[6 + bounce]};
-    if (!traverse_refill(src, claim, g_tables_wf))
-        atomicOr(out.err, kErrStackOverflow);
+    QueueStore store{st};
+    QueueClaim claim{jobs, scenes, st, st.queue[bounce & 1], st.counts[bounce] * 8u, &st.counts[6 + bounce]};
+    if (!traverse_refill(store, claim, g_tables_wf)) atomicOr(out.err, kErrStackOverflow);
 }
 
 __device__ __forceinline__ void finalize(const Job& j, uint32_t gi, int k, F3 color, F3 d, bool hit_em,
