@@ -199,8 +199,11 @@ struct EachClaim {
 // pushed, and culled entries are popped within the same iteration.
 // The whole warp must call this. `src` provides
 //   void store(r, const Hit&, uint32_t boxes, uint32_t triangles)
+// (box and triangle counts when COUNT, else 0). LEAF_AFTER_PAIR: a lane whose
+// pair test leads to a leaf tests that leaf in the same iteration (fewer
+// iterations for deep trees; the order of decisions is the same either way).
 // Returns false if a ray overflowed the stack (its hit is then incomplete).
-template <class Src, class Claim>
+template <bool COUNT, bool LEAF_AFTER_PAIR, class Src, class Claim>
 __device__ __forceinline__ bool traverse_refill(const Src& src, Claim& claim, const ApproxTables& tab) {
     const int lane = threadIdx.x & 31;
     const float4* nodes = nullptr;
@@ -263,44 +266,63 @@ __device__ __forceinline__ bool traverse_refill(const Src& src, Claim& claim, co
             }
         }
         uint32_t len = cur & 31u, idx = cur >> 5;
-        if (len == 31u) {  // escaped leaf: read its (index, len) from the node pair
-            uint32_t id = idx;
-            float4 q3 = __ldg(nodes + 4 * (id >> 1) + 3);
-            idx = __float_as_uint((id & 1u) ? q3.z : q3.x);
-            len = __float_as_uint((id & 1u) ? q3.w : q3.y);
-        }
-        if (len != 0u) {
+        if (!LEAF_AFTER_PAIR && len != 0u) {  // a popped leaf; the pair loop continues next iteration
+            if (len == 31u) {  // escaped leaf: read its (index, len) from the node pair
+                uint32_t id = idx;
+                float4 q3 = __ldg(nodes + 4 * (id >> 1) + 3);
+                idx = __float_as_uint((id & 1u) ? q3.z : q3.x);
+                len = __float_as_uint((id & 1u) ? q3.w : q3.y);
+            }
             for (uint32_t i = idx; i < idx + len; i++) tri_test(geom, i, o, d, true, h);
-            nt += len;
+            if (COUNT) nt += len;
             cur = kNone;
             continue;
         }
-        if (cur != 0u) na += 2;  // every pair but the root pair (bvh.rs:604-634)
-        const float4* np = nodes + 4 * (idx >> 1);
-        float4 q0 = __ldg(np), q1 = __ldg(np + 1), q2 = __ldg(np + 2), q3 = __ldg(np + 3);
-        BoxT b0 = box_test(q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, o, inv);
-        BoxT b1 = box_test(q1.z, q1.w, q2.x, q2.y, q2.z, q2.w, o, inv);
-        bool first0 = !sneg(b0.tmin - b1.tmin);
-        bool hit0 = b0.mask & !sneg(b0.tmax);
-        bool hit1 = b1.mask & !sneg(b1.tmax);
-        uint32_t r0 = node_ref(idx, __float_as_uint(q3.x), __float_as_uint(q3.y));
-        uint32_t r1 = node_ref(idx + 1u, __float_as_uint(q3.z), __float_as_uint(q3.w));
-        // The reference pushes `first` then `second` and pops `second` first.
-        bool hit_first = first0 ? hit0 : hit1, hit_second = first0 ? hit1 : hit0;
-        uint32_t ref_first = first0 ? r0 : r1, ref_second = first0 ? r1 : r0;
-        float t_first = first0 ? b0.tmin : b1.tmin, t_second = first0 ? b1.tmin : b0.tmin;
-        if (sp + (int)hit_first + (int)hit_second > kStackDepth) {
-            overflow = true;
-            sp = 0;
+        if (len == 0u) {
+            // An internal node: test its two children.
+            if (COUNT && cur != 0u) na += 2;  // every pair but the root pair (bvh.rs:604-634)
+            const float4* np = nodes + 4 * (idx >> 1);
+            float4 q0 = __ldg(np), q1 = __ldg(np + 1), q2 = __ldg(np + 2), q3 = __ldg(np + 3);
+            BoxT b0 = box_test(q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, o, inv);
+            BoxT b1 = box_test(q1.z, q1.w, q2.x, q2.y, q2.z, q2.w, o, inv);
+            bool first0 = !sneg(b0.tmin - b1.tmin);
+            bool hit0 = b0.mask & !sneg(b0.tmax);
+            bool hit1 = b1.mask & !sneg(b1.tmax);
+            uint32_t r0 = node_ref(idx, __float_as_uint(q3.x), __float_as_uint(q3.y));
+            uint32_t r1 = node_ref(idx + 1u, __float_as_uint(q3.z), __float_as_uint(q3.w));
+            // The reference pushes `first` then `second` and pops `second` first.
+            bool hit_first = first0 ? hit0 : hit1, hit_second = first0 ? hit1 : hit0;
+            uint32_t ref_first = first0 ? r0 : r1, ref_second = first0 ? r1 : r0;
+            float t_first = first0 ? b0.tmin : b1.tmin, t_second = first0 ? b1.tmin : b0.tmin;
+            if (sp + (int)hit_first + (int)hit_second > kStackDepth) {
+                overflow = true;
+                sp = 0;
+                cur = kNone;
+                continue;
+            }
+            if (hit_first) {
+                if (sp > 0) stack[sp - 1] = top;
+                top = make_uint2(ref_first, __float_as_uint(t_first));
+                sp++;
+            }
+            cur = (hit_second && !geq(t_second, h.t)) ? ref_second : kNone;
+            if (!LEAF_AFTER_PAIR || cur == kNone) continue;
+            len = cur & 31u;
+            idx = cur >> 5;
+        }
+        // LEAF_AFTER_PAIR: a leaf, popped or reached from the pair just tested
+        // (the reference would pop it next with no decision in between).
+        if (len != 0u) {
+            if (len == 31u) {  // escaped leaf: read its (index, len) from the node pair
+                uint32_t id = idx;
+                float4 q3 = __ldg(nodes + 4 * (id >> 1) + 3);
+                idx = __float_as_uint((id & 1u) ? q3.z : q3.x);
+                len = __float_as_uint((id & 1u) ? q3.w : q3.y);
+            }
+            for (uint32_t i = idx; i < idx + len; i++) tri_test(geom, i, o, d, true, h);
+            if (COUNT) nt += len;
             cur = kNone;
-            continue;
         }
-        if (hit_first) {
-            if (sp > 0) stack[sp - 1] = top;
-            top = make_uint2(ref_first, __float_as_uint(t_first));
-            sp++;
-        }
-        cur = (hit_second && !geq(t_second, h.t)) ? ref_second : kNone;
     }
     return !overflow;
 }
