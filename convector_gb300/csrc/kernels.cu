@@ -207,7 +207,7 @@ __global__ void __launch_bounds__(128, MINB) k_intersect_refill(SoaRays src, uin
     __shared__ float stage[4][2][6][32];
     StagedSoaClaim claim{src, next_ray, stage[threadIdx.x >> 5], 0u, 0u, 0u, 0};
     claim.init(threadIdx.x & 31);
-    bool ok = traverse_refill<COUNT, false>(src, claim, g_tables);
+    bool ok = traverse_refill<COUNT, false, 16>(src, claim, g_tables);
     if (!ok) atomicOr(err, kErrStackOverflow);
 }
 

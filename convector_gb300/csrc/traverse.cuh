@@ -202,8 +202,10 @@ struct EachClaim {
 // (box and triangle counts when COUNT, else 0). LEAF_AFTER_PAIR: a lane whose
 // pair test leads to a leaf tests that leaf in the same iteration (fewer
 // iterations for deep trees; the order of decisions is the same either way).
+// CLAIM_MIN: lanes without a ray wait until that many want one; results do
+// not depend on it (each ray's traversal is independent of when it starts).
 // Returns false if a ray overflowed the stack (its hit is then incomplete).
-template <bool COUNT, bool LEAF_AFTER_PAIR, class Src, class Claim>
+template <bool COUNT, bool LEAF_AFTER_PAIR, int CLAIM_MIN, class Src, class Claim>
 __device__ __forceinline__ bool traverse_refill(const Src& src, Claim& claim, const ApproxTables& tab) {
     const int lane = threadIdx.x & 31;
     const float4* nodes = nullptr;
@@ -224,6 +226,11 @@ __device__ __forceinline__ bool traverse_refill(const Src& src, Claim& claim, co
     for (;;) {
         bool want = !have && !done;
         unsigned b = __ballot_sync(0xffffffffu, want);
+        // Claim only when CLAIM_MIN lanes want a ray (or none has work): the
+        // claim path then runs with many lanes at once instead of with one or
+        // two lanes in nearly every iteration.
+        if (CLAIM_MIN > 1 && b && __popc(b) < CLAIM_MIN && __any_sync(0xffffffffu, have)) b = 0u;
+        want = want && b;
         if (b) {
             uint32_t r = 0;
             RayIn in;

@@ -204,7 +204,7 @@ __global__ void __launch_bounds__(128) k_wf_traverse_single(const Job* __restric
                                                             int bounce, WaveOutputs out) {
     QueueStore store{st};
     QueueClaim claim{jobs, scenes, st, st.queue[bounce & 1], st.counts[bounce] * 8u, &st.counts[6 + bounce]};
-    if (!traverse_refill<false, true>(store, claim, g_tables_wf)) atomicOr(out.err, kErrStackOverflow);
+    if (!traverse_refill<false, true, 8>(store, claim, g_tables_wf)) atomicOr(out.err, kErrStackOverflow);
 }
 
 __device__ __forceinline__ void finalize(const Job& j, uint32_t gi, int k, F3 color, F3 d, bool hit_em,
