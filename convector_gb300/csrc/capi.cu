@@ -87,6 +87,10 @@ struct cvx_scene {
     int32_t* d_tri = nullptr;
     size_t scratch_n = 0;
     cudaStream_t stream = nullptr;
+    // the host-buffer query's copy/compute pipeline: streams and per-chunk
+    // (status, ray counter) words
+    cudaStream_t qstreams[3] = {nullptr, nullptr, nullptr};
+    uint32_t* d_qerr = nullptr;
 
     DeviceScene view() const {
         DeviceScene s;
@@ -109,6 +113,9 @@ struct cvx_scene {
         cudaFree(d_rays);
         cudaFree(d_t);
         cudaFree(d_tri);
+        cudaFree(d_qerr);
+        for (cudaStream_t q : qstreams)
+            if (q) cudaStreamDestroy(q);
         if (stream) cudaStreamDestroy(stream);
     }
 };
@@ -299,20 +306,41 @@ int32_t cvx_intersect_nearest(cvx_scene* s, const float* ox, const float* oy, co
         if ((st = dalloc(&s->d_tri, n, "hit buffer"))) return st;
         s->scratch_n = n;
     }
+    // Copy/compute pipeline: the rays are cut into chunks that go round-robin
+    // to three streams, so the copies of one chunk overlap the traversal of
+    // another (and a chunk's kernel starts on SMs the previous one has left).
+    // Up to four chunks of at least 2^19 rays (measured on 4M rays: 4 chunks
+    // beat 8 and 16, whose shorter launches and copies cost more than they overlap).
+    constexpr uint32_t kMaxChunks = 4, kMinChunk = 1u << 19;
+    if (!s->d_qerr && (st = dalloc(&s->d_qerr, 2 * kMaxChunks, "status"))) return st;
+    for (cudaStream_t& q : s->qstreams)
+        if (!q) CK(cudaStreamCreateWithFlags(&q, cudaStreamNonBlocking), "cudaStreamCreate");
+    uint32_t chunks = n / kMinChunk;
+    chunks = chunks < 1 ? 1 : (chunks > kMaxChunks ? kMaxChunks : chunks);
+    uint32_t per = (n + chunks - 1) / chunks;
+    per = (per + 31u) & ~31u;
     const float* src[6] = {ox, oy, oz, dx, dy, dz};
-    for (int k = 0; k < 6; k++)
-        CK(cudaMemcpyAsync(s->d_rays + (size_t)k * n, src[k], (size_t)n * 4, cudaMemcpyHostToDevice, s->stream),
-           "copy rays");
-    CK(cudaMemsetAsync(s->d_err, 0, 4, s->stream), "reset status");
-    CK(launch_intersect(s->view(), s->d_rays, n, far_dist, traversal == CVX_TRAVERSE_PACKET, s->d_t, s->d_tri,
-                        nullptr, s->d_err, 0, s->blocks_per_sm, s->stream),
-       "intersect launch");
-    CK(cudaMemcpyAsync(t_out, s->d_t, (size_t)n * 4, cudaMemcpyDeviceToHost, s->stream), "copy distances");
-    CK(cudaMemcpyAsync(tri_out, s->d_tri, (size_t)n * 4, cudaMemcpyDeviceToHost, s->stream), "copy indices");
-    uint32_t err = 0;
-    CK(cudaMemcpyAsync(&err, s->d_err, 4, cudaMemcpyDeviceToHost, s->stream), "copy status");
-    CK(cudaStreamSynchronize(s->stream), "intersect");
-    if (err) return set_error(CVX_ERR_DEVICE, "traversal stack overflow reported by the kernel");
+    uint32_t c = 0;
+    for (uint32_t off = 0; off < n; off += per, c++) {
+        uint32_t len = n - off < per ? n - off : per;
+        cudaStream_t q = s->qstreams[c % 3];
+        float* rays = s->d_rays + (size_t)6 * off;
+        for (int k = 0; k < 6; k++)
+            CK(cudaMemcpyAsync(rays + (size_t)k * len, src[k] + off, (size_t)len * 4, cudaMemcpyHostToDevice, q),
+               "copy rays");
+        CK(cudaMemsetAsync(s->d_qerr + 2 * c, 0, 8, q), "reset status");
+        CK(launch_intersect(s->view(), rays, len, far_dist, traversal == CVX_TRAVERSE_PACKET, s->d_t + off,
+                            s->d_tri + off, nullptr, s->d_qerr + 2 * c, 0, s->blocks_per_sm, q),
+           "intersect launch");
+        CK(cudaMemcpyAsync(t_out + off, s->d_t + off, (size_t)len * 4, cudaMemcpyDeviceToHost, q), "copy distances");
+        CK(cudaMemcpyAsync(tri_out + off, s->d_tri + off, (size_t)len * 4, cudaMemcpyDeviceToHost, q),
+           "copy indices");
+    }
+    for (cudaStream_t q : s->qstreams) CK(cudaStreamSynchronize(q), "intersect");
+    uint32_t err[2 * kMaxChunks] = {};
+    CK(cudaMemcpy(err, s->d_qerr, 8 * c, cudaMemcpyDeviceToHost), "copy status");
+    for (uint32_t k = 0; k < c; k++)
+        if (err[2 * k]) return set_error(CVX_ERR_DEVICE, "traversal stack overflow reported by the kernel");
     return CVX_OK;
 }
 

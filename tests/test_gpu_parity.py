@@ -75,6 +75,24 @@ def test_intersect_single_launch_shapes_bitexact(icosphere, orc, launch):
 
 
 @pytest.mark.parametrize("traversal", [0, 1])
+def test_intersect_host_pipeline_equals_device_query(icosphere, traversal):
+    """The host-buffer query cuts large batches into chunks on several
+    streams; its results equal the one-launch device query, ragged end included."""
+    import torch
+    bvh, scene, _ = icosphere
+    n = (1 << 21) + 77
+    o, d = scenes.random_rays(n, seed=23)
+    t, tri = scene.intersect_nearest(o, d, traversal=traversal)
+    rays = torch.from_numpy(np.concatenate([o.T, d.T]).copy()).cuda()
+    td = torch.empty(n, dtype=torch.float32, device="cuda")
+    trd = torch.empty(n, dtype=torch.int32, device="cuda")
+    scene.intersect_nearest_device(rays, td, trd, traversal=traversal)
+    torch.cuda.synchronize()
+    assert (tri == trd.cpu().numpy()).all()
+    assert (t.view(np.uint32) == td.cpu().numpy().view(np.uint32)).all()
+
+
+@pytest.mark.parametrize("traversal", [0, 1])
 def test_intersect_counters_match_reference_debug_counts(icosphere, orc, traversal):
     """Box and triangle counts per packet (bvh.rs:604-651, the debug view) or per ray."""
     import torch
