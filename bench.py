@@ -475,9 +475,11 @@ def bench_batched(cg):
             "speedup_wall": wall_p / wall_b}
 
 
-def _served_run(cg, scs, reqs, sequential):
+def _served_run(cg, scs, reqs, sequential, engine=None):
+    engine = engine or {}
     srv = cg.Server(scs, framebuffer_bytes=24 << 30, max_groups=1 << 21, traversal=cg.TRAVERSE_SINGLE,
-                    sequential=sequential)
+                    sequential=sequential, blocks_per_sm=engine.get("blocks_per_sm", 0),
+                    refill_mode=engine.get("refill_mode", cg.REFILL_AFTER_CAMERA))
     # warm-up: one small request per scene
     for k in range(len(scs)):
         srv.wait(srv.submit(k, 64, 64, 1, reqs[0][5]))
@@ -565,13 +567,25 @@ def bench_served(cg, duration=2.0, rate=200.0, seed=4):
         w = int(round(np.exp(rng.uniform(np.log(320), np.log(1920)))))
         h = int(min(1080, max(184, round(w * 184 / 320))))
         reqs.append((t, int(rng.integers(0, 3)), w, h, int(rng.integers(1, 17)), cam))
-    served = _served_run(cg, scs, reqs, sequential=False)
+    # The server's wavefront engine takes the autotuner's configuration for
+    # the scene it runs in wavefront form (the tube: deeper than 40 levels).
+    from convector_gb300 import autotune
+    wf = [k for k, b in enumerate(bvhs) if b.depth > 40 or b.triangles.shape[0] > 200000]
+    engine = {}
+    if wf:
+        scenes.default_camera(scs[wf[0]].camera)
+        best, _ = autotune.tune_wavefront(scs[wf[0]], 1280, 736, frames=3)
+        engine = {"blocks_per_sm": best["blocks_per_sm"], "refill_mode": best["refill_mode"]}
+    served = _served_run(cg, scs, reqs, sequential=False, engine=engine)
+    served_default = _served_run(cg, scs, reqs, sequential=False)
     sequential = _served_run(cg, scs, reqs, sequential=True)
     plain = _plain_renderer_run(cg, scs, bvhs, reqs)
-    return {"rate_per_s": rate, "duration_s": duration, "served": served, "plain_renderer": plain,
+    return {"rate_per_s": rate, "duration_s": duration, "served": served, "served_engine": engine,
+            "served_default_engine": served_default, "plain_renderer": plain,
             "server_one_at_a_time": sequential,
             "throughput_ratio": served["mrays_per_s"] / plain["mrays_per_s"],
-            "throughput_ratio_vs_server_one_at_a_time": served["mrays_per_s"] / sequential["mrays_per_s"]}
+            "throughput_ratio_default_engine": served_default["mrays_per_s"] / plain["mrays_per_s"],
+            "throughput_ratio_vs_server_one_at_a_time": served_default["mrays_per_s"] / sequential["mrays_per_s"]}
 
 
 def bench_bvh_build(cg):

@@ -89,6 +89,22 @@ def tune(scene, width, height, rng_order=RNG_GROUP, allow_packet=True, frames=5,
     return best, table
 
 
+def tune_wavefront(scene, width, height, frames=5):
+    """The fastest single-ray wavefront configuration (blocks per SM, refill
+    mode) for this scene: what a batch or server engine running the scene in
+    wavefront mode should use. Returns (config dict, {config key: ms})."""
+    table = {}
+    best, best_ms = None, None
+    for cfg in candidates(RNG_GROUP, allow_packet=False):
+        if cfg["mode"] != MODE_WAVEFRONT:
+            continue
+        ms = measure(scene, width, height, cfg, frames=frames)
+        table[json.dumps(cfg, sort_keys=True)] = ms
+        if best_ms is None or ms < best_ms:
+            best, best_ms = cfg, ms
+    return best, table
+
+
 def autotuned_renderer(scene, width, height, rng_order=RNG_GROUP, allow_packet=True):
     best, _ = tune(scene, width, height, rng_order=rng_order, allow_packet=allow_packet)
     return Renderer(scene, width, height, **best)
