@@ -479,7 +479,8 @@ def _served_run(cg, scs, reqs, sequential, engine=None):
     engine = engine or {}
     srv = cg.Server(scs, framebuffer_bytes=24 << 30, max_groups=1 << 21, traversal=cg.TRAVERSE_SINGLE,
                     sequential=sequential, blocks_per_sm=engine.get("blocks_per_sm", 0),
-                    refill_mode=engine.get("refill_mode", cg.REFILL_AFTER_CAMERA))
+                    refill_mode=engine.get("refill_mode", cg.REFILL_AFTER_CAMERA),
+                    fused_blocks_per_sm=engine.get("fused_blocks_per_sm", 0))
     # warm-up: one small request per scene
     for k in range(len(scs)):
         srv.wait(srv.submit(k, 64, 64, 1, reqs[0][5]))
@@ -498,7 +499,8 @@ def _served_run(cg, scs, reqs, sequential, engine=None):
     srv.close()
     return {"requests": len(res), "latency_ms_p50": float(np.percentile(lat, 50)),
             "latency_ms_p99": float(np.percentile(lat, 99)), "mrays_per_s": rays / span / 1e6, "span_s": span,
-            "waves": st["waves"], "device_busy_s": st["busy_s"]}
+            "waves": st["waves"], "device_busy_s": st["busy_s"], "fused_busy_s": st["fused_busy_s"],
+            "wavefront_busy_s": st["wavefront_busy_s"]}
 
 
 def _plain_renderer_run(cg, scs, bvhs, reqs):

@@ -57,7 +57,7 @@ class _ServerConfig(ctypes.Structure):
     _fields_ = [("framebuffer_bytes", ctypes.c_uint64), ("max_groups", ctypes.c_uint32),
                 ("traversal", ctypes.c_uint32), ("use_graph", ctypes.c_uint32), ("sequential", ctypes.c_uint32),
                 ("blocks_per_sm", ctypes.c_uint32), ("refill_mode", ctypes.c_uint32),
-                ("kernel_mode", ctypes.c_uint32)]
+                ("kernel_mode", ctypes.c_uint32), ("fused_blocks_per_sm", ctypes.c_uint32)]
 
 
 class _Request(ctypes.Structure):
@@ -135,6 +135,7 @@ def lib(build=False):
         "cvx_server_wait": (I32, [P, ctypes.c_uint64, U32, P]),
         "cvx_server_cancel": (I32, [P, ctypes.c_uint64]),
         "cvx_server_stats": (I32, [P, P, P, P, P]),
+        "cvx_server_engine_stats": (I32, [P, P, P]),
         "cvx_server_destroy": (None, [P]),
         "cvx_renderer_set_debug_view": (I32, [P, U32]),
         "cvx_display_create": (I32, [U32, U32, P, P, U32, U32, P]),
@@ -521,11 +522,12 @@ class Server:
     """Continuously batched request server over resident scenes."""
 
     def __init__(self, scenes, framebuffer_bytes=4 << 30, max_groups=1 << 21, traversal=TRAVERSE_SINGLE,
-                 use_graph=1, sequential=False, blocks_per_sm=0, refill_mode=REFILL_AFTER_CAMERA, kernel_mode=0):
+                 use_graph=1, sequential=False, blocks_per_sm=0, refill_mode=REFILL_AFTER_CAMERA, kernel_mode=0,
+                 fused_blocks_per_sm=0):
         self.scenes = list(scenes)
         arr = (ctypes.c_void_p * len(self.scenes))(*[s._h.value for s in self.scenes])
         cfg = _ServerConfig(framebuffer_bytes, max_groups, traversal, use_graph, int(sequential), blocks_per_sm,
-                            refill_mode, kernel_mode)
+                            refill_mode, kernel_mode, fused_blocks_per_sm)
         out = ctypes.c_void_p()
         _check(lib().cvx_server_create(arr, len(self.scenes), ctypes.byref(cfg), ctypes.byref(out)))
         self._h = out
@@ -556,7 +558,10 @@ class Server:
         now, waves, rays, busy = ctypes.c_double(), ctypes.c_uint64(), ctypes.c_uint64(), ctypes.c_double()
         _check(lib().cvx_server_stats(self._h, ctypes.byref(now), ctypes.byref(waves), ctypes.byref(rays),
                                       ctypes.byref(busy)))
-        return {"now_s": now.value, "waves": waves.value, "rays": rays.value, "busy_s": busy.value}
+        f, w = ctypes.c_double(), ctypes.c_double()
+        _check(lib().cvx_server_engine_stats(self._h, ctypes.byref(f), ctypes.byref(w)))
+        return {"now_s": now.value, "waves": waves.value, "rays": rays.value, "busy_s": busy.value,
+                "fused_busy_s": f.value, "wavefront_busy_s": w.value}
 
     def close(self):
         if getattr(self, "_h", None) and self._h.value and _LIB is not None:

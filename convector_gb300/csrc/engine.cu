@@ -461,6 +461,7 @@ struct cvx_server {
     Clock::time_point t0 = Clock::now();
     std::atomic<uint64_t> waves{0}, rays{0};
     double busy_s = 0.0;
+    double busy_fused_s = 0.0, busy_wavefront_s = 0.0;  // per engine (the two overlap)
     int32_t fatal = CVX_OK;
     std::string fatal_msg;
 
@@ -557,6 +558,8 @@ struct cvx_server {
                 waves++;
                 rays += r;
                 busy_s += ms * 1e-3;
+                busy_fused_s += ms0 * 1e-3;
+                busy_wavefront_s += ms1 * 1e-3;
                 for (size_t i = 0; i < wave.size(); i++) {
                     auto& q = wave[i];
                     if (st) {
@@ -626,13 +629,18 @@ extern "C" int32_t cvx_server_create(cvx_scene* const* scenes, uint32_t n_scenes
     std::unique_ptr<cvx_server> s(new cvx_server());
     s->scenes.assign(scenes, scenes + n_scenes);
     s->cfg = *cfg;
-    ECK(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking), "cudaStreamCreate");
-    ECK(cudaStreamCreateWithFlags(&s->stream2, cudaStreamNonBlocking), "cudaStreamCreate");
+    // The wavefront waves (deep scenes) are the longer part of a wave: their
+    // stream gets the highest priority, so that their bounce kernels take SMs
+    // ahead of the single-launch waves running beside them.
+    int least = 0, greatest = 0;
+    ECK(cudaDeviceGetStreamPriorityRange(&least, &greatest), "stream priorities");
+    ECK(cudaStreamCreateWithPriority(&s->stream, cudaStreamNonBlocking, greatest), "cudaStreamCreate");
+    ECK(cudaStreamCreateWithPriority(&s->stream2, cudaStreamNonBlocking, least), "cudaStreamCreate");
     int32_t st = s->engine.init(cfg->max_groups, 1024, cfg->traversal == CVX_TRAVERSE_PACKET, cfg->use_graph != 0,
                                 cfg->blocks_per_sm, refill_from(cfg->refill_mode));
     if (st) return st;
-    if ((st = s->fused.init(0xffffffffu, 1024, cfg->traversal == CVX_TRAVERSE_PACKET, cfg->use_graph != 0, 0, 1,
-                            true)))
+    if ((st = s->fused.init(0xffffffffu, 1024, cfg->traversal == CVX_TRAVERSE_PACKET, cfg->use_graph != 0,
+                            cfg->fused_blocks_per_sm, 1, true)))
         return st;
     if ((st = s->engine.set_scenes(scenes, n_scenes))) return st;
     if ((st = s->fused.set_scenes(scenes, n_scenes))) return st;
@@ -711,6 +719,14 @@ extern "C" int32_t cvx_server_stats(cvx_server* s, double* now_s, uint64_t* wave
     if (waves) *waves = s->waves;
     if (rays) *rays = s->rays;
     if (busy_s) *busy_s = s->busy_s;
+    return CVX_OK;
+}
+
+extern "C" int32_t cvx_server_engine_stats(cvx_server* s, double* fused_busy_s, double* wavefront_busy_s) {
+    if (!s) return set_error(CVX_ERR_INVALID, "null server");
+    std::lock_guard<std::mutex> lk(s->mu);
+    if (fused_busy_s) *fused_busy_s = s->busy_fused_s;
+    if (wavefront_busy_s) *wavefront_busy_s = s->busy_wavefront_s;
     return CVX_OK;
 }
 

@@ -199,7 +199,9 @@ struct QueueClaim {
     }
 };
 
-__global__ void __launch_bounds__(128) k_wf_traverse_single(const Job* __restrict__ jobs,
+// 10 resident blocks per SM (48 registers): measured on the 870k-triangle
+// tube, 4.17 ms per sample against 4.56 (56 registers, 9 blocks), 4.69 (12) and 5.46 (16).
+__global__ void __launch_bounds__(128, 10) k_wf_traverse_single(const Job* __restrict__ jobs,
                                                             const DeviceScene* __restrict__ scenes, WaveState st,
                                                             int bounce, WaveOutputs out) {
     QueueStore store{st};

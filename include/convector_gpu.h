@@ -268,6 +268,7 @@ typedef struct cvx_server_config {
     uint32_t blocks_per_sm;     /* persistent blocks per SM (0: 12) */
     uint32_t refill_mode;       /* CVX_REFILL_* */
     uint32_t kernel_mode;       /* 0: per scene as CVX_MODE_AUTO; 1: all fused; 2: all wavefront */
+    uint32_t fused_blocks_per_sm; /* blocks per SM of the single-launch waves (0: 16) */
 } cvx_server_config;
 
 typedef struct cvx_request {
@@ -298,6 +299,10 @@ int32_t cvx_server_cancel(cvx_server* s, uint64_t id);
 int32_t cvx_server_set_scene_mode(cvx_server* s, uint32_t scene, uint32_t mode);
 /* The server clock (seconds), waves run, rays traced and device busy time. */
 int32_t cvx_server_stats(cvx_server* s, double* now_s, uint64_t* waves, uint64_t* rays, double* busy_s);
+/* Device time spent so far by each of the server's two engines (single-launch
+ * waves and wavefront waves; they run concurrently, so the sum can exceed
+ * the busy time above). No counterpart in the reference. */
+int32_t cvx_server_engine_stats(cvx_server* s, double* fused_busy_s, double* wavefront_busy_s);
 void cvx_server_destroy(cvx_server* s);
 
 /* ---- device: display post-process ----------------------------------------
