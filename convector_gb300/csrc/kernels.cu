@@ -268,7 +268,7 @@ __device__ __forceinline__ void flush_rays(const FrameArgs& a, uint32_t rays) {
 }
 
 template <bool PACKET>
-__global__ void __launch_bounds__(128) k_render_group(FrameArgs a) {
+__global__ void __launch_bounds__(128, 8) k_render_group(FrameArgs a) {
     __shared__ ApproxTables tab;
     load_tables(tab);
     const int k = threadIdx.x & 7;

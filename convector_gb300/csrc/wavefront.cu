@@ -322,7 +322,9 @@ static int sms() {
 // groups with a grid-stride loop. Same per-group RNG order and outputs as the
 // wavefront kernels.
 template <bool PACKET>
-__global__ void __launch_bounds__(128) k_wave_fused(const Job* __restrict__ jobs, const WaveHeader* __restrict__ hdr,
+// 8 resident blocks per SM (64 registers, small spill): batches of small
+// scenes render 12 % faster than at the compiler's 80 registers (6 blocks).
+__global__ void __launch_bounds__(128, 8) k_wave_fused(const Job* __restrict__ jobs, const WaveHeader* __restrict__ hdr,
                                                     const DeviceScene* __restrict__ scenes, WaveOutputs out) {
     __shared__ ApproxTables tab;
     load_tables_wf(tab);
