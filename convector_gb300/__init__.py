@@ -554,6 +554,11 @@ class Server:
     def cancel(self, rid):
         _check(lib().cvx_server_cancel(self._h, rid))
 
+    def set_scene_mode(self, scene, mode):
+        """Kernel organisation of one scene's waves: MODE_MEGAKERNEL (single
+        launch) or MODE_WAVEFRONT; only while no request is queued or admitted."""
+        _check(lib().cvx_server_set_scene_mode(self._h, scene, mode))
+
     def stats(self):
         now, waves, rays, busy = ctypes.c_double(), ctypes.c_uint64(), ctypes.c_uint64(), ctypes.c_double()
         _check(lib().cvx_server_stats(self._h, ctypes.byref(now), ctypes.byref(waves), ctypes.byref(rays),

@@ -128,6 +128,34 @@ def test_server_mix_equals_alone(two_scenes, gpu, kernel_mode):
         srv.close()
 
 
+def test_server_two_engines_concurrent_equal_alone(two_scenes, gpu):
+    """One scene in single-launch waves and one in wavefront waves, run
+    concurrently on two streams (the wavefront one at higher priority) with a
+    reduced single-launch block count: every image equals the same request
+    rendered alone, and both engines report device time."""
+    scs = [s for _, s, _ in two_scenes]
+    srv = gpu.Server(scs, framebuffer_bytes=64 << 20, max_groups=1 << 14, fused_blocks_per_sm=4,
+                     blocks_per_sm=10, refill_mode=gpu.REFILL_ALL)
+    srv.set_scene_mode(0, gpu.MODE_MEGAKERNEL)
+    srv.set_scene_mode(1, gpu.MODE_WAVEFRONT)
+    rng = np.random.default_rng(8)
+    reqs, ids = [], []
+    for k in range(10):
+        cam = gpu.Camera()
+        scenes.default_camera(cam, eye=(rng.uniform(-1, 1), 1.2, 1.6))
+        reqs.append((k % 2, int(rng.choice([64, 96])), int(rng.choice([40, 64])), int(rng.integers(1, 4)), cam))
+    for i, (sc, w, h, spp, cam) in enumerate(reqs):
+        ids.append(srv.submit(sc, w, h, spp, cam, frame_base=7 * i))
+    for i, rid in enumerate(ids):
+        st, img, _ = srv.wait(rid)
+        sc, w, h, spp, cam = reqs[i]
+        assert st == 0
+        assert (img == _alone(gpu, scs[sc], gpu.View(sc, w, h, spp, 7 * i, cam))).all()
+    stats = srv.stats()
+    assert stats["fused_busy_s"] > 0.0 and stats["wavefront_busy_s"] > 0.0
+    srv.close()
+
+
 def test_server_admission_cancel_timeout(two_scenes, gpu):
     scs = [s for _, s, _ in two_scenes]
     cam = scenes.default_camera(gpu.Camera())
