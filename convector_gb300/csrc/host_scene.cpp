@@ -685,70 +685,118 @@ void tsah_tables(uint32_t n, std::vector<float>& x, std::vector<float>& t, float
 
 // crystallize (bvh.rs:389-428) and the statistics of bvh.rs:536-545 over an
 // interim tree built elsewhere (the device build): node 0 is the root, a
-// leaf's triangles are order[beg .. beg + cnt) in leaf order.
+// leaf's triangles are order[beg .. beg + cnt) in leaf order, and every child
+// has a larger id than its parent. The recursion of crystallize becomes two
+// linear passes: bottom-up (decreasing ids) subtree sizes and the summed area
+// ratio, then top-down (increasing ids) each node's place in the depth-first
+// order. A node's first child goes to 2 + 2 * (internal nodes before it in
+// depth-first order), a leaf's triangles follow those of the leaves before it.
 static float interim_area(const InterimNode& n) {
     Aabb a{S3{n.lo[0], n.lo[1], n.lo[2]}, S3{n.hi[0], n.hi[1], n.hi[2]}};
     return area(a);
 }
-static float interim_summed_area_ratio(const std::vector<InterimNode>& t, uint32_t i) {  // bvh.rs:380-385
-    const InterimNode& n = t[i];
-    if (!n.c0) return 0.0f;
-    float child_contrib = 0.0f;
-    child_contrib += interim_summed_area_ratio(t, n.c0);
-    child_contrib += interim_summed_area_ratio(t, n.c1);
-    float self_area = interim_area(n);
-    float child_sum = 0.0f;
-    child_sum += interim_area(t[n.c0]) / self_area;
-    child_sum += interim_area(t[n.c1]) / self_area;
-    return child_sum + child_contrib;
-}
-static void interim_crystallize(const std::vector<InterimNode>& t, uint32_t i, const std::vector<uint32_t>& order,
-                                const cvx_triangle* src, cvx_bvh& out, size_t into, uint32_t depth, size_t* leaves) {
-    const InterimNode& n = t[i];
-    cvx_bvh_node& nd = out.nodes[into];
-    for (int k = 0; k < 3; k++) {
-        nd.origin[k] = n.lo[k];
-        nd.far_[k] = n.hi[k];
-    }
-    out.depth = std::max(out.depth, depth);
-    if (n.c0) {
-        size_t child = out.nodes.size();
-        out.nodes.push_back(cvx_bvh_node{});
-        out.nodes.push_back(cvx_bvh_node{});
-        interim_crystallize(t, n.c0, order, src, out, child, depth + 1, leaves);
-        interim_crystallize(t, n.c1, order, src, out, child + 1, depth + 1, leaves);
-        out.nodes[into].index = (uint32_t)child;
-        out.nodes[into].len = 0;
-    } else {
-        (*leaves)++;
-        out.nodes[into].index = (uint32_t)out.triangles.size();
-        out.nodes[into].len = n.cnt;
-        for (uint32_t k = 0; k < n.cnt; k++) {
-            uint32_t tri = order[n.beg + k];
-            out.triangles.push_back(src[tri]);
-            out.source_index.push_back(tri);
-        }
-    }
-}
 
 int32_t bvh_from_interim(const std::vector<InterimNode>& t, const std::vector<uint32_t>& order,
                          const cvx_triangle* src, uint32_t n, cvx_bvh** out) {
-    const InterimNode& root = t[0];
-    if (!root.c0)
+    const size_t N = t.size();
+    if (N == 0 || !t[0].c0)
         return set_error(CVX_ERR_INVALID,
                          "the BVH root did not split: the reference needs at least two root nodes (bvh.rs:509-512)");
+    for (size_t v = 0; v < N; v++)
+        if (t[v].c0 && (t[v].c0 <= v || t[v].c1 <= v || t[v].c0 >= N || t[v].c1 >= N))
+            return set_error(CVX_ERR_DEVICE, "device BVH build: malformed interim tree");
+    // Bottom-up: internal nodes and triangles per subtree; summed area ratio
+    // with the operation order of bvh.rs:380-385.
+    std::vector<uint32_t> sint(N), stri(N);
+    std::vector<float> sar(N);
+    for (size_t v = N; v-- > 0;) {
+        const InterimNode& x = t[v];
+        if (!x.c0) {
+            sint[v] = 0;
+            stri[v] = x.cnt;
+            sar[v] = 0.0f;
+            continue;
+        }
+        sint[v] = 1 + sint[x.c0] + sint[x.c1];
+        stri[v] = stri[x.c0] + stri[x.c1];
+        float child_contrib = 0.0f;
+        child_contrib += sar[x.c0];
+        child_contrib += sar[x.c1];
+        float self_area = interim_area(x);
+        float child_sum = 0.0f;
+        child_sum += interim_area(t[x.c0]) / self_area;
+        child_sum += interim_area(t[x.c1]) / self_area;
+        sar[v] = child_sum + child_contrib;
+    }
+    if (stri[0] != n) return set_error(CVX_ERR_DEVICE, "device BVH build lost triangles");
+    // Top-down: crystal index, internal nodes before in depth-first order,
+    // first triangle, depth.
+    std::vector<uint32_t> cidx(N), ipre(N), toff(N), dep(N);
+    const InterimNode& root = t[0];
+    cidx[root.c0] = 0;
+    cidx[root.c1] = 1;
+    ipre[root.c0] = 0;
+    ipre[root.c1] = sint[root.c0];
+    toff[root.c0] = 0;
+    toff[root.c1] = stri[root.c0];
+    dep[root.c0] = dep[root.c1] = 1;
+    for (size_t v = 1; v < N; v++) {
+        const InterimNode& x = t[v];
+        if (!x.c0) continue;
+        uint32_t child = 2 + 2 * ipre[v];
+        cidx[x.c0] = child;
+        cidx[x.c1] = child + 1;
+        ipre[x.c0] = ipre[v] + 1;
+        ipre[x.c1] = ipre[v] + 1 + sint[x.c0];
+        toff[x.c0] = toff[v];
+        toff[x.c1] = toff[v] + stri[x.c0];
+        dep[x.c0] = dep[x.c1] = dep[v] + 1;
+    }
     std::unique_ptr<cvx_bvh> bvh(new cvx_bvh());
-    bvh->nodes.reserve(t.size());
-    bvh->triangles.reserve(n);
-    bvh->source_index.reserve(n);
-    bvh->nodes.push_back(cvx_bvh_node{});
-    bvh->nodes.push_back(cvx_bvh_node{});
+    const size_t M = 2 + 2 * (size_t)(sint[0] - 1);
+    if (M != N - 1) return set_error(CVX_ERR_DEVICE, "device BVH build: unreachable interim nodes");
+    bvh->nodes.assign(M, cvx_bvh_node{});
+    bvh->triangles.resize(n);
+    bvh->source_index.resize(n);
     size_t leaves = 0;
-    interim_crystallize(t, root.c0, order, src, *bvh, 0, 1, &leaves);
-    interim_crystallize(t, root.c1, order, src, *bvh, 1, 1, &leaves);
-    if (bvh->triangles.size() != n) return set_error(CVX_ERR_DEVICE, "device BVH build lost triangles");
-    size_t num_nodes = bvh->nodes.size() + 1;  // the interim nodes: crystallized ones and the root
-    bvh->avg_area_ratio = interim_summed_area_ratio(t, 0) / (float)num_nodes;
+    uint32_t depth = 0;
+    std::vector<uint32_t> leaf_ids;
+    leaf_ids.reserve(N / 2 + 1);
+    for (size_t v = 1; v < N; v++) {
+        const InterimNode& x = t[v];
+        cvx_bvh_node& nd = bvh->nodes[cidx[v]];
+        for (int k = 0; k < 3; k++) {
+            nd.origin[k] = x.lo[k];
+            nd.far_[k] = x.hi[k];
+        }
+        nd.index = x.c0 ? 2 + 2 * ipre[v] : toff[v];
+        nd.len = x.c0 ? 0u : x.cnt;
+        depth = std::max(depth, dep[v]);
+        if (!x.c0) {
+            leaves++;
+            leaf_ids.push_back((uint32_t)v);
+        }
+    }
+    // Triangles in leaf order, gathered on all host threads.
+    unsigned hw = std::thread::hardware_concurrency();
+    size_t nth = std::max<size_t>(1, std::min<size_t>(hw ? hw : 1, (leaf_ids.size() + 4095) / 4096));
+    std::vector<std::thread> pool;
+    for (size_t k = 0; k < nth; k++)
+        pool.emplace_back([&, k] {
+            for (size_t i = k; i < leaf_ids.size(); i += nth) {
+                const InterimNode& x = t[leaf_ids[i]];
+                uint32_t o = toff[leaf_ids[i]];
+                for (uint32_t j = 0; j < x.cnt; j++) {
+                    uint32_t tri = order[x.beg + j];
+                    bvh->triangles[o + j] = src[tri];
+                    bvh->source_index[o + j] = tri;
+                }
+            }
+        });
+    for (auto& th : pool) th.join();
+    bvh->depth = depth;
+    size_t num_nodes = M + 1;  // the interim nodes: crystallized ones and the root
+    bvh->avg_area_ratio = sar[0] / (float)num_nodes;
     bvh->avg_tris_per_leaf = (float)n / (float)leaves;
     *out = bvh.release();
     return CVX_OK;
