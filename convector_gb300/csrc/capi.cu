@@ -102,6 +102,7 @@ struct cvx_scene {
         s.n_tris = n_tris;
         s.n_lights = n_lights;
         s.general_pick = general_pick;
+        s.depth = depth;
         return s;
     }
     ~cvx_scene() {

@@ -199,7 +199,11 @@ struct StagedSoaClaim {
 
 // MINB: resident blocks per SM the register allocation must allow (8: the
 // compiler's choice, 64 registers; 10 and 12 cap registers for occupancy).
-template <int MINB, bool COUNT>
+// CLAIM: lanes without a ray wait until this many want one. Short traversals
+// (shallow trees) gain from large batches of claims, long ones lose more to
+// the waiting: 16 for trees up to 40 levels, 8 beyond (measured on the
+// 82k-triangle icosphere and on the 70-level tube).
+template <int MINB, bool COUNT, int CLAIM>
 __global__ void __launch_bounds__(128, MINB) k_intersect_refill(SoaRays src, uint32_t* __restrict__ next_ray,
                                                                 uint32_t* __restrict__ err) {
     // The reciprocal table is read three times per ray: from global memory
@@ -207,7 +211,7 @@ __global__ void __launch_bounds__(128, MINB) k_intersect_refill(SoaRays src, uin
     __shared__ float stage[4][2][6][32];
     StagedSoaClaim claim{src, next_ray, stage[threadIdx.x >> 5], 0u, 0u, 0u, 0};
     claim.init(threadIdx.x & 31);
-    bool ok = traverse_refill<COUNT, false, 16>(src, claim, g_tables);
+    bool ok = traverse_refill<COUNT, false, CLAIM>(src, claim, g_tables);
     if (!ok) atomicOr(err, kErrStackOverflow);
 }
 
@@ -399,10 +403,17 @@ cudaError_t launch_intersect(const DeviceScene& s, const float* rays, uint32_t n
         uint32_t need = (n + 127u) / 128u;
         if (blocks > need) blocks = need;
         SoaRays src{s.nodes, s.geom, rays, n, far_dist, t_out, tri_out, counters};
-        if (counters) k_intersect_refill<8, true><<<blocks, 128, 0, st>>>(src, err + 1, err);
-        else if (bps >= 12) k_intersect_refill<12, false><<<blocks, 128, 0, st>>>(src, err + 1, err);
-        else if (bps >= 10) k_intersect_refill<10, false><<<blocks, 128, 0, st>>>(src, err + 1, err);
-        else k_intersect_refill<8, false><<<blocks, 128, 0, st>>>(src, err + 1, err);
+        bool deep = s.depth > 40;
+        if (counters) k_intersect_refill<8, true, 16><<<blocks, 128, 0, st>>>(src, err + 1, err);
+        else if (deep) {
+            if (bps >= 12) k_intersect_refill<12, false, 8><<<blocks, 128, 0, st>>>(src, err + 1, err);
+            else if (bps >= 10) k_intersect_refill<10, false, 8><<<blocks, 128, 0, st>>>(src, err + 1, err);
+            else k_intersect_refill<8, false, 8><<<blocks, 128, 0, st>>>(src, err + 1, err);
+        } else {
+            if (bps >= 12) k_intersect_refill<12, false, 16><<<blocks, 128, 0, st>>>(src, err + 1, err);
+            else if (bps >= 10) k_intersect_refill<10, false, 16><<<blocks, 128, 0, st>>>(src, err + 1, err);
+            else k_intersect_refill<8, false, 16><<<blocks, 128, 0, st>>>(src, err + 1, err);
+        }
         return cudaGetLastError();
     }
     if (block == 0) block = 128;

@@ -33,6 +33,7 @@ struct DeviceScene {
     const float4* lights;  // LightRec[n_lights], 4 float4 each
     uint32_t n_nodes, n_tris, n_lights;
     uint32_t general_pick;  // 1: (bits * n) >> 32; 0: bits >> 29 (needs n == 8)
+    uint32_t depth;         // BVH depth (launch choices only)
 };
 
 struct DeviceCamera {

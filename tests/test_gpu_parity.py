@@ -74,6 +74,28 @@ def test_intersect_single_launch_shapes_bitexact(icosphere, orc, launch):
     assert (t.view(np.uint32) == ot.view(np.uint32)).all()
 
 
+def test_intersect_deep_tree_bitexact(gpu, orc):
+    """A 70-level tree (the 870k-triangle tube) takes the deep-tree launch of
+    the single-ray query; results equal the oracle's on rays from the camera
+    position into the tube and on random rays in the room."""
+    tris, _ = scenes.random_walk_tube(obj=False)
+    bvh = gpu.Bvh.build_device(tris)
+    assert bvh.depth > 40
+    scene = gpu.Scene(bvh)
+    osc = orc.OracleScene.from_bvh(bvh)
+    o, d = scenes.random_rays(1 << 16, seed=29)
+    eye = np.broadcast_to(np.array([0.0, 1.2, 1.6], np.float32), (4096, 3))
+    rng = np.random.default_rng(5)
+    dc = np.stack([rng.uniform(-0.6, 0.6, 4096), rng.uniform(-0.4, 0.3, 4096), -np.ones(4096)], 1)
+    dc = (dc / np.linalg.norm(dc, axis=1, keepdims=True)).astype(np.float32)
+    o, d = np.concatenate([eye, o]).astype(np.float32), np.concatenate([dc, d]).astype(np.float32)
+    t, tri = scene.intersect_nearest(o, d, traversal=1)
+    ot, otri = osc.intersect(o, d, mode=1)
+    assert (tri == otri).all(), np.nonzero(tri != otri)[0][:10]
+    assert (t.view(np.uint32) == ot.view(np.uint32)).all()
+    assert (tri >= 0).mean() > 0.5
+
+
 @pytest.mark.parametrize("traversal", [0, 1])
 def test_intersect_host_pipeline_equals_device_query(icosphere, traversal):
     """The host-buffer query cuts large batches into chunks on several
