@@ -113,6 +113,13 @@ int32_t WaveEngine::set_scenes(cvx_scene* const* scenes, uint32_t n) {
     }
     ECK(cudaMemcpy(d_scenes_, v.data(), n * sizeof(DeviceScene), cudaMemcpyHostToDevice), "upload scene table");
     n_scenes_ = n;
+    bool deep = false;
+    for (const DeviceScene& d : v) deep = deep || d.depth > 40;
+    if (deep != deep_) {  // captured graphs hold the other traversal variant
+        for (auto& g : graphs_) cudaGraphExecDestroy(g.exec);
+        graphs_.clear();
+        deep_ = deep;
+    }
     return CVX_OK;
 }
 
@@ -120,14 +127,14 @@ static bool same_out(const WaveOutputs& a, const WaveOutputs& b) { return std::m
 
 static cudaError_t launch_any(bool fused, const Job* jobs, const WaveHeader* hdr, const DeviceScene* scenes,
                               const WaveState& st, const WaveOutputs& out, bool packet, uint32_t bps,
-                              uint32_t refill_from, cudaStream_t stream) {
+                              uint32_t refill_from, bool deep, cudaStream_t stream) {
     return fused ? launch_wave_fused(jobs, hdr, scenes, out, packet, bps, stream)
-                 : launch_wave(jobs, hdr, scenes, st, out, packet, bps, refill_from, stream);
+                 : launch_wave(jobs, hdr, scenes, st, out, packet, bps, refill_from, deep, stream);
 }
 
 int32_t WaveEngine::launch(const WaveOutputs& out, cudaStream_t stream) {
     if (!use_graph_) {
-        ECK(launch_any(fused_, d_jobs_, d_hdr_, d_scenes_, st_, out, packet_, blocks_per_sm_, refill_from_, stream),
+        ECK(launch_any(fused_, d_jobs_, d_hdr_, d_scenes_, st_, out, packet_, blocks_per_sm_, refill_from_, deep_, stream),
             "wave launch");
         return CVX_OK;
     }
@@ -139,7 +146,7 @@ int32_t WaveEngine::launch(const WaveOutputs& out, cudaStream_t stream) {
     cudaGraph_t graph;
     ECK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal), "begin capture");
     cudaError_t e =
-        launch_any(fused_, d_jobs_, d_hdr_, d_scenes_, st_, out, packet_, blocks_per_sm_, refill_from_, stream);
+        launch_any(fused_, d_jobs_, d_hdr_, d_scenes_, st_, out, packet_, blocks_per_sm_, refill_from_, deep_, stream);
     cudaError_t e2 = cudaStreamEndCapture(stream, &graph);
     if (e != cudaSuccess) return cuda_err(e, "capture wave");
     if (e2 != cudaSuccess) return cuda_err(e2, "end capture");

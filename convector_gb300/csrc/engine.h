@@ -62,7 +62,7 @@ class WaveEngine {
     unsigned long long* d_job_rays_ = nullptr;
     uint32_t* d_err_ = nullptr;
     uint32_t n_scenes_ = 0, scene_cap_ = 0, max_groups_ = 0, max_jobs_ = 0, blocks_per_sm_ = 0, refill_from_ = 1;
-    bool packet_ = false, use_graph_ = false;
+    bool packet_ = false, use_graph_ = false, deep_ = false;  // deep_: a scene deeper than 40 levels
     std::vector<void*> owned_;
     std::vector<Graph> graphs_;
     cudaEvent_t e0_ = nullptr, e1_ = nullptr;

@@ -23,7 +23,7 @@ cudaError_t launch_resolve(const float* accum, uint32_t npx, float factor, uint3
 // refill_from: first bounce whose single-ray traversal uses ray refill (the
 // earlier ones traverse one octet per group); packet traversal ignores it.
 cudaError_t launch_wave(const Job* jobs, const WaveHeader* hdr, const DeviceScene* scenes, const WaveState& st,
-                        const WaveOutputs& out, bool packet, uint32_t blocks_per_sm, uint32_t refill_from,
+                        const WaveOutputs& out, bool packet, uint32_t blocks_per_sm, uint32_t refill_from, bool deep,
                         cudaStream_t stream);
 // The fused (megakernel) form of a wave: one persistent launch.
 cudaError_t launch_wave_fused(const Job* jobs, const WaveHeader* hdr, const DeviceScene* scenes,

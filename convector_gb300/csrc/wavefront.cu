@@ -201,12 +201,16 @@ struct QueueClaim {
 
 // 10 resident blocks per SM (48 registers): measured on the 870k-triangle
 // tube, 4.17 ms per sample against 4.56 (56 registers, 9 blocks), 4.69 (12) and 5.46 (16).
+// CLAIM: lanes without a ray wait until this many want one; 16 for waves of
+// shallow trees, 8 when a scene is deeper than 40 levels (room scene frame
+// 1.013 against 1.063 ms at 8; tube sample 4.23 against 4.33 ms at 16).
+template <int CLAIM>
 __global__ void __launch_bounds__(128, 10) k_wf_traverse_single(const Job* __restrict__ jobs,
                                                             const DeviceScene* __restrict__ scenes, WaveState st,
                                                             int bounce, WaveOutputs out) {
     QueueStore store{st};
     QueueClaim claim{jobs, scenes, st, st.queue[bounce & 1], st.counts[bounce] * 8u, &st.counts[6 + bounce]};
-    if (!traverse_refill<false, true, 8>(store, claim, g_tables_wf)) atomicOr(out.err, kErrStackOverflow);
+    if (!traverse_refill<false, true, CLAIM>(store, claim, g_tables_wf)) atomicOr(out.err, kErrStackOverflow);
 }
 
 __device__ __forceinline__ void finalize(const Job& j, uint32_t gi, int k, F3 color, F3 d, bool hit_em,
@@ -413,7 +417,7 @@ cudaError_t launch_resolve_multi(const ResolveItem* items, uint32_t n_items, con
 
 cudaError_t launch_wave(const Job* jobs, const WaveHeader* hdr, const DeviceScene* scenes, const WaveState& st,
                         const WaveOutputs& out, bool packet, uint32_t blocks_per_sm, uint32_t refill_from,
-                        cudaStream_t stream) {
+                        bool deep, cudaStream_t stream) {
     if (blocks_per_sm == 0) blocks_per_sm = 12;
     uint32_t grid = (uint32_t)sms() * blocks_per_sm;
     // counts[0..5]: queue lengths per bounce; counts[6..10]: ray counters of
@@ -424,7 +428,8 @@ cudaError_t launch_wave(const Job* jobs, const WaveHeader* hdr, const DeviceScen
     for (int b = 0; b < 5; b++) {
         if (packet) k_wf_traverse_octet<true><<<grid, 128, 0, stream>>>(jobs, scenes, st, b, out);
         else if ((uint32_t)b < refill_from) k_wf_traverse_octet<false><<<grid, 128, 0, stream>>>(jobs, scenes, st, b, out);
-        else k_wf_traverse_single<<<grid, 128, 0, stream>>>(jobs, scenes, st, b, out);
+        else if (deep) k_wf_traverse_single<8><<<grid, 128, 0, stream>>>(jobs, scenes, st, b, out);
+        else k_wf_traverse_single<16><<<grid, 128, 0, stream>>>(jobs, scenes, st, b, out);
         k_wf_shade<<<grid, 128, 0, stream>>>(jobs, scenes, st, b, out);
     }
     return cudaGetLastError();
