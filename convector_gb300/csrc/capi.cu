@@ -375,7 +375,7 @@ int32_t cvx_renderer_create(cvx_scene* scene, uint32_t w, uint32_t h, const cvx_
     if ((st = dalloc(&r->d_color, npx * 3, "frame buffer"))) return st;
     if ((st = dalloc(&r->d_accum, npx * 3, "accumulator"))) return st;
     if ((st = dalloc(&r->d_rays, 1, "counters"))) return st;
-    if ((st = dalloc(&r->d_err, 1, "status"))) return st;
+    if ((st = dalloc(&r->d_err, 2, "status"))) return st;  // [0] status, [1] group counter
     CK(cudaStreamCreateWithFlags(&r->stream, cudaStreamNonBlocking), "cudaStreamCreate");
     CK(cudaEventCreate(&r->e0), "cudaEventCreate");
     CK(cudaEventCreate(&r->e1), "cudaEventCreate");
@@ -433,7 +433,7 @@ static int32_t run_frame(cvx_renderer* r, uint32_t frame, bool accumulate, uint3
     if (r->engine && !r->debug) return run_frame_wavefront(r, frame, accumulate, rgba, gbuf);
     size_t npx = (size_t)r->w * r->h;
     CK(cudaMemsetAsync(r->d_rays, 0, 8, r->stream), "reset counters");
-    CK(cudaMemsetAsync(r->d_err, 0, 4, r->stream), "reset status");
+    CK(cudaMemsetAsync(r->d_err, 0, 8, r->stream), "reset status");
     CK(cudaEventRecord(r->e0, r->stream), "event");
     CK(launch_render(r->scene->view(), r->cam, r->w, r->h, frame, r->cfg.traversal == CVX_TRAVERSE_PACKET,
                      r->cfg.rng_order == CVX_RNG_PATCH, accumulate ? nullptr : r->d_rgba, r->d_gbuf, r->d_color,

@@ -87,7 +87,7 @@ int32_t WaveEngine::init(uint32_t max_groups, uint32_t max_jobs, bool packet, bo
     if ((st = alloc(&d_hdr_, 1, owned_))) return st;
     if ((st = alloc(&d_rays_, 1, owned_))) return st;
     if ((st = alloc(&d_job_rays_, max_jobs, owned_))) return st;
-    if ((st = alloc(&d_err_, 1, owned_))) return st;
+    if ((st = alloc(&d_err_, 2, owned_))) return st;  // [0] status, [1] group counter of the fused kernel
     ECK(cudaMallocHost((void**)&h_jobs_, max_jobs * sizeof(Job)), "pinned job staging");
     ECK(cudaMallocHost((void**)&h_hdr_, sizeof(WaveHeader)), "pinned job staging");
     ECK(cudaMallocHost((void**)&h_read_, sizeof(Readback)), "pinned readback");
@@ -188,7 +188,7 @@ int32_t WaveEngine::submit(const std::vector<Job>& jobs_in, WaveOutputs out, cud
         "upload jobs");
     ECK(cudaMemcpyAsync(d_hdr_, h_hdr_, sizeof(WaveHeader), cudaMemcpyHostToDevice, stream), "upload jobs");
     ECK(cudaMemsetAsync(d_rays_, 0, 8, stream), "reset counters");
-    ECK(cudaMemsetAsync(d_err_, 0, 4, stream), "reset status");
+    ECK(cudaMemsetAsync(d_err_, 0, 8, stream), "reset status");
     if (want_job_rays) ECK(cudaMemsetAsync(d_job_rays_, 0, jobs_in.size() * 8, stream), "reset counters");
     ECK(cudaEventRecord(e0_, stream), "event");
     int32_t st = launch(out, stream);
