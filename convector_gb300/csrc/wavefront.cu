@@ -139,9 +139,10 @@ __global__ void __launch_bounds__(128, 8) k_wf_traverse_octet(const Job* __restr
     const unsigned omask = 0xffu << (threadIdx.x & 24u);
     const uint32_t n = st.counts[bounce];
     const uint32_t* queue = st.queue[bounce & 1];
-    const uint32_t octets = (gridDim.x * blockDim.x) >> 3;
     bool ok = true;
-    for (uint32_t qi = (blockIdx.x * blockDim.x + threadIdx.x) >> 3; qi < n; qi += octets) {
+    // Queue entries claimed one at a time by each octet (counter counts[11 + bounce]).
+    uint32_t* next = &st.counts[11 + bounce];
+    for (uint32_t qi = octet_claim_wf(next, omask, k); qi < n; qi = octet_claim_wf(next, omask, k)) {
         uint32_t gi = queue[qi];
         size_t l = (size_t)gi * 8 + k;
         const DeviceScene s = scenes[jobs[st.group_job[gi]].scene];
@@ -431,7 +432,8 @@ cudaError_t launch_wave(const Job* jobs, const WaveHeader* hdr, const DeviceScen
     if (blocks_per_sm == 0) blocks_per_sm = 12;
     uint32_t grid = (uint32_t)sms() * blocks_per_sm;
     // counts[0..5]: queue lengths per bounce; counts[6..10]: ray counters of
-    // the refill traversal, one per bounce
+    // the refill traversal, one per bounce; counts[11..15]: queue-entry
+    // counters of the octet traversal, one per bounce
     cudaError_t e = cudaMemsetAsync(st.counts, 0, 16 * sizeof(uint32_t), stream);
     if (e != cudaSuccess) return e;
     k_wf_raygen<<<grid, 128, 0, stream>>>(jobs, hdr, st);

@@ -38,7 +38,8 @@ struct WaveState {
     int32_t* htri;
     uint32_t* group_job;
     uint32_t* queue[2];  // group queues, alternating between bounces
-    uint32_t* counts;    // [b]: groups alive before bounce b (0..5); [6 + b]: refill ray counter of bounce b
+    uint32_t* counts;    // [b]: groups alive before bounce b (0..5); [6 + b]: refill ray counter of
+                         // bounce b; [11 + b]: octet traversal's queue-entry counter of bounce b
 };
 
 struct WaveOutputs {
