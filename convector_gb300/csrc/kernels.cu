@@ -67,6 +67,13 @@ __global__ void k_prep_lights(const cvx_triangle* __restrict__ tris, const uint3
 // ---------------------------------------------------------------------------
 // Nearest hit over SoA rays (Bvh::intersect_nearest, bvh.rs:659)
 
+// Next unit (group or packet) index for the calling octet (one atomic by its lane 0).
+__device__ __forceinline__ uint32_t octet_claim(uint32_t* counter, unsigned omask, int k) {
+    uint32_t g = 0;
+    if (k == 0) g = atomicAdd(counter, 1u);
+    return __shfl_sync(omask, g, (int)(threadIdx.x & 24u));
+}
+
 template <bool PACKET>
 __global__ void __launch_bounds__(256) k_intersect(DeviceScene s, const float* __restrict__ rays, uint32_t n,
                                                    float far_dist, float* __restrict__ t_out,
@@ -74,10 +81,12 @@ __global__ void __launch_bounds__(256) k_intersect(DeviceScene s, const float* _
                                                    uint32_t* __restrict__ err) {
     __shared__ ApproxTables tab;
     load_tables(tab);
-    const uint32_t stride = gridDim.x * blockDim.x;
     const unsigned omask = 0xffu << (threadIdx.x & 24u);
-    const uint32_t npad = (n + 7u) & ~7u;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < npad; i += stride) {
+    const int k = threadIdx.x & 7;
+    const uint32_t npk = (n + 7u) >> 3;
+    // Packets (8 consecutive rays, one per octet) claimed one at a time from err[1].
+    for (uint32_t pk = octet_claim(err + 1, omask, k); pk < npk; pk = octet_claim(err + 1, omask, k)) {
+        uint32_t i = pk * 8u + (uint32_t)k;
         bool active = i < n;
         uint32_t src = active ? i : (i & ~7u);
         F3 o = f3(__ldg(rays + src), __ldg(rays + n + src), __ldg(rays + 2 * n + src));
@@ -231,13 +240,6 @@ struct FrameArgs {
     uint32_t* err;
     uint32_t debug;  // Renderer::toggle_debug_view (renderer.rs:150-152)
 };
-
-// Next group index for the calling octet (one atomic by its lane 0).
-__device__ __forceinline__ uint32_t octet_claim(uint32_t* counter, unsigned omask, int k) {
-    uint32_t g = 0;
-    if (k == 0) g = atomicAdd(counter, 1u);
-    return __shfl_sync(omask, g, (int)(threadIdx.x & 24u));
-}
 
 // Screen x (or y) of lane k of group g of the 16x4 block at (xb, yb), before
 // jitter (renderer.rs:171-198).
@@ -426,6 +428,8 @@ cudaError_t launch_intersect(const DeviceScene& s, const float* rays, uint32_t n
         }
         return cudaGetLastError();
     }
+    cudaError_t e = cudaMemsetAsync(err + 1, 0, 4, st);  // packet counter
+    if (e != cudaSuccess) return e;
     if (block == 0) block = 128;
     if (blocks_per_sm == 0) blocks_per_sm = 8;
     uint32_t need = ((n + 7u) & ~7u) / block + 1u;
