@@ -372,8 +372,11 @@ def _frames(r, frames, first=42, accumulate=False):
         nr, m = r.stats()
         ms.append(m)
         rays += nr
+    # a path is one pixel's sample: camera ray and its bounces
+    paths = r.width * r.height * frames
     return {"frame_ms_p50": float(np.percentile(ms, 50)), "frame_ms_p99": float(np.percentile(ms, 99)),
-            "mrays_per_s": rays / (sum(ms) * 1e-3) / 1e6, "rays_per_frame": rays / frames, "frames": frames}
+            "mrays_per_s": rays / (sum(ms) * 1e-3) / 1e6, "mpaths_per_s": paths / (sum(ms) * 1e-3) / 1e6,
+            "rays_per_frame": rays / frames, "frames": frames}
 
 
 def bench_render(cg):
