@@ -106,6 +106,9 @@ def lib(build=False):
         "cvx_camera_default": (None, [P]),
         "cvx_camera_set_rotation": (None, [P, F32, F32]),
         "cvx_camera_set_fov": (None, [P, F32]),
+        "cvx_camera_set_interactive": (None, [P, F32, F32]),
+        "cvx_renderer_set_time": (I32, [P, F32, F32]),
+        "cvx_renderer_update_scene": (I32, [P]),
         "cvx_scene_create": (I32, [P, U32, P, U32, P]),
         "cvx_scene_from_bvh": (I32, [P, P]),
         "cvx_scene_num_direct_samples": (U32, [P]),
@@ -317,6 +320,11 @@ class Camera:
     def set_rotation(self, radians, delta=0.0):
         lib().cvx_camera_set_rotation(ctypes.byref(self._c), radians, delta)
 
+    def set_interactive(self, time, time_delta=0.0):
+        """The camera of Renderer::update_scene (renderer.rs:140-147) at `time`."""
+        lib().cvx_camera_set_interactive(ctypes.byref(self._c), time, time_delta)
+        return self
+
     def set_fov(self, fov):
         lib().cvx_camera_set_fov(ctypes.byref(self._c), fov)
 
@@ -404,6 +412,15 @@ class Renderer:
 
     def set_camera(self, camera):
         _check(lib().cvx_renderer_set_camera(self._h, ctypes.byref(camera._c)))
+
+    def set_time(self, time, time_delta=0.0):
+        """Renderer::set_time (renderer.rs:134-137)."""
+        _check(lib().cvx_renderer_set_time(self._h, time, time_delta))
+
+    def update_scene(self):
+        """Renderer::update_scene (renderer.rs:140-147): moves this renderer's
+        camera along the interactive path to the time set by set_time."""
+        _check(lib().cvx_renderer_update_scene(self._h))
 
     def toggle_debug_view(self, enable=None):
         """Renderer::toggle_debug_view (renderer.rs:150-152); with an argument, sets it."""

@@ -141,6 +141,7 @@ struct cvx_renderer {
     cudaStream_t stream = nullptr;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     uint64_t last_rays = 0;
+    float time = 0.0f, time_delta = 0.0f;  // Renderer::set_time (renderer.rs:134-137)
     float last_ms = 0.0f;
     bool debug = false;
     ~cvx_renderer() {
@@ -394,6 +395,22 @@ int32_t cvx_renderer_create(cvx_scene* scene, uint32_t w, uint32_t h, const cvx_
 }
 
 void cvx_renderer_destroy(cvx_renderer* r) { delete r; }
+
+int32_t cvx_renderer_set_time(cvx_renderer* r, float time, float time_delta) {
+    if (!r) return set_error(CVX_ERR_INVALID, "null renderer");
+    r->time = time;
+    r->time_delta = time_delta;
+    return CVX_OK;
+}
+
+int32_t cvx_renderer_update_scene(cvx_renderer* r) {
+    if (!r) return set_error(CVX_ERR_INVALID, "null renderer");
+    cvx_camera cam;
+    std::memcpy(&cam, &r->cam, sizeof cam);
+    cvx_camera_set_interactive(&cam, r->time, r->time_delta);
+    std::memcpy(&r->cam, &cam, sizeof cam);
+    return CVX_OK;
+}
 
 int32_t cvx_renderer_set_camera(cvx_renderer* r, const cvx_camera* cam) {
     if (!r || !cam) return set_error(CVX_ERR_INVALID, "null argument");

@@ -939,4 +939,20 @@ void cvx_camera_set_rotation(cvx_camera* c, float radians, float delta) {
 // scene.rs:61-63
 void cvx_camera_set_fov(cvx_camera* c, float fov) { c->screen_distance = 1.0f / std::sin(fov / 2.0f); }
 
+// Renderer::update_scene (renderer.rs:140-147): the interactive camera path
+// around the scene at `time` seconds, moving by `time_delta` over one frame.
+void cvx_camera_set_interactive(cvx_camera* c, float time, float time_delta) {
+    float alpha = time * -0.02f + 0.1f;
+    float alpha_delta = time_delta * -0.02f;
+    float sa = std::sin(alpha), ca = std::cos(alpha);
+    // scene.rs:47-50 (set_position) with SVector3 * f32 (vector3.rs)
+    c->position[0] = -3.8f * sa;
+    c->position[1] = 1.6f;
+    c->position[2] = 3.0f * ca;
+    c->position_delta[0] = (-3.8f * ca) * alpha_delta;
+    c->position_delta[1] = 0.0f * alpha_delta;
+    c->position_delta[2] = (-3.0f * sa) * alpha_delta;
+    cvx_camera_set_rotation(c, alpha, alpha_delta);
+}
+
 }  // extern "C"

@@ -108,6 +108,10 @@ void cvx_bvh_destroy(cvx_bvh* bvh);
 void cvx_camera_default(cvx_camera* cam);
 void cvx_camera_set_rotation(cvx_camera* cam, float radians, float delta);
 void cvx_camera_set_fov(cvx_camera* cam, float fov);
+/* The camera step of Renderer::update_scene (renderer.rs:140-147): position
+ * and rotation on the interactive path at `time`, with the deltas of a frame
+ * lasting `time_delta` (motion blur over the frame). */
+void cvx_camera_set_interactive(cvx_camera* cam, float time, float time_delta);
 
 /* ---- device: scenes ------------------------------------------------------ */
 
@@ -198,6 +202,12 @@ int32_t cvx_renderer_create(cvx_scene* scene, uint32_t width, uint32_t height, c
 void cvx_renderer_destroy(cvx_renderer* r);
 /* The scene's camera (scene.rs:103 `pub camera`). */
 int32_t cvx_renderer_set_camera(cvx_renderer* r, const cvx_camera* cam);
+/* Renderer::set_time (renderer.rs:134-137): the time of the next frame and
+ * the frame's duration. */
+int32_t cvx_renderer_set_time(cvx_renderer* r, float time, float time_delta);
+/* Renderer::update_scene (renderer.rs:140-147): moves this renderer's camera
+ * to the interactive path position of the time set above. */
+int32_t cvx_renderer_update_scene(cvx_renderer* r);
 /* Renderer::toggle_debug_view (renderer.rs:150-152): frames show log2 of the
  * boxes (green) and triangles (blue) tested per packet, times 0.1
  * (renderer.rs:470-486). The debug view always runs the fused kernel. */

@@ -161,6 +161,23 @@ def _render_both(gpu, orc, scene, osc, w, h, frame, rng_order, traversal):
     return (rgba, gb, col, rays), (orgba, ogb, ocol, orays)
 
 
+def test_render_after_update_scene_bitexact(room, gpu, orc):
+    """Renderer::set_time + update_scene (renderer.rs:134-147) move the camera
+    with a per-frame delta (motion blur); the frame equals the oracle's with
+    the same camera."""
+    bvh, scene, osc = room
+    r = gpu.Renderer(scene, 160, 96, rng_order=gpu.RNG_PATCH, traversal=gpu.TRAVERSE_PACKET)
+    r.set_time(7.25, 0.04)
+    r.update_scene()
+    rgba, gb = r.render_frame_u8(42)
+    cam = gpu.Camera().set_interactive(7.25, 0.04)
+    orgba, ogb, _, _ = osc.render(cam.as_array(), 160, 96, 42, rng_order=0, traversal=0)
+    assert (rgba == orgba).all() and (gb == ogb).all()
+    still = gpu.Renderer(scene, 160, 96, rng_order=gpu.RNG_PATCH, traversal=gpu.TRAVERSE_PACKET)
+    still.set_camera(gpu.Camera().set_interactive(7.25, 0.0))
+    assert not (still.render_frame_u8(42)[0] == rgba).all()  # the delta blurs the frame
+
+
 @pytest.mark.parametrize("rng_order", [0, 1])
 @pytest.mark.parametrize("traversal", [0, 1])
 def test_render_small_bitexact(room, gpu, orc, rng_order, traversal):

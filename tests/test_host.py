@@ -282,3 +282,27 @@ def test_obj_vertex_coordinate_syntax(cvx, tok, ok):
     else:
         with pytest.raises(cvx.CvxError, match="bad vertex coordinate"):
             cvx.Mesh.parse(text)
+
+
+@pytest.mark.parametrize("time,delta", [(0.0, 0.0), (12.5, 0.016), (-3.0, 0.05), (1000.0, 1.0)])
+def test_interactive_camera_path(cvx, time, delta):
+    """renderer.rs:140-147 and scene.rs:47-74 in f32, with the sinf/cosf of the
+    C library the product is linked against."""
+    libm = ctypes.CDLL(None)
+    for name in ("sinf", "cosf"):
+        getattr(libm, name).restype = ctypes.c_float
+        getattr(libm, name).argtypes = [ctypes.c_float]
+    f = np.float32
+    alpha = f(f(f(time) * f(-0.02)) + f(0.1))
+    ad = f(f(delta) * f(-0.02))
+    sa, ca = f(libm.sinf(alpha)), f(libm.cosf(alpha))
+    c = cvx.Camera().set_interactive(time, delta)
+    assert np.array(c._c.position, np.float32).tolist() == [f(f(-3.8) * sa), f(1.6), f(f(3.0) * ca)]
+    pd = np.array(c._c.position_delta, np.float32)
+    assert pd.tobytes() == np.array([f(f(f(-3.8) * ca) * ad), f(f(0.0) * ad), f(f(f(-3.0) * sa) * ad)],
+                                    np.float32).tobytes()
+    r = cvx.Camera()
+    r.set_rotation(float(alpha), float(ad))
+    assert np.array(c._c.orientation, np.float32).tobytes() == np.array(r._c.orientation, np.float32).tobytes()
+    assert np.array(c._c.orientation_delta, np.float32).tobytes() == \
+        np.array(r._c.orientation_delta, np.float32).tobytes()
