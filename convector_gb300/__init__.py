@@ -122,6 +122,8 @@ def lib(build=False):
         "cvx_renderer_destroy": (None, [P]),
         "cvx_renderer_set_camera": (I32, [P, P]),
         "cvx_render_frame_u8": (I32, [P, U32, P, P]),
+        "cvx_render_patches_u8": (I32, [P, U32, P, U32, U32, P, P]),
+        "cvx_accumulate_patches_f32": (I32, [P, U32, P, U32, U32, P]),
         "cvx_accumulate_frame_f32": (I32, [P, U32, P]),
         "cvx_resolve_u8": (I32, [P, U32, P]),
         "cvx_read_accumulator": (I32, [P, P]),
@@ -432,6 +434,24 @@ class Renderer:
         gb = np.empty((self.height, self.width), dtype=np.uint32) if gbuffer else None
         _check(lib().cvx_render_frame_u8(self._h, frame_number, _ptr(rgba), _ptr(gb)))
         return rgba, gb
+
+    def render_patches_u8(self, patch_width, origins, frame_number, rgba=None, gbuffer=None):
+        """Renderer::render_patch_u8 (renderer.rs:306-327) for every (x, y) in
+        `origins`, into full-frame uint32 buffers (created when None; pixels
+        outside the patches are left as they are). Returns (rgba, gbuffer)."""
+        xy = np.ascontiguousarray(np.asarray(origins, dtype=np.uint32).reshape(-1, 2))
+        rgba = np.zeros((self.height, self.width), np.uint32) if rgba is None else rgba
+        gbuffer = np.zeros((self.height, self.width), np.uint32) if gbuffer is None else gbuffer
+        _check(lib().cvx_render_patches_u8(self._h, patch_width, _ptr(xy), xy.shape[0], frame_number, _ptr(rgba),
+                                           _ptr(gbuffer)))
+        return rgba, gbuffer
+
+    def accumulate_patches_f32(self, patch_width, origins, frame_number, gbuffer=None):
+        """Renderer::accumulate_patch_f32 (renderer.rs:339-362) for every (x, y) in `origins`."""
+        xy = np.ascontiguousarray(np.asarray(origins, dtype=np.uint32).reshape(-1, 2))
+        _check(lib().cvx_accumulate_patches_f32(self._h, patch_width, _ptr(xy), xy.shape[0], frame_number,
+                                                _ptr(gbuffer)))
+        return gbuffer
 
     def accumulate_frame_f32(self, frame_number, gbuffer=False):
         gb = np.empty((self.height, self.width), dtype=np.uint32) if gbuffer else None

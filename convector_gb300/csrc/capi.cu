@@ -144,7 +144,10 @@ struct cvx_renderer {
     float time = 0.0f, time_delta = 0.0f;  // Renderer::set_time (renderer.rs:134-137)
     float last_ms = 0.0f;
     bool debug = false;
+    uint32_t* d_patches = nullptr;  // patch origins of the patch entry points
+    uint32_t patch_cap = 0;
     ~cvx_renderer() {
+        cudaFree(d_patches);
         cudaFree(d_rgba);
         cudaFree(d_gbuf);
         cudaFree(d_color);
@@ -475,6 +478,73 @@ int32_t cvx_renderer_set_debug_view(cvx_renderer* r, uint32_t enable) {
     if (!r) return set_error(CVX_ERR_INVALID, "null renderer");
     r->debug = enable != 0;
     return CVX_OK;
+}
+
+// The listed patches with the reference's per-patch generator, in one launch
+// (one octet per patch); only the patches' pixels are copied to the caller's
+// full-frame buffers.
+static int32_t run_patches(cvx_renderer* r, uint32_t pw, const uint32_t* xy, uint32_t n, uint32_t frame,
+                           bool accumulate, uint32_t* rgba, uint32_t* gbuf) {
+    if (!r) return set_error(CVX_ERR_INVALID, "null renderer");
+    if (pw == 0 || (pw & 15u)) return set_error(CVX_ERR_INVALID, "patch width must be a positive multiple of 16");
+    if (n && !xy) return set_error(CVX_ERR_INVALID, "null patch list");
+    for (uint32_t i = 0; i < n; i++) {
+        uint32_t x = xy[2 * i], y = xy[2 * i + 1];
+        if ((x & 15u) || (y & 3u) || x >= r->w || y >= r->h)
+            return set_error(CVX_ERR_INVALID, "patch origin " + std::to_string(x) + "," + std::to_string(y) +
+                                                  " must lie in the frame at a multiple of 16 (x) and 4 (y)");
+    }
+    if (n == 0) return CVX_OK;
+    int32_t st = 0;
+    if (n > r->patch_cap) {
+        cudaFree(r->d_patches);
+        r->d_patches = nullptr;
+        r->patch_cap = 0;
+        if ((st = dalloc(&r->d_patches, (size_t)2 * n, "patch list"))) return st;
+        r->patch_cap = n;
+    }
+    CK(cudaMemcpyAsync(r->d_patches, xy, (size_t)8 * n, cudaMemcpyHostToDevice, r->stream), "copy patch list");
+    CK(cudaMemsetAsync(r->d_rays, 0, 8, r->stream), "reset counters");
+    CK(cudaMemsetAsync(r->d_err, 0, 8, r->stream), "reset status");
+    CK(cudaEventRecord(r->e0, r->stream), "event");
+    CK(launch_render(r->scene->view(), r->cam, r->w, r->h, frame, r->cfg.traversal == CVX_TRAVERSE_PACKET, true,
+                     accumulate ? nullptr : r->d_rgba, r->d_gbuf, r->d_color, accumulate ? r->d_accum : nullptr,
+                     r->d_rays, r->d_err, r->cfg.block_size, r->debug, r->stream, pw, r->d_patches, n),
+       "render launch");
+    CK(cudaEventRecord(r->e1, r->stream), "event");
+    size_t pitch = (size_t)r->w * 4;
+    for (uint32_t i = 0; i < n; i++) {
+        uint32_t x = xy[2 * i], y = xy[2 * i + 1];
+        size_t cols = std::min<size_t>(pw, r->w - x), rows = std::min<size_t>(pw, r->h - y);
+        size_t off = (size_t)y * r->w + x;
+        if (rgba && !accumulate)
+            CK(cudaMemcpy2DAsync(rgba + off, pitch, r->d_rgba + off, pitch, cols * 4, rows, cudaMemcpyDeviceToHost,
+                                 r->stream),
+               "copy colour");
+        if (gbuf)
+            CK(cudaMemcpy2DAsync(gbuf + off, pitch, r->d_gbuf + off, pitch, cols * 4, rows, cudaMemcpyDeviceToHost,
+                                 r->stream),
+               "copy gbuffer");
+    }
+    unsigned long long rays = 0;
+    uint32_t err = 0;
+    CK(cudaMemcpyAsync(&rays, r->d_rays, 8, cudaMemcpyDeviceToHost, r->stream), "copy counters");
+    CK(cudaMemcpyAsync(&err, r->d_err, 4, cudaMemcpyDeviceToHost, r->stream), "copy status");
+    CK(cudaStreamSynchronize(r->stream), "render");
+    cudaEventElapsedTime(&r->last_ms, r->e0, r->e1);
+    r->last_rays = rays;
+    if (err) return set_error(CVX_ERR_DEVICE, "traversal stack overflow reported by the kernel");
+    return CVX_OK;
+}
+
+int32_t cvx_render_patches_u8(cvx_renderer* r, uint32_t patch_width, const uint32_t* origins, uint32_t n_patches,
+                              uint32_t frame, uint32_t* rgba, uint32_t* gbuffer) {
+    return run_patches(r, patch_width, origins, n_patches, frame, false, rgba, gbuffer);
+}
+
+int32_t cvx_accumulate_patches_f32(cvx_renderer* r, uint32_t patch_width, const uint32_t* origins,
+                                   uint32_t n_patches, uint32_t frame, uint32_t* gbuffer) {
+    return run_patches(r, patch_width, origins, n_patches, frame, true, nullptr, gbuffer);
 }
 
 int32_t cvx_render_frame_u8(cvx_renderer* r, uint32_t frame, uint32_t* rgba, uint32_t* gbuffer) {

@@ -239,6 +239,11 @@ struct FrameArgs {
     unsigned long long* rays;
     uint32_t* err;
     uint32_t debug;  // Renderer::toggle_debug_view (renderer.rs:150-152)
+    // patch order: patch width (a multiple of 16) and the patch origins
+    // (x, y pairs; null: every patch of the frame, column by column)
+    uint32_t patch;
+    const uint32_t* patches;
+    uint32_t n_patches;
 };
 
 // Screen x (or y) of lane k of group g of the 16x4 block at (xb, yb), before
@@ -323,16 +328,19 @@ __global__ void __launch_bounds__(128) k_render_patch(FrameArgs a) {
     load_tables(tab);
     const int k = threadIdx.x & 7;
     const unsigned omask = 0xffu << (threadIdx.x & 24u);
-    const uint32_t pw = (a.w + 31u) / 32u, ph = (a.h + 31u) / 32u;
+    const uint32_t pw = (a.w + a.patch - 1u) / a.patch, ph = (a.h + a.patch - 1u) / a.patch;
+    const uint32_t n = a.patches ? a.n_patches : pw * ph;
+    const uint32_t wb = a.patch / 16u, hb = a.patch / 4u;  // 16x4 blocks across and up a patch
     const uint32_t octets = (gridDim.x * blockDim.x) >> 3;
     uint32_t rays = 0;
     bool ok = true;
-    for (uint32_t pi = (blockIdx.x * blockDim.x + threadIdx.x) >> 3; pi < pw * ph; pi += octets) {
-        uint32_t x0 = (pi / ph) * 32u, y0 = (pi % ph) * 32u;
+    for (uint32_t pi = (blockIdx.x * blockDim.x + threadIdx.x) >> 3; pi < n; pi += octets) {
+        uint32_t x0 = a.patches ? a.patches[2 * pi] : (pi / ph) * a.patch;
+        uint32_t y0 = a.patches ? a.patches[2 * pi + 1] : (pi % ph) * a.patch;
         LaneRng rng;
         rng.seed(x0, y0, a.frame, k);
-        for (uint32_t i = 0; i < 2; i++) {
-            for (uint32_t j = 0; j < 8; j++) {
+        for (uint32_t i = 0; i < wb; i++) {
+            for (uint32_t j = 0; j < hb; j++) {
                 uint32_t xb = x0 + i * 16u, yb = y0 + j * 4u;
                 float jx[8], jy[8];
                 for (int q = 0; q < 8; q++) jx[q] = unit_from(rng.next());
@@ -444,11 +452,13 @@ cudaError_t launch_intersect(const DeviceScene& s, const float* rays, uint32_t n
 
 cudaError_t launch_render(const DeviceScene& s, const DeviceCamera& cam, uint32_t w, uint32_t h, uint32_t frame,
                           bool packet, bool patch_order, uint32_t* rgba, uint32_t* gbuf, float* color, float* accum,
-                          unsigned long long* rays, uint32_t* err, uint32_t block, bool debug, cudaStream_t st) {
-    FrameArgs a{s, cam, w, h, frame, rgba, gbuf, color, accum, rays, err, debug ? 1u : 0u};
+                          unsigned long long* rays, uint32_t* err, uint32_t block, bool debug, cudaStream_t st,
+                          uint32_t patch, const uint32_t* patches, uint32_t n_patches) {
+    if (patch == 0) patch = 32;
+    FrameArgs a{s, cam, w, h, frame, rgba, gbuf, color, accum, rays, err, debug ? 1u : 0u, patch, patches, n_patches};
     if (block == 0) block = 128;
     if (patch_order) {
-        uint32_t units = ((w + 31) / 32) * ((h + 31) / 32);
+        uint32_t units = patches ? n_patches : ((w + patch - 1) / patch) * ((h + patch - 1) / patch);
         uint32_t blocks = (units * 8 + block - 1) / block;
         if (packet) k_render_patch<true><<<blocks, block, 0, st>>>(a);
         else k_render_patch<false><<<blocks, block, 0, st>>>(a);

@@ -18,7 +18,8 @@ cudaError_t launch_intersect(const DeviceScene& s, const float* rays, uint32_t n
                              uint32_t blocks_per_sm, cudaStream_t st);
 cudaError_t launch_render(const DeviceScene& s, const DeviceCamera& cam, uint32_t w, uint32_t h, uint32_t frame,
                           bool packet, bool patch_order, uint32_t* rgba, uint32_t* gbuf, float* color, float* accum,
-                          unsigned long long* rays, uint32_t* err, uint32_t block, bool debug, cudaStream_t st);
+                          unsigned long long* rays, uint32_t* err, uint32_t block, bool debug, cudaStream_t st, uint32_t patch = 32,
+                          const uint32_t* patches = nullptr, uint32_t n_patches = 0);
 cudaError_t launch_resolve(const float* accum, uint32_t npx, float factor, uint32_t* rgba, cudaStream_t st);
 // refill_from: first bounce whose single-ray traversal uses ray refill (the
 // earlier ones traverse one octet per group); packet traversal ignores it.

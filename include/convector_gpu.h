@@ -219,6 +219,20 @@ int32_t cvx_render_frame_u8(cvx_renderer* r, uint32_t frame_number, uint32_t* rg
 /* Renderer::accumulate_patch_f32 (renderer.rs:339-362) over the frame: adds
  * this frame's colour to the device accumulator; gbuffer may be NULL. */
 int32_t cvx_accumulate_frame_f32(cvx_renderer* r, uint32_t frame_number, uint32_t* gbuffer);
+/* Renderer::render_patch_u8 (renderer.rs:306-327) for a list of patches in
+ * one call: origins holds n_patches (x, y) pairs, each patch patch_width
+ * pixels square (a multiple of 16) with its own generator seeded (x, y,
+ * frame_number), as in the reference whatever the renderer's rng_order.
+ * x must be a multiple of 16 and y of 4, inside the frame. Only the patches'
+ * pixels of the full-frame rgba / gbuffer buffers (either may be NULL) are
+ * written; the rest of the caller's buffers is left as it is. */
+int32_t cvx_render_patches_u8(cvx_renderer* r, uint32_t patch_width, const uint32_t* origins, uint32_t n_patches,
+                              uint32_t frame_number, uint32_t* rgba, uint32_t* gbuffer);
+/* Renderer::accumulate_patch_f32 (renderer.rs:339-362) for a list of
+ * patches: adds their colour to the device accumulator (read it with
+ * cvx_resolve_u8) and writes their gbuffer pixels (may be NULL). */
+int32_t cvx_accumulate_patches_f32(cvx_renderer* r, uint32_t patch_width, const uint32_t* origins,
+                                   uint32_t n_patches, uint32_t frame_number, uint32_t* gbuffer);
 /* Renderer::buffer_f32_into_render_buffer (renderer.rs:378-410). */
 int32_t cvx_resolve_u8(cvx_renderer* r, uint32_t num_samples, uint32_t* rgba);
 /* Reads (row-major, 3 floats per pixel) or zeroes the accumulator

@@ -680,9 +680,10 @@ inline void store_group(const Frame& f, uint32_t gx, uint32_t gy, const PixelOut
     }
 }
 
-// renderer.rs:306-327: one 32x32 patch with one RNG, blocks x-major.
-uint64_t render_patch(const Frame& f, uint32_t x, uint32_t y) {
-    const uint32_t pw = 32, wb = pw / 16, hb = pw / 4;
+// renderer.rs:306-327 (render_patch_u8) and 339-362 (accumulate_patch_f32):
+// one patch of pw x pw pixels (pw a multiple of 16) with one RNG, blocks x-major.
+uint64_t render_patch(const Frame& f, uint32_t x, uint32_t y, uint32_t pw = 32) {
+    const uint32_t wb = pw / 16, hb = pw / 4;
     Rng rng = Rng::with_seed(x, y, f.frame);
     uint64_t rays = 0;
     for (uint32_t i = 0; i < wb; i++) {
@@ -902,6 +903,32 @@ void orc_intersect(void* sp, const float* ox, const float* oy, const float* oz, 
             }
         }
     });
+}
+
+// The listed patches (origins xy[2 i], xy[2 i + 1], width pw) of one frame,
+// as a caller of render_patch_u8 / accumulate_patch_f32 would render them.
+uint64_t orc_render_patches(void* sp, const float* cam, uint32_t w, uint32_t h, uint32_t frame, int traversal,
+                            uint32_t pw, const uint32_t* xy, uint32_t n, uint32_t* rgba, uint32_t* gbuf,
+                            float* color, float* accum, int nthreads) {
+    Frame f;
+    f.s = (const Scene*)sp;
+    f.cam.pos = v3(cam[0], cam[1], cam[2]);
+    f.cam.pos_delta = v3(cam[3], cam[4], cam[5]);
+    f.cam.q = Quat{cam[6], cam[7], cam[8], cam[9]};
+    f.cam.dq = Quat{cam[10], cam[11], cam[12], cam[13]};
+    f.cam.screen_distance = cam[14];
+    f.w = w;
+    f.h = h;
+    f.frame = frame;
+    f.single = traversal == 1;
+    f.rgba = rgba;
+    f.gbuf = gbuf;
+    f.color = color;
+    f.accum = accum;
+    f.debug = false;
+    std::atomic<uint64_t> rays{0};
+    parallel_for(n, nthreads, [&](uint32_t i) { rays += render_patch(f, xy[2 * i], xy[2 * i + 1], pw); });
+    return rays.load();
 }
 
 // One frame. cam: pos[3], pos_delta[3], q[4], dq[4], screen_distance.

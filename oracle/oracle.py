@@ -31,6 +31,8 @@ def lib():
             "orc_intersect": (None, [P, P, P, P, P, P, P, U32, F32, ctypes.c_int, P, P, P, P, P, P, ctypes.c_int]),
             "orc_render": (U64, [P, P, U32, U32, U32, ctypes.c_int, ctypes.c_int, P, P, P, P, ctypes.c_int,
                                  ctypes.c_int]),
+            "orc_render_patches": (U64, [P, P, U32, U32, U32, ctypes.c_int, U32, P, U32, P, P, P, P,
+                                         ctypes.c_int]),
             "orc_display_new": (P, [U32, U32, P, P, U32, U32]),
             "orc_display_free": (None, [P]),
             "orc_display_frame": (None, [P, P, P, ctypes.c_int, ctypes.c_int, P]),
@@ -110,6 +112,16 @@ class OracleScene:
         rays = lib().orc_render(self._h, _p(cam), width, height, frame, rng_order, traversal, _p(rgba), _p(gbuf),
                                 _p(col), _p(accum), nthreads or default_threads(), int(debug))
         return rgba, gbuf, col, rays
+
+    def render_patches(self, camera, width, height, frame, patch_width, origins, traversal=TRAVERSE_PACKET,
+                       rgba=None, gbuf=None, accum=None, nthreads=None):
+        """renderer.rs:306-362 for the listed patch origins (x, y), into the given
+        full-frame buffers (rgba and gbuf uint32 [h, w], accum float32 [h, w, 3])."""
+        cam = np.ascontiguousarray(camera, dtype=np.float32)
+        xy = np.ascontiguousarray(np.asarray(origins, dtype=np.uint32).reshape(-1, 2))
+        return lib().orc_render_patches(self._h, _p(cam), width, height, frame, traversal, patch_width, _p(xy),
+                                        xy.shape[0], _p(rgba), _p(gbuf), None, _p(accum),
+                                        nthreads or default_threads())
 
     def __del__(self):
         if getattr(self, "_h", None) and _L is not None:

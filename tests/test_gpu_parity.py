@@ -161,6 +161,59 @@ def _render_both(gpu, orc, scene, osc, w, h, frame, rng_order, traversal):
     return (rgba, gb, col, rays), (orgba, ogb, ocol, orays)
 
 
+@pytest.mark.parametrize("traversal", [0, 1])
+def test_render_patches_all_equal_frame(room, gpu, traversal):
+    """Every 32x32 patch through the patch entry (one call) gives the frame of
+    the reference patch order."""
+    bvh, scene, osc = room
+    w, h = 160, 96
+    r = gpu.Renderer(scene, w, h, rng_order=gpu.RNG_PATCH, traversal=traversal)
+    rgba, gb = r.render_frame_u8(42)
+    origins = [(x, y) for x in range(0, w, 32) for y in range(0, h, 32)]
+    prgba, pgb = r.render_patches_u8(32, origins, 42)
+    assert (prgba == rgba).all() and (pgb == gb).all()
+
+
+@pytest.mark.parametrize("patch_width", [16, 64])
+def test_render_patches_bitexact_and_local(room, gpu, orc, patch_width):
+    """Patches of other widths, some crossing the frame edge, equal the
+    oracle's; pixels outside the listed patches keep the caller's values."""
+    bvh, scene, osc = room
+    w, h = 150, 90
+    r = gpu.Renderer(scene, w, h, rng_order=gpu.RNG_GROUP, traversal=gpu.TRAVERSE_PACKET)
+    origins = [(0, 0), (patch_width, 4 * 3), (144, 88), (96, 40)]
+    sentinel = np.uint32(0xDEADBEEF)
+    rgba = np.full((h, w), sentinel, np.uint32)
+    gb = np.full((h, w), sentinel, np.uint32)
+    r.render_patches_u8(patch_width, origins, 7, rgba, gb)
+    orgba = np.full((h, w), sentinel, np.uint32)
+    ogb = np.full((h, w), sentinel, np.uint32)
+    osc.render_patches(scene.camera.as_array(), w, h, 7, patch_width, origins, traversal=0, rgba=orgba, gbuf=ogb)
+    assert (rgba == orgba).all() and (gb == ogb).all()
+    assert (rgba == sentinel).any() and (rgba != sentinel).any()
+
+
+def test_accumulate_patches_equal_frames(room, gpu):
+    bvh, scene, osc = room
+    w, h = 96, 64
+    origins = [(x, y) for x in range(0, w, 32) for y in range(0, h, 32)]
+    a = gpu.Renderer(scene, w, h, rng_order=gpu.RNG_PATCH, traversal=gpu.TRAVERSE_PACKET)
+    b = gpu.Renderer(scene, w, h, rng_order=gpu.RNG_PATCH, traversal=gpu.TRAVERSE_PACKET)
+    for f in (5, 6, 7):
+        a.accumulate_frame_f32(f)
+        b.accumulate_patches_f32(32, origins, f)
+    assert (a.resolve_u8(3) == b.resolve_u8(3)).all()
+
+
+def test_render_patches_refuses_bad_arguments(room, gpu):
+    bvh, scene, osc = room
+    r = gpu.Renderer(scene, 64, 64, rng_order=gpu.RNG_PATCH, traversal=gpu.TRAVERSE_PACKET)
+    for pw, xy in ((24, [(0, 0)]), (32, [(8, 0)]), (32, [(0, 2)]), (32, [(64, 0)])):
+        with pytest.raises(gpu.CvxError) as e:
+            r.render_patches_u8(pw, xy, 1)
+        assert e.value.status == 1
+
+
 def test_render_after_update_scene_bitexact(room, gpu, orc):
     """Renderer::set_time + update_scene (renderer.rs:134-147) move the camera
     with a per-frame delta (motion blur); the frame equals the oracle's with
