@@ -65,7 +65,10 @@ __global__ void k_prep_lights(const cvx_triangle* __restrict__ tris, const uint3
 }
 
 // ---------------------------------------------------------------------------
-// Nearest hit over SoA rays (Bvh::intersect_nearest, bvh.rs:659)
+// Nearest hit over SoA rays (Bvh::intersect_nearest, bvh.rs:659). The packet
+// form (k_intersect<true>: eight consecutive rays are one reference packet)
+// is the reference's traversal exactly; the single-ray form is
+// k_intersect_refill below.
 
 // Next unit (group or packet) index for the calling octet (one atomic by its lane 0).
 __device__ __forceinline__ uint32_t octet_claim(uint32_t* counter, unsigned omask, int k) {
@@ -443,10 +446,7 @@ cudaError_t launch_intersect(const DeviceScene& s, const float* rays, uint32_t n
     uint32_t need = ((n + 7u) & ~7u) / block + 1u;
     uint32_t blocks = (uint32_t)num_sms() * blocks_per_sm;
     if (blocks > need) blocks = need;
-    if (packet)
-        k_intersect<true><<<blocks, block, 0, st>>>(s, rays, n, far_dist, t_out, tri_out, counters, err);
-    else
-        k_intersect<false><<<blocks, block, 0, st>>>(s, rays, n, far_dist, t_out, tri_out, counters, err);
+    k_intersect<true><<<blocks, block, 0, st>>>(s, rays, n, far_dist, t_out, tri_out, counters, err);
     return cudaGetLastError();
 }
 
