@@ -334,10 +334,15 @@ __global__ void __launch_bounds__(128) k_render_patch(FrameArgs a) {
     const uint32_t pw = (a.w + a.patch - 1u) / a.patch, ph = (a.h + a.patch - 1u) / a.patch;
     const uint32_t n = a.patches ? a.n_patches : pw * ph;
     const uint32_t wb = a.patch / 16u, hb = a.patch / 4u;  // 16x4 blocks across and up a patch
-    const uint32_t octets = (gridDim.x * blockDim.x) >> 3;
+    // One octet per warp: a patch is one long serial chain, so its octet gets a
+    // scheduler slot of its own instead of sharing a warp (and diverging) with
+    // three other patches, and the few hundred chains of a frame spread over
+    // every SM.
+    if ((threadIdx.x & 31u) >= 8u) return;
+    const uint32_t octets = (gridDim.x * blockDim.x) >> 5;
     uint32_t rays = 0;
     bool ok = true;
-    for (uint32_t pi = (blockIdx.x * blockDim.x + threadIdx.x) >> 3; pi < n; pi += octets) {
+    for (uint32_t pi = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; pi < n; pi += octets) {
         uint32_t x0 = a.patches ? a.patches[2 * pi] : (pi / ph) * a.patch;
         uint32_t y0 = a.patches ? a.patches[2 * pi + 1] : (pi % ph) * a.patch;
         LaneRng rng;
@@ -364,7 +369,10 @@ __global__ void __launch_bounds__(128) k_render_patch(FrameArgs a) {
         }
     }
     if (!ok) atomicOr(a.err, kErrStackOverflow);
-    flush_rays(a, rays);
+    // only the warp's first octet is alive here: reduce over it alone
+    unsigned long long v = rays;
+    for (int off = 4; off > 0; off >>= 1) v += __shfl_down_sync(0xffu, v, off, 8);
+    if (k == 0 && v) atomicAdd(a.rays, v);
 }
 
 __global__ void k_resolve(const float* __restrict__ accum, uint32_t npx, float factor, uint32_t* __restrict__ rgba) {
@@ -459,7 +467,7 @@ cudaError_t launch_render(const DeviceScene& s, const DeviceCamera& cam, uint32_
     if (block == 0) block = 128;
     if (patch_order) {
         uint32_t units = patches ? n_patches : ((w + patch - 1) / patch) * ((h + patch - 1) / patch);
-        uint32_t blocks = (units * 8 + block - 1) / block;
+        uint32_t blocks = (units * 32 + block - 1) / block;  // one warp per patch
         if (packet) k_render_patch<true><<<blocks, block, 0, st>>>(a);
         else k_render_patch<false><<<blocks, block, 0, st>>>(a);
     } else {
