@@ -463,87 +463,134 @@ __global__ void __launch_bounds__(kTile) k_uniform_stats(const Tile* __restrict_
     sm_flush(cnt, key, st, tl.slot, tl.axis, tl.axis);
 }
 
-// bvh.rs:218-322: the cheapest split over the three axes, or a leaf.
-__global__ void k_choose(const Slot* __restrict__ slots, uint32_t n_slots, const InterimNode* __restrict__ nodes,
-                         BinStats st, Tsah ts, Decision* __restrict__ dec) {
-    uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= n_slots) return;
+// bvh.rs:218-322: the cheapest split over the three axes, or a leaf. One
+// warp per slot (lane l owns bins l and l + 32):
+// prefix and suffix boxes and counts by warp scans, the candidate costs in
+// parallel, and lane 0 applying the host's first-minimum rule in bin order.
+__device__ __forceinline__ void box_scan_empty(Box& b) {
+    for (int c = 0; c < 3; c++) {
+        b.lo[c] = __int_as_float(0x7f800000);   // +inf
+        b.hi[c] = __int_as_float((int)0xff800000u);  // -inf
+    }
+}
+__device__ __forceinline__ void box_join(Box& a, const Box& b) {
+    for (int c = 0; c < 3; c++) {
+        a.lo[c] = fminf(a.lo[c], b.lo[c]);
+        a.hi[c] = fmaxf(a.hi[c], b.hi[c]);
+    }
+}
+__device__ __forceinline__ Box box_shfl_up(const Box& b, int o) {
+    Box r;
+    for (int c = 0; c < 3; c++) {
+        r.lo[c] = __shfl_up_sync(0xffffffffu, b.lo[c], o);
+        r.hi[c] = __shfl_up_sync(0xffffffffu, b.hi[c], o);
+    }
+    return r;
+}
+__device__ __forceinline__ Box box_shfl_down(const Box& b, int o) {
+    Box r;
+    for (int c = 0; c < 3; c++) {
+        r.lo[c] = __shfl_down_sync(0xffffffffu, b.lo[c], o);
+        r.hi[c] = __shfl_down_sync(0xffffffffu, b.hi[c], o);
+    }
+    return r;
+}
+__device__ __forceinline__ Box box_shfl(const Box& b, int src) {
+    Box r;
+    for (int c = 0; c < 3; c++) {
+        r.lo[c] = __shfl_sync(0xffffffffu, b.lo[c], src);
+        r.hi[c] = __shfl_sync(0xffffffffu, b.hi[c], src);
+    }
+    return r;
+}
+
+__global__ void __launch_bounds__(128) k_choose_warp(const Slot* __restrict__ slots, uint32_t n_slots,
+                                                     const InterimNode* __restrict__ nodes, BinStats st, Tsah ts,
+                                                     Decision* __restrict__ dec) {
+    const int lane = threadIdx.x & 31;
+    const uint32_t k = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (k >= n_slots) return;  // warp-uniform
     Slot s = slots[k];
     Box outer;
     for (int c = 0; c < 3; c++) {
         outer.lo[c] = nodes[s.id].lo[c];
         outer.hi[c] = nodes[s.id].hi[c];
     }
-    float parent_area = area(outer);
+    const float parent_area = area(outer);
     float best_cost = 0.0f;
     bool is_first = true;
     Decision d{3u, 0u, 0u, 1u};
     for (int a = 0; a < 3; a++) {
         const uint32_t* cn = st.count + ((size_t)k * 3 + a) * kBins;
         const uint32_t* ky = st.key + ((size_t)k * 3 + a) * kBins * 6;
-        int first = -1, last = -1, nonempty = 0;
-        for (int b = 0; b < kBins; b++)
-            if (cn[b]) {
-                if (first < 0) first = b + 1;
-                last = b + 1;
-                nonempty++;
+        uint32_t c0 = cn[lane], c1 = cn[lane + 32];
+        unsigned m0 = __ballot_sync(0xffffffffu, c0 != 0u), m1 = __ballot_sync(0xffffffffu, c1 != 0u);
+        int nonempty = __popc(m0) + __popc(m1);
+        if (nonempty <= 1) continue;  // warp-uniform
+        int first = (m0 ? __ffs(m0) - 1 : 32 + __ffs(m1) - 1) + 1;
+        int last = (m1 ? 32 + 31 - __clz(m1) : 31 - __clz(m0)) + 1;
+        Box b0, b1;
+        box_scan_empty(b0);
+        box_scan_empty(b1);
+        if (c0)
+            for (int c = 0; c < 3; c++) {
+                b0.lo[c] = from_okey(ky[6 * lane + c]);
+                b0.hi[c] = from_okey(ky[6 * lane + 3 + c]);
             }
-        if (nonempty <= 1) continue;
-        // Suffix boxes and counts: sfx[i] encloses bins i..63.
-        Box sfx[kBins];
-        uint32_t sc[kBins];
-        Box acc;
-        bool any = false;
-        uint32_t c_acc = 0;
-        for (int b = kBins - 1; b >= 0; b--) {
-            if (cn[b]) {
-                Box bb;
-                for (int c = 0; c < 3; c++) {
-                    bb.lo[c] = from_okey(ky[6 * b + c]);
-                    bb.hi[c] = from_okey(ky[6 * b + 3 + c]);
-                }
-                if (any)
-                    for (int c = 0; c < 3; c++) {
-                        acc.lo[c] = fmin_rs(bb.lo[c], acc.lo[c]);
-                        acc.hi[c] = fmax_rs(bb.hi[c], acc.hi[c]);
-                    }
-                else
-                    acc = bb;
-                any = true;
-                c_acc += cn[b];
+        if (c1)
+            for (int c = 0; c < 3; c++) {
+                b1.lo[c] = from_okey(ky[6 * (lane + 32) + c]);
+                b1.hi[c] = from_okey(ky[6 * (lane + 32) + 3 + c]);
             }
-            sfx[b] = acc;
-            sc[b] = c_acc;
+        // Inclusive prefix (bins 0..b) and suffix (bins b..63) of boxes and counts.
+        Box p0 = b0, p1 = b1, q0 = b0, q1 = b1;
+        uint32_t pc0 = c0, pc1 = c1, qc0 = c0, qc1 = c1;
+        for (int o = 1; o < 32; o <<= 1) {
+            Box u0 = box_shfl_up(p0, o), u1 = box_shfl_up(p1, o);
+            uint32_t uc0 = __shfl_up_sync(0xffffffffu, pc0, o), uc1 = __shfl_up_sync(0xffffffffu, pc1, o);
+            Box v0 = box_shfl_down(q0, o), v1 = box_shfl_down(q1, o);
+            uint32_t vc0 = __shfl_down_sync(0xffffffffu, qc0, o), vc1 = __shfl_down_sync(0xffffffffu, qc1, o);
+            if (lane >= o) {
+                box_join(p0, u0);
+                box_join(p1, u1);
+                pc0 += uc0;
+                pc1 += uc1;
+            }
+            if (lane + o < 32) {
+                box_join(q0, v0);
+                box_join(q1, v1);
+                qc0 += vc0;
+                qc1 += vc1;
+            }
         }
-        Box left;
-        bool lany = false;
-        uint32_t lc = 0;
+        Box lowtot = box_shfl(p0, 31), hightot = box_shfl(q1, 0);
+        uint32_t lowcnt = __shfl_sync(0xffffffffu, pc0, 31), highcnt = __shfl_sync(0xffffffffu, qc1, 0);
+        box_join(p1, lowtot);  // prefix of bins 32 + lane includes all of 0..31
+        pc1 += lowcnt;
+        box_join(q0, hightot);  // suffix of bins lane includes all of 32..63
+        qc0 += highcnt;
+        // Split i = b + 1 puts bins 0..b left and i..63 right: left = prefix(b),
+        // right = suffix(b + 1). Lane l evaluates i = l + 1 and i = l + 33.
+        Box r0 = box_shfl_down(q0, 1), r1 = box_shfl_down(q1, 1);
+        uint32_t rc0 = __shfl_down_sync(0xffffffffu, qc0, 1), rc1 = __shfl_down_sync(0xffffffffu, qc1, 1);
+        Box q1_first = box_shfl(q1, 0);  // suffix(32) for i = 32
+        uint32_t qc1_first = __shfl_sync(0xffffffffu, qc1, 0);
+        if (lane == 31) {
+            r0 = q1_first;
+            rc0 = qc1_first;
+        }
+        int i0 = lane + 1, i1 = lane + 33;
+        float cost0 = 0.0f, cost1 = 0.0f;
+        if (i0 >= first && i0 < last) cost0 = tsah_cost(ts, parent_area, p0, pc0) + tsah_cost(ts, parent_area, r0, rc0);
+        if (i1 >= first && i1 < last) cost1 = tsah_cost(ts, parent_area, p1, pc1) + tsah_cost(ts, parent_area, r1, rc1);
+        // bvh.rs:241-258: the first candidate, then strictly cheaper ones, in bin order.
         float best = 0.0f;
         int at = 0;
         bool first_i = true;
-        for (int b = 0; b < last; b++) {
-            // left: bins 0..b (the split after bin b is i = b + 1)
-            if (cn[b]) {
-                Box bb;
-                for (int c = 0; c < 3; c++) {
-                    bb.lo[c] = from_okey(ky[6 * b + c]);
-                    bb.hi[c] = from_okey(ky[6 * b + 3 + c]);
-                }
-                if (lany)
-                    for (int c = 0; c < 3; c++) {
-                        left.lo[c] = fmin_rs(left.lo[c], bb.lo[c]);
-                        left.hi[c] = fmax_rs(left.hi[c], bb.hi[c]);
-                    }
-                else
-                    left = bb;
-                lany = true;
-                lc += cn[b];
-            }
-            int i = b + 1;
-            if (i < first || i >= last) continue;
-            float cost = tsah_cost(ts, parent_area, left, lc) + tsah_cost(ts, parent_area, sfx[i], sc[i]);
-            if (cost < best || first_i) {
-                best = cost;
+        for (int i = first; i < last; i++) {
+            float c = i <= 32 ? __shfl_sync(0xffffffffu, cost0, i - 1) : __shfl_sync(0xffffffffu, cost1, i - 33);
+            if (c < best || first_i) {
+                best = c;
                 at = i;
                 first_i = false;
             }
@@ -551,13 +598,13 @@ __global__ void k_choose(const Slot* __restrict__ slots, uint32_t n_slots, const
         if (best < best_cost || is_first) {
             best_cost = best;
             is_first = false;
-            uint32_t nl = 0;
-            for (int b = 0; b < at; b++) nl += cn[b];
+            // left count: prefix count of bin at - 1
+            uint32_t nl = at <= 32 ? __shfl_sync(0xffffffffu, pc0, at - 1) : __shfl_sync(0xffffffffu, pc1, at - 33);
             d = Decision{(uint32_t)a, (uint32_t)at, nl, 0u};
         }
     }
     if (is_first || (float)s.cnt * 120.0f < best_cost) d.leaf = 1u;
-    dec[k] = d;
+    if (lane == 0) dec[k] = d;
 }
 
 // Partition of the split slots. Coordinate-binned axis: a stable counting
@@ -1113,7 +1160,7 @@ int32_t bvh_build_device(const cvx_triangle* tris, uint32_t n, cvx_bvh** out) {
             k_uniform_stats<<<(unsigned)uni_tiles.size(), kTile, 0, st>>>(
                 (const Tile*)d_tiles2.p, (uint32_t)uni_tiles.size(), ds, K, R, order, n, srt, bs, misc + 1);
         }
-        k_choose<<<blocks(K, 64), 64, 0, st>>>(ds, K, nodes, bs, ts, (Decision*)d_dec.p);
+        k_choose_warp<<<blocks((size_t)K * 32, 128), 128, 0, st>>>(ds, K, nodes, bs, ts, (Decision*)d_dec.p);
         std::vector<Decision> dec(K);
         BK(cudaMemcpyAsync(dec.data(), d_dec.p, K * sizeof(Decision), cudaMemcpyDeviceToHost, st), "download");
         BK(cudaStreamSynchronize(st), "split choice");
