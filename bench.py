@@ -483,7 +483,8 @@ def _served_run(cg, scs, reqs, sequential, engine=None):
     srv = cg.Server(scs, framebuffer_bytes=24 << 30, max_groups=1 << 21, traversal=cg.TRAVERSE_SINGLE,
                     sequential=sequential, blocks_per_sm=engine.get("blocks_per_sm", 0),
                     refill_mode=engine.get("refill_mode", cg.REFILL_AFTER_CAMERA),
-                    fused_blocks_per_sm=engine.get("fused_blocks_per_sm", 0))
+                    fused_blocks_per_sm=engine.get("fused_blocks_per_sm", 0),
+                    wavefront_streams=engine.get("wavefront_streams", 1))
     # warm-up: one small request per scene
     for k in range(len(scs)):
         srv.wait(srv.submit(k, 64, 64, 1, reqs[0][5]))
@@ -580,7 +581,8 @@ def bench_served(cg, duration=2.0, rate=200.0, seed=4):
     if wf:
         scenes.default_camera(scs[wf[0]].camera)
         best, _ = autotune.tune_wavefront(scs[wf[0]], 1280, 736, frames=3)
-        engine = {"blocks_per_sm": best["blocks_per_sm"], "refill_mode": best["refill_mode"]}
+        engine = {"blocks_per_sm": best["blocks_per_sm"], "refill_mode": best["refill_mode"],
+                  "wavefront_streams": 2}
     served = _served_run(cg, scs, reqs, sequential=False, engine=engine)
     served_default = _served_run(cg, scs, reqs, sequential=False)
     sequential = _served_run(cg, scs, reqs, sequential=True)

@@ -448,7 +448,10 @@ struct cvx_server {
     std::vector<uint32_t> mode;  // per scene: 0 fused, 1 wavefront
     cvx_server_config cfg{};
     WaveEngine engine;  // wavefront
+    WaveEngine engine2;  // second wavefront engine (two_wf): its waves fill the first one's bounce tails
     WaveEngine fused;
+    bool two_wf = false;
+    cudaStream_t stream3 = nullptr;
     cudaStream_t stream2 = nullptr;
     float* d_accum = nullptr;
     uint32_t* d_rgba = nullptr;
@@ -524,8 +527,11 @@ struct cvx_server {
                 wave = admitted;
             }
             if (wave.empty()) continue;
-            std::vector<Job> sub[2];
-            std::vector<size_t> where[2];
+            // sub[0]: single-launch jobs; sub[1], sub[2]: wavefront jobs of the
+            // first and the second wavefront engine (balanced by groups).
+            std::vector<Job> sub[3];
+            std::vector<size_t> where[3];
+            uint64_t wf_groups[2] = {0, 0};
             for (size_t i = 0; i < wave.size(); i++) {
                 auto& q = wave[i];
                 Job j{};
@@ -536,27 +542,35 @@ struct cvx_server {
                 j.frame = q->r.frame_base + q->next_sample;
                 j.out_offset = q->offset;
                 uint32_t m = mode[q->r.scene];
+                if (m == 1 && two_wf && wf_groups[1] < wf_groups[0]) m = 2;
+                if (m) wf_groups[m - 1] += groups_of(j.w, j.h);
                 sub[m].push_back(j);
                 where[m].push_back(i);
             }
-            // A request's accumulator starts at zero with its first sample.
-            for (auto& q : wave)
-                if (q->next_sample == 0)
-                    cudaMemsetAsync(d_accum + 3 * q->offset, 0, q->npx * 12, mode[q->r.scene] ? stream : stream2);
+            cudaStream_t sub_stream[3] = {stream2, stream, stream3};
+            // A request's accumulator starts at zero with its first sample, on
+            // the stream that renders it.
+            for (int m = 0; m < 3; m++)
+                for (size_t k : where[m])
+                    if (wave[k]->next_sample == 0)
+                        cudaMemsetAsync(d_accum + 3 * wave[k]->offset, 0, wave[k]->npx * 12, sub_stream[m]);
             WaveOutputs out{};
             out.accum = d_accum;
-            uint64_t r = 0, r0 = 0, r1 = 0;
-            float ms = 0.0f, ms0 = 0.0f, ms1 = 0.0f;
-            std::vector<uint64_t> jr[2];
+            uint64_t r = 0, r0 = 0, r1 = 0, r2 = 0;
+            float ms = 0.0f, ms0 = 0.0f, ms1 = 0.0f, ms2 = 0.0f;
+            std::vector<uint64_t> jr[3];
             int32_t st = fused.submit(sub[0], out, stream2, true);
             if (!st) st = engine.submit(sub[1], out, stream, true);
+            if (!st && two_wf) st = engine2.submit(sub[2], out, stream3, true);
             int32_t st0 = fused.collect(stream2, &r0, &jr[0], &ms0);
             int32_t st1 = engine.collect(stream, &r1, &jr[1], &ms1);
-            if (!st) st = st0 ? st0 : st1;
-            r = r0 + r1;
+            int32_t st2 = two_wf ? engine2.collect(stream3, &r2, &jr[2], &ms2) : CVX_OK;
+            if (!st) st = st0 ? st0 : st1 ? st1 : st2;
+            r = r0 + r1 + r2;
+            if (ms2 > ms1) ms1 = ms2;
             ms = ms0 > ms1 ? ms0 : ms1;
             job_rays.assign(wave.size(), 0);
-            for (int m = 0; m < 2; m++)
+            for (int m = 0; m < 3; m++)
                 for (size_t k = 0; k < where[m].size() && k < jr[m].size(); k++) job_rays[where[m][k]] = jr[m][k];
             std::vector<std::shared_ptr<Request>> done;
             std::vector<ResolveItem> items;
@@ -623,6 +637,7 @@ struct cvx_server {
         cudaFree(d_items);
         if (stream) cudaStreamDestroy(stream);
         if (stream2) cudaStreamDestroy(stream2);
+        if (stream3) cudaStreamDestroy(stream3);
     }
 };
 
@@ -651,6 +666,14 @@ extern "C" int32_t cvx_server_create(cvx_scene* const* scenes, uint32_t n_scenes
         return st;
     if ((st = s->engine.set_scenes(scenes, n_scenes))) return st;
     if ((st = s->fused.set_scenes(scenes, n_scenes))) return st;
+    if (cfg->wavefront_streams >= 2) {
+        s->two_wf = true;
+        ECK(cudaStreamCreateWithPriority(&s->stream3, cudaStreamNonBlocking, greatest), "cudaStreamCreate");
+        if ((st = s->engine2.init(cfg->max_groups, 1024, cfg->traversal == CVX_TRAVERSE_PACKET, cfg->use_graph != 0,
+                                  cfg->blocks_per_sm, refill_from(cfg->refill_mode))))
+            return st;
+        if ((st = s->engine2.set_scenes(scenes, n_scenes))) return st;
+    }
     for (uint32_t i = 0; i < n_scenes; i++)
         s->mode.push_back(cfg->kernel_mode == 1 ? 0u : cfg->kernel_mode == 2 ? 1u : default_scene_mode(scenes[i]));
     s->pool_px = cfg->framebuffer_bytes / 16;  // 12 B accumulator + 4 B RGBA per pixel

@@ -128,15 +128,16 @@ def test_server_mix_equals_alone(two_scenes, gpu, kernel_mode):
         srv.close()
 
 
-def test_server_two_engines_concurrent_equal_alone(two_scenes, gpu):
+@pytest.mark.parametrize("wavefront_streams", [1, 2])
+def test_server_two_engines_concurrent_equal_alone(two_scenes, gpu, wavefront_streams):
     """One scene in single-launch waves and one in wavefront waves, run
     concurrently on two streams (the wavefront one at higher priority) with a
     reduced single-launch block count: every image equals the same request
     rendered alone, and both engines report device time."""
     scs = [s for _, s, _ in two_scenes]
     srv = gpu.Server(scs, framebuffer_bytes=64 << 20, max_groups=1 << 14, fused_blocks_per_sm=4,
-                     blocks_per_sm=10, refill_mode=gpu.REFILL_ALL)
-    srv.set_scene_mode(0, gpu.MODE_MEGAKERNEL)
+                     blocks_per_sm=10, refill_mode=gpu.REFILL_ALL, wavefront_streams=wavefront_streams)
+    srv.set_scene_mode(0, gpu.MODE_MEGAKERNEL if wavefront_streams == 1 else gpu.MODE_WAVEFRONT)
     srv.set_scene_mode(1, gpu.MODE_WAVEFRONT)
     rng = np.random.default_rng(8)
     reqs, ids = [], []
@@ -152,7 +153,8 @@ def test_server_two_engines_concurrent_equal_alone(two_scenes, gpu):
         assert st == 0
         assert (img == _alone(gpu, scs[sc], gpu.View(sc, w, h, spp, 7 * i, cam))).all()
     stats = srv.stats()
-    assert stats["fused_busy_s"] > 0.0 and stats["wavefront_busy_s"] > 0.0
+    assert stats["wavefront_busy_s"] > 0.0
+    assert (stats["fused_busy_s"] > 0.0) == (wavefront_streams == 1)
     srv.close()
 
 
