@@ -405,6 +405,8 @@ struct Request {
     uint32_t groups = 0;
     uint64_t offset = 0;  // pixel offset in the framebuffer pool
     uint32_t next_sample = 0;
+    int eng = -1;            // engine it is rendered on: 0 single-launch, 1 and 2 wavefront
+    bool in_flight = false;  // a sample of it is on the GPU
     bool admitted = false, finished = false, cancelled = false;
     cvx_request_result res{};
 };
@@ -465,7 +467,9 @@ struct cvx_server {
     std::vector<std::shared_ptr<Request>> admitted;
     std::unordered_map<uint64_t, std::shared_ptr<Request>> all;
     uint64_t next_id = 1;
-    uint32_t admitted_groups = 0;
+    uint32_t eng_groups[3] = {0, 0, 0};  // ray-queue groups admitted per engine
+    uint32_t eng_jobs[3] = {0, 0, 0};
+    uint64_t arrivals = 0;  // bumped by submissions, cancellations and finished waves
     bool stop = false;
     std::thread worker;
     Clock::time_point t0 = Clock::now();
@@ -483,40 +487,147 @@ struct cvx_server {
         q->res.done_s = now();
         if (q->admitted) {
             pool.give(q->offset, q->npx);
-            admitted_groups -= q->groups;
+            eng_groups[q->eng] -= q->groups;
+            eng_jobs[q->eng]--;
             q->admitted = false;
         }
     }
 
-    void loop() {
+    // The engines and their streams: 0 single-launch (low priority), 1 and 2
+    // wavefront (high priority; 2 only with two_wf).
+    WaveEngine* eng_of(int e) { return e == 0 ? &fused : e == 1 ? &engine : &engine2; }
+    cudaStream_t stream_of(int e) const { return e == 0 ? stream2 : e == 1 ? stream : stream3; }
+
+    // Under mu. Admits pending requests in FIFO order while they fit; a
+    // request is bound to one engine, so its samples run in order.
+    void admit() {
+        while (!pending.empty()) {
+            auto& q = pending.front();
+            if (cfg.sequential && !admitted.empty()) break;
+            int e = mode[q->r.scene] == 0 ? 0 : (two_wf && eng_groups[2] < eng_groups[1] ? 2 : 1);
+            uint32_t qg = e ? q->groups : 0u;
+            uint64_t off = 0;
+            if (eng_groups[e] + qg > eng_of(e)->max_groups() || eng_jobs[e] >= eng_of(e)->max_jobs() ||
+                !pool.take(q->npx, &off))
+                break;
+            q->offset = off;
+            q->admitted = true;
+            q->eng = e;
+            q->res.start_s = now();
+            q->groups = qg;
+            eng_groups[e] += qg;
+            eng_jobs[e]++;
+            admitted.push_back(q);
+            pending.pop_front();
+        }
+    }
+
+    // Queues the next sample of each request in `reqs` as one wave on engine e.
+    int32_t submit_wave(int e, const std::vector<std::shared_ptr<Request>>& reqs) {
         std::vector<Job> jobs;
-        std::vector<std::shared_ptr<Request>> wave;
-        std::vector<uint64_t> job_rays;
+        jobs.reserve(reqs.size());
+        cudaStream_t st = stream_of(e);
+        for (auto& q : reqs) {
+            Job j{};
+            std::memcpy(&j.cam, &q->r.camera, sizeof(cvx_camera));
+            j.scene = q->r.scene;
+            j.w = q->r.width;
+            j.h = q->r.height;
+            j.frame = q->r.frame_base + q->next_sample;
+            j.out_offset = q->offset;
+            jobs.push_back(j);
+            // a request's accumulator starts at zero with its first sample
+            if (q->next_sample == 0) cudaMemsetAsync(d_accum + 3 * q->offset, 0, q->npx * 12, st);
+        }
+        WaveOutputs out{};
+        out.accum = d_accum;
+        return eng_of(e)->submit(jobs, out, st, true);
+    }
+
+    // Engine e's wave over `reqs` has ended with status st: account for it,
+    // resolve and copy out the requests that have all their samples.
+    void complete(int e, const std::vector<std::shared_ptr<Request>>& reqs, int32_t st) {
+        uint64_t r = 0;
+        float ms = 0.0f;
+        std::vector<uint64_t> jr;
+        int32_t cst = eng_of(e)->collect(stream_of(e), &r, &jr, &ms);
+        if (!st) st = cst;
+        std::vector<std::shared_ptr<Request>> done;
+        std::vector<ResolveItem> items;
+        {
+            std::lock_guard<std::mutex> lk(mu);
+            waves++;
+            rays += r;
+            (e == 0 ? busy_fused_s : busy_wavefront_s) += ms * 1e-3;
+            for (size_t i = 0; i < reqs.size(); i++) {
+                auto& q = reqs[i];
+                q->in_flight = false;
+                if (st) {
+                    if (!q->finished) {
+                        finish(q, st);
+                        admitted.erase(std::find(admitted.begin(), admitted.end(), q));
+                    }
+                    continue;
+                }
+                q->res.rays += i < jr.size() ? jr[i] : 0;
+                q->next_sample++;
+                if (q->next_sample == q->r.spp && !q->cancelled) {
+                    done.push_back(q);
+                    items.push_back(ResolveItem{q->offset, (uint32_t)q->npx, 1.0f / (float)q->r.spp});
+                }
+            }
+            if (st) {
+                char buf[256];
+                cvx_last_error(buf, sizeof buf);
+                fatal_msg = buf;
+            }
+            arrivals++;  // the loop re-checks admission: memory or queue space may have freed
+        }
+        if (!done.empty()) {
+            cudaStream_t rs = stream_of(e);
+            ResolveItem* di = d_items + 1024 * e;  // each engine resolves through its own item list
+            cudaError_t ce = cudaMemcpyAsync(di, items.data(), items.size() * sizeof(ResolveItem),
+                                             cudaMemcpyHostToDevice, rs);
+            if (ce == cudaSuccess) ce = launch_resolve_multi(di, (uint32_t)items.size(), d_accum, d_rgba, rs);
+            for (auto& q : done)
+                if (ce == cudaSuccess && q->host_rgba)
+                    ce = cudaMemcpyAsync(q->host_rgba, d_rgba + q->offset, q->npx * 4, cudaMemcpyDeviceToHost, rs);
+            if (ce == cudaSuccess) ce = cudaStreamSynchronize(rs);
+            std::lock_guard<std::mutex> lk(mu);
+            for (auto& q : done) {
+                finish(q, ce == cudaSuccess ? CVX_OK : CVX_ERR_CUDA);
+                admitted.erase(std::find(admitted.begin(), admitted.end(), q));
+            }
+        }
+        std::lock_guard<std::mutex> lk(mu);
+        done_cv.notify_all();
+    }
+
+    // The request loop. Each engine has at most one wave on the GPU; an
+    // engine whose wave ends starts its next one at once, without waiting
+    // for the others, so the engines run out of phase and each fills SMs the
+    // others leave idle (bounce tails, the gaps between launches). The host
+    // waits by polling completion events (no GPU-side waiting).
+    void loop() {
+        struct Flight {
+            bool busy = false;
+            std::vector<std::shared_ptr<Request>> reqs;
+            cudaEvent_t done = nullptr;
+        } fl[3];
+        for (auto& f : fl) cudaEventCreateWithFlags(&f.done, cudaEventDisableTiming);
+        int n_busy = 0;
+        double busy_from = 0.0;
+        uint64_t seen = 0;
         for (;;) {
+            std::vector<std::shared_ptr<Request>> start[3];
             {
                 std::unique_lock<std::mutex> lk(mu);
-                cv.wait(lk, [&] { return stop || !pending.empty() || !admitted.empty(); });
-                if (stop) return;
-                // Admission, FIFO: stop at the first request that does not fit
-                // (framebuffer pool; ray queues of wavefront-mode scenes).
-                while (!pending.empty()) {
-                    auto& q = pending.front();
-                    if (cfg.sequential && !admitted.empty()) break;
-                    uint64_t off = 0;
-                    uint32_t qg = mode[q->r.scene] ? q->groups : 0u;
-                    if (admitted_groups + qg > engine.max_groups() || admitted.size() >= engine.max_jobs() ||
-                        !pool.take(q->npx, &off))
-                        break;
-                    q->offset = off;
-                    q->admitted = true;
-                    q->res.start_s = now();
-                    q->groups = qg;
-                    admitted_groups += qg;
-                    admitted.push_back(q);
-                    pending.pop_front();
-                }
+                if (n_busy == 0) cv.wait(lk, [&] { return stop || !pending.empty() || !admitted.empty(); });
+                if (stop) break;
+                seen = arrivals;
+                admit();
                 for (auto it = admitted.begin(); it != admitted.end();) {
-                    if ((*it)->cancelled) {
+                    if ((*it)->cancelled && !(*it)->in_flight) {
                         finish(*it, CVX_ERR_CANCELLED);
                         it = admitted.erase(it);
                     } else {
@@ -524,105 +635,53 @@ struct cvx_server {
                     }
                 }
                 done_cv.notify_all();
-                wave = admitted;
+                for (int e = 0; e < 3; e++)
+                    if (!fl[e].busy)
+                        for (auto& q : admitted)
+                            if (q->eng == e && !q->in_flight) {
+                                q->in_flight = true;
+                                start[e].push_back(q);
+                            }
             }
-            if (wave.empty()) continue;
-            // sub[0]: single-launch jobs; sub[1], sub[2]: wavefront jobs of the
-            // first and the second wavefront engine (balanced by groups).
-            std::vector<Job> sub[3];
-            std::vector<size_t> where[3];
-            uint64_t wf_groups[2] = {0, 0};
-            for (size_t i = 0; i < wave.size(); i++) {
-                auto& q = wave[i];
-                Job j{};
-                std::memcpy(&j.cam, &q->r.camera, sizeof(cvx_camera));
-                j.scene = q->r.scene;
-                j.w = q->r.width;
-                j.h = q->r.height;
-                j.frame = q->r.frame_base + q->next_sample;
-                j.out_offset = q->offset;
-                uint32_t m = mode[q->r.scene];
-                if (m == 1 && two_wf && wf_groups[1] < wf_groups[0]) m = 2;
-                if (m) wf_groups[m - 1] += groups_of(j.w, j.h);
-                sub[m].push_back(j);
-                where[m].push_back(i);
-            }
-            cudaStream_t sub_stream[3] = {stream2, stream, stream3};
-            // A request's accumulator starts at zero with its first sample, on
-            // the stream that renders it.
-            for (int m = 0; m < 3; m++)
-                for (size_t k : where[m])
-                    if (wave[k]->next_sample == 0)
-                        cudaMemsetAsync(d_accum + 3 * wave[k]->offset, 0, wave[k]->npx * 12, sub_stream[m]);
-            WaveOutputs out{};
-            out.accum = d_accum;
-            uint64_t r = 0, r0 = 0, r1 = 0, r2 = 0;
-            float ms = 0.0f, ms0 = 0.0f, ms1 = 0.0f, ms2 = 0.0f;
-            std::vector<uint64_t> jr[3];
-            int32_t st = fused.submit(sub[0], out, stream2, true);
-            if (!st) st = engine.submit(sub[1], out, stream, true);
-            if (!st && two_wf) st = engine2.submit(sub[2], out, stream3, true);
-            int32_t st0 = fused.collect(stream2, &r0, &jr[0], &ms0);
-            int32_t st1 = engine.collect(stream, &r1, &jr[1], &ms1);
-            int32_t st2 = two_wf ? engine2.collect(stream3, &r2, &jr[2], &ms2) : CVX_OK;
-            if (!st) st = st0 ? st0 : st1 ? st1 : st2;
-            r = r0 + r1 + r2;
-            if (ms2 > ms1) ms1 = ms2;
-            ms = ms0 > ms1 ? ms0 : ms1;
-            job_rays.assign(wave.size(), 0);
-            for (int m = 0; m < 3; m++)
-                for (size_t k = 0; k < where[m].size() && k < jr[m].size(); k++) job_rays[where[m][k]] = jr[m][k];
-            std::vector<std::shared_ptr<Request>> done;
-            std::vector<ResolveItem> items;
-            {
-                std::lock_guard<std::mutex> lk(mu);
-                waves++;
-                rays += r;
-                busy_s += ms * 1e-3;
-                busy_fused_s += ms0 * 1e-3;
-                busy_wavefront_s += ms1 * 1e-3;
-                for (size_t i = 0; i < wave.size(); i++) {
-                    auto& q = wave[i];
-                    if (st) {
-                        if (!q->finished) {
-                            finish(q, st);
-                            admitted.erase(std::find(admitted.begin(), admitted.end(), q));
-                        }
-                        continue;
-                    }
-                    q->res.rays += job_rays.empty() ? 0 : job_rays[i];
-                    q->next_sample++;
-                    if (q->next_sample == q->r.spp && !q->cancelled) {
-                        done.push_back(q);
-                        items.push_back(ResolveItem{q->offset, (uint32_t)q->npx, 1.0f / (float)q->r.spp});
-                    }
-                }
+            for (int e = 0; e < 3; e++) {
+                if (start[e].empty()) continue;
+                int32_t st = submit_wave(e, start[e]);
                 if (st) {
-                    char buf[256];
-                    cvx_last_error(buf, sizeof buf);
-                    fatal_msg = buf;
+                    complete(e, start[e], st);
+                    continue;
                 }
+                cudaEventRecord(fl[e].done, stream_of(e));
+                fl[e].busy = true;
+                fl[e].reqs = std::move(start[e]);
+                if (n_busy++ == 0) busy_from = now();
             }
-            if (!done.empty()) {
-                cudaError_t e = cudaMemcpyAsync(d_items, items.data(), items.size() * sizeof(ResolveItem),
-                                                cudaMemcpyHostToDevice, stream);
-                if (e == cudaSuccess) e = launch_resolve_multi(d_items, (uint32_t)items.size(), d_accum, d_rgba, stream);
-                for (auto& q : done)
-                    if (e == cudaSuccess && q->host_rgba)
-                        e = cudaMemcpyAsync(q->host_rgba, d_rgba + q->offset, q->npx * 4, cudaMemcpyDeviceToHost,
-                                            stream);
-                if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
-                std::lock_guard<std::mutex> lk(mu);
-                for (auto& q : done) {
-                    finish(q, e == cudaSuccess ? CVX_OK : CVX_ERR_CUDA);
-                    admitted.erase(std::find(admitted.begin(), admitted.end(), q));
+            if (n_busy == 0) continue;
+            // Wait for an engine to finish, or for new work an idle engine could take.
+            for (;;) {
+                bool ready = false;
+                for (auto& f : fl)
+                    if (f.busy && cudaEventQuery(f.done) != cudaErrorNotReady) ready = true;
+                if (ready) break;
+                {
+                    std::lock_guard<std::mutex> lk(mu);
+                    if (stop || arrivals != seen) break;
                 }
-                done_cv.notify_all();
-            } else if (st) {
-                std::lock_guard<std::mutex> lk(mu);
-                done_cv.notify_all();
+                std::this_thread::sleep_for(std::chrono::microseconds(20));
+            }
+            for (int e = 0; e < 3; e++) {
+                if (!fl[e].busy || cudaEventQuery(fl[e].done) == cudaErrorNotReady) continue;
+                fl[e].busy = false;
+                complete(e, fl[e].reqs, CVX_OK);
+                fl[e].reqs.clear();
+                if (--n_busy == 0) {
+                    std::lock_guard<std::mutex> lk(mu);
+                    busy_s += now() - busy_from;
+                }
             }
         }
+        for (int e = 0; e < 3; e++)
+            if (fl[e].busy) cudaStreamSynchronize(stream_of(e));
+        for (auto& f : fl) cudaEventDestroy(f.done);
     }
 
     ~cvx_server() {
@@ -680,7 +739,7 @@ extern "C" int32_t cvx_server_create(cvx_scene* const* scenes, uint32_t n_scenes
     std::vector<void*> owned;
     if ((st = alloc(&s->d_accum, s->pool_px * 3, owned))) return st;
     if ((st = alloc(&s->d_rgba, s->pool_px, owned))) return st;
-    if ((st = alloc(&s->d_items, 1024, owned))) return st;
+    if ((st = alloc(&s->d_items, 3 * 1024, owned))) return st;
     s->pool.init(s->pool_px);
     s->worker = std::thread([p = s.get()] { p->loop(); });
     *out = s.release();
@@ -704,6 +763,7 @@ extern "C" int32_t cvx_server_submit(cvx_server* s, const cvx_request* req, uint
         q->res.submit_s = s->now();
         s->pending.push_back(q);
         s->all[q->id] = q;
+        s->arrivals++;
         *id = q->id;
     }
     s->cv.notify_all();
@@ -732,6 +792,7 @@ extern "C" int32_t cvx_server_cancel(cvx_server* s, uint64_t id) {
     auto q = it->second;
     if (q->finished) return CVX_OK;
     q->cancelled = true;
+    s->arrivals++;
     auto p = std::find(s->pending.begin(), s->pending.end(), q);
     if (p != s->pending.end()) {
         s->pending.erase(p);
