@@ -450,10 +450,13 @@ struct cvx_server {
     std::vector<uint32_t> mode;  // per scene: 0 fused, 1 wavefront
     cvx_server_config cfg{};
     WaveEngine engine;  // wavefront
-    WaveEngine engine2;  // second wavefront engine (two_wf): its waves fill the first one's bounce tails
+    // further wavefront engines (wavefront_streams > 1): their waves fill the
+    // first one's bounce tails
+    static constexpr int kMaxEngines = 5;  // the single-launch engine and up to 4 wavefront engines
+    WaveEngine extra_wf[kMaxEngines - 2];
+    cudaStream_t extra_stream[kMaxEngines - 2] = {nullptr, nullptr, nullptr};
+    int n_wf = 1;
     WaveEngine fused;
-    bool two_wf = false;
-    cudaStream_t stream3 = nullptr;
     cudaStream_t stream2 = nullptr;
     float* d_accum = nullptr;
     uint32_t* d_rgba = nullptr;
@@ -467,8 +470,8 @@ struct cvx_server {
     std::vector<std::shared_ptr<Request>> admitted;
     std::unordered_map<uint64_t, std::shared_ptr<Request>> all;
     uint64_t next_id = 1;
-    uint32_t eng_groups[3] = {0, 0, 0};  // ray-queue groups admitted per engine
-    uint32_t eng_jobs[3] = {0, 0, 0};
+    uint32_t eng_groups[kMaxEngines] = {};  // ray-queue groups admitted per engine
+    uint32_t eng_jobs[kMaxEngines] = {};
     uint64_t arrivals = 0;  // bumped by submissions, cancellations and finished waves
     bool stop = false;
     std::thread worker;
@@ -493,10 +496,10 @@ struct cvx_server {
         }
     }
 
-    // The engines and their streams: 0 single-launch (low priority), 1 and 2
-    // wavefront (high priority; 2 only with two_wf).
-    WaveEngine* eng_of(int e) { return e == 0 ? &fused : e == 1 ? &engine : &engine2; }
-    cudaStream_t stream_of(int e) const { return e == 0 ? stream2 : e == 1 ? stream : stream3; }
+    // The engines and their streams: 0 single-launch (low priority), 1 .. n_wf
+    // wavefront (high priority).
+    WaveEngine* eng_of(int e) { return e == 0 ? &fused : e == 1 ? &engine : &extra_wf[e - 2]; }
+    cudaStream_t stream_of(int e) const { return e == 0 ? stream2 : e == 1 ? stream : extra_stream[e - 2]; }
 
     // Under mu. Admits pending requests in FIFO order while they fit; a
     // request is bound to one engine, so its samples run in order.
@@ -504,7 +507,12 @@ struct cvx_server {
         while (!pending.empty()) {
             auto& q = pending.front();
             if (cfg.sequential && !admitted.empty()) break;
-            int e = mode[q->r.scene] == 0 ? 0 : (two_wf && eng_groups[2] < eng_groups[1] ? 2 : 1);
+            int e = 0;
+            if (mode[q->r.scene] != 0) {  // the wavefront engine with the fewest admitted groups
+                e = 1;
+                for (int k = 2; k <= n_wf; k++)
+                    if (eng_groups[k] < eng_groups[e]) e = k;
+            }
             uint32_t qg = e ? q->groups : 0u;
             uint64_t off = 0;
             if (eng_groups[e] + qg > eng_of(e)->max_groups() || eng_jobs[e] >= eng_of(e)->max_jobs() ||
@@ -613,13 +621,13 @@ struct cvx_server {
             bool busy = false;
             std::vector<std::shared_ptr<Request>> reqs;
             cudaEvent_t done = nullptr;
-        } fl[3];
+        } fl[kMaxEngines];
         for (auto& f : fl) cudaEventCreateWithFlags(&f.done, cudaEventDisableTiming);
         int n_busy = 0;
         double busy_from = 0.0;
         uint64_t seen = 0;
         for (;;) {
-            std::vector<std::shared_ptr<Request>> start[3];
+            std::vector<std::shared_ptr<Request>> start[kMaxEngines];
             {
                 std::unique_lock<std::mutex> lk(mu);
                 if (n_busy == 0) cv.wait(lk, [&] { return stop || !pending.empty() || !admitted.empty(); });
@@ -635,7 +643,7 @@ struct cvx_server {
                     }
                 }
                 done_cv.notify_all();
-                for (int e = 0; e < 3; e++)
+                for (int e = 0; e <= n_wf; e++)
                     if (!fl[e].busy)
                         for (auto& q : admitted)
                             if (q->eng == e && !q->in_flight) {
@@ -643,7 +651,7 @@ struct cvx_server {
                                 start[e].push_back(q);
                             }
             }
-            for (int e = 0; e < 3; e++) {
+            for (int e = 0; e <= n_wf; e++) {
                 if (start[e].empty()) continue;
                 int32_t st = submit_wave(e, start[e]);
                 if (st) {
@@ -668,7 +676,7 @@ struct cvx_server {
                 }
                 std::this_thread::sleep_for(std::chrono::microseconds(20));
             }
-            for (int e = 0; e < 3; e++) {
+            for (int e = 0; e <= n_wf; e++) {
                 if (!fl[e].busy || cudaEventQuery(fl[e].done) == cudaErrorNotReady) continue;
                 fl[e].busy = false;
                 complete(e, fl[e].reqs, CVX_OK);
@@ -679,7 +687,7 @@ struct cvx_server {
                 }
             }
         }
-        for (int e = 0; e < 3; e++)
+        for (int e = 0; e <= n_wf; e++)
             if (fl[e].busy) cudaStreamSynchronize(stream_of(e));
         for (auto& f : fl) cudaEventDestroy(f.done);
     }
@@ -696,7 +704,8 @@ struct cvx_server {
         cudaFree(d_items);
         if (stream) cudaStreamDestroy(stream);
         if (stream2) cudaStreamDestroy(stream2);
-        if (stream3) cudaStreamDestroy(stream3);
+        for (cudaStream_t x : extra_stream)
+            if (x) cudaStreamDestroy(x);
     }
 };
 
@@ -725,13 +734,16 @@ extern "C" int32_t cvx_server_create(cvx_scene* const* scenes, uint32_t n_scenes
         return st;
     if ((st = s->engine.set_scenes(scenes, n_scenes))) return st;
     if ((st = s->fused.set_scenes(scenes, n_scenes))) return st;
-    if (cfg->wavefront_streams >= 2) {
-        s->two_wf = true;
-        ECK(cudaStreamCreateWithPriority(&s->stream3, cudaStreamNonBlocking, greatest), "cudaStreamCreate");
-        if ((st = s->engine2.init(cfg->max_groups, 1024, cfg->traversal == CVX_TRAVERSE_PACKET, cfg->use_graph != 0,
-                                  cfg->blocks_per_sm, refill_from(cfg->refill_mode))))
+    if (cfg->wavefront_streams > (uint32_t)cvx_server::kMaxEngines - 1)
+        return set_error(CVX_ERR_INVALID, "at most 4 wavefront streams");
+    for (uint32_t k = 1; k < cfg->wavefront_streams; k++) {
+        ECK(cudaStreamCreateWithPriority(&s->extra_stream[k - 1], cudaStreamNonBlocking, greatest),
+            "cudaStreamCreate");
+        if ((st = s->extra_wf[k - 1].init(cfg->max_groups, 1024, cfg->traversal == CVX_TRAVERSE_PACKET,
+                                          cfg->use_graph != 0, cfg->blocks_per_sm, refill_from(cfg->refill_mode))))
             return st;
-        if ((st = s->engine2.set_scenes(scenes, n_scenes))) return st;
+        if ((st = s->extra_wf[k - 1].set_scenes(scenes, n_scenes))) return st;
+        s->n_wf = (int)k + 1;
     }
     for (uint32_t i = 0; i < n_scenes; i++)
         s->mode.push_back(cfg->kernel_mode == 1 ? 0u : cfg->kernel_mode == 2 ? 1u : default_scene_mode(scenes[i]));
@@ -739,7 +751,7 @@ extern "C" int32_t cvx_server_create(cvx_scene* const* scenes, uint32_t n_scenes
     std::vector<void*> owned;
     if ((st = alloc(&s->d_accum, s->pool_px * 3, owned))) return st;
     if ((st = alloc(&s->d_rgba, s->pool_px, owned))) return st;
-    if ((st = alloc(&s->d_items, 3 * 1024, owned))) return st;
+    if ((st = alloc(&s->d_items, (size_t)cvx_server::kMaxEngines * 1024, owned))) return st;
     s->pool.init(s->pool_px);
     s->worker = std::thread([p = s.get()] { p->loop(); });
     *out = s.release();

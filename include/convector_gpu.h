@@ -293,8 +293,9 @@ typedef struct cvx_server_config {
     uint32_t refill_mode;       /* CVX_REFILL_* */
     uint32_t kernel_mode;       /* 0: per scene as CVX_MODE_AUTO; 1: all fused; 2: all wavefront */
     uint32_t fused_blocks_per_sm; /* blocks per SM of the single-launch waves (0: 16) */
-    uint32_t wavefront_streams; /* 2: split each wave's wavefront jobs over two engines on two
-                                   streams, whose bounce kernels fill each other's tails (0, 1: one) */
+    uint32_t wavefront_streams; /* wavefront engines, each on its own stream (0, 1: one; at most
+                                   4): requests are spread over them and their waves, running
+                                   out of phase, fill each other's bounce tails */
 } cvx_server_config;
 
 typedef struct cvx_request {
