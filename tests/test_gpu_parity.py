@@ -58,6 +58,55 @@ def test_intersect_bitexact(icosphere, orc, traversal):
     assert (tri >= 0).mean() > 0.5
 
 
+@pytest.mark.parametrize("traversal", [0, 1])
+def test_intersect_origins_on_box_planes_bitexact(icosphere, orc, traversal):
+    """Rays starting exactly on node bound planes (zero plane distances, so
+    0 * inf and signed-zero slab distances), with unit directions and with
+    length-3 ones: hits equal the oracle's bit for bit."""
+    bvh, scene, osc = icosphere
+    rng = np.random.default_rng(31)
+    nodes = bvh.nodes_f32[2:]
+    pick = nodes[rng.integers(0, nodes.shape[0], 1 << 15)]
+    o = rng.uniform(pick[:, 0:3], pick[:, 3:6]).astype(np.float32)
+    axis = rng.integers(0, 3, o.shape[0])
+    side = rng.integers(0, 2, o.shape[0])
+    o[np.arange(o.shape[0]), axis] = pick[np.arange(o.shape[0]), axis + 3 * side]
+    d = rng.normal(size=o.shape).astype(np.float32)
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    d[::4] *= np.float32(3.0)  # |d| = 3: reciprocals near 1/3
+    d = d.astype(np.float32)
+    t, tri = scene.intersect_nearest(o, d, traversal=traversal)
+    ot, otri = osc.intersect(o, d, mode=traversal)
+    assert (tri == otri).all(), np.nonzero(tri != otri)[0][:10]
+    assert (t.view(np.uint32) == ot.view(np.uint32)).all()
+
+
+def test_intersect_negative_zero_bounds_bitexact(gpu, orc):
+    """Leaf bounds at -0 (triangles touching a coordinate plane at a -0
+    vertex): the slab test's signed-zero min/max order matches the oracle's."""
+    rng = np.random.default_rng(12)
+    c = rng.uniform(-1.0, 1.0, (2000, 1, 3))
+    v = (c + rng.normal(0.0, 0.04, (2000, 3, 3))).astype(np.float32)
+    # Every fifth triangle touches the x = 0 plane from above at a -0 vertex,
+    # every seventh the z = 0 plane from below: leaf bounds at -0.
+    v[::5, :, 0] = np.abs(v[::5, :, 0])
+    v[::5, 0, 0] = np.float32(-0.0)
+    v[::7, :, 2] = -np.abs(v[::7, :, 2])
+    v[::7, 1, 2] = np.float32(-0.0)
+    t16 = np.zeros((2000, 16), np.float32)
+    t16[:, :9] = v.reshape(-1, 9)
+    w = t16.view(np.uint32)
+    w[:, 15] = 0x00FFFFFF
+    bvh = gpu.Bvh.build(w)
+    scene = gpu.Scene(bvh)
+    osc = orc.OracleScene.from_bvh(bvh)
+    o, d = scenes.random_rays(1 << 14, seed=3)
+    o = (o * np.float32(0.3)).astype(np.float32)
+    t, tri = scene.intersect_nearest(o, d, traversal=1)
+    ot, otri = osc.intersect(o, d, mode=1)
+    assert (tri == otri).all() and (t.view(np.uint32) == ot.view(np.uint32)).all()
+
+
 @pytest.mark.parametrize("launch", [8, 10, 12])
 def test_intersect_single_launch_shapes_bitexact(icosphere, orc, launch):
     """Every launch shape of the single-ray query (occupancy variants of the
