@@ -32,6 +32,7 @@ TRAVERSE_PACKET, TRAVERSE_SINGLE = 0, 1
 REFILL_AFTER_CAMERA, REFILL_ALL, REFILL_NONE = 0, 1, 2
 RNG_PATCH, RNG_GROUP = 0, 1
 MODE_MEGAKERNEL, MODE_WAVEFRONT, MODE_AUTO = 0, 1, 2
+HOST_ACCESS_AUTO, HOST_ACCESS_COPY = 0, 1
 
 _LIB = None
 
@@ -115,6 +116,7 @@ def lib(build=False):
         "cvx_scene_num_direct_samples": (U32, [P]),
         "cvx_scene_set_light_pick": (I32, [P, U32]),
         "cvx_scene_set_query_launch": (I32, [P, U32]),
+        "cvx_scene_set_host_access": (I32, [P, U32, P]),
         "cvx_scene_destroy": (None, [P]),
         "cvx_intersect_nearest": (I32, [P, P, P, P, P, P, P, U32, F32, U32, P, P]),
         "cvx_intersect_nearest_device": (I32, [P, P, U32, F32, U32, P, P, P, P]),
@@ -358,6 +360,15 @@ class Scene:
     def set_query_launch(self, blocks_per_sm):
         """Resident blocks per SM of the nearest-hit kernel (0: default)."""
         _check(lib().cvx_scene_set_query_launch(self._h, blocks_per_sm))
+
+    def set_host_access(self, mode):
+        """How intersect_nearest brings host rays to the device: HOST_ACCESS_AUTO
+        reads them in place where the device shares the host's page tables,
+        HOST_ACCESS_COPY copies them first. Returns True when calls will read in
+        place."""
+        in_place = ctypes.c_uint32()
+        _check(lib().cvx_scene_set_host_access(self._h, mode, ctypes.byref(in_place)))
+        return bool(in_place.value)
 
     def direct_sample_num(self):
         return lib().cvx_scene_num_direct_samples(self._h)

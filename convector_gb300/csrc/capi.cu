@@ -69,6 +69,17 @@ int32_t dalloc(T** p, size_t count, const char* what) {
     return CVX_OK;
 }
 
+// Host memory the driver can copy without staging (allocated or registered
+// page-locked through CUDA).
+bool page_locked(const void* p) {
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeHost;
+}
+
 }  // namespace
 
 struct cvx_scene {
@@ -81,6 +92,12 @@ struct cvx_scene {
     uint32_t n_nodes = 0, n_tris = 0, n_lights = 0, depth = 0;
     uint32_t general_pick = 1;
     uint32_t blocks_per_sm = 0;  // launch shape of the nearest-hit query (0: default)
+    // The device reads host memory through the host's page tables (address
+    // translation over a coherent CPU-GPU link): the host-buffer query may
+    // read the caller's ray arrays in place. host_access: CVX_HOST_ACCESS_*.
+    bool host_page_tables = false;
+    uint32_t host_access = CVX_HOST_ACCESS_AUTO;
+    bool reads_host_in_place() const { return host_page_tables && host_access == CVX_HOST_ACCESS_AUTO; }
     // scratch for the host-buffer query
     float* d_rays = nullptr;
     float* d_t = nullptr;
@@ -91,6 +108,7 @@ struct cvx_scene {
     // (status, ray counter) words
     cudaStream_t qstreams[3] = {nullptr, nullptr, nullptr};
     uint32_t* d_qerr = nullptr;
+    uint32_t* h_qerr = nullptr;  // page-locked copy of d_qerr
 
     DeviceScene view() const {
         DeviceScene s;
@@ -115,6 +133,7 @@ struct cvx_scene {
         cudaFree(d_t);
         cudaFree(d_tri);
         cudaFree(d_qerr);
+        if (h_qerr) cudaFreeHost(h_qerr);
         for (cudaStream_t q : qstreams)
             if (q) cudaStreamDestroy(q);
         if (stream) cudaStreamDestroy(stream);
@@ -209,6 +228,12 @@ int32_t cvx_scene_create(const cvx_triangle* tris, uint32_t n_tris, const cvx_bv
     if (st) return st;
     std::unique_ptr<cvx_scene> s(new cvx_scene());
     s->device = dev;
+    int host_tables = 0;
+    if (cudaDeviceGetAttribute(&host_tables, cudaDevAttrPageableMemoryAccessUsesHostPageTables, dev) != cudaSuccess) {
+        cudaGetLastError();
+        host_tables = 0;
+    }
+    s->host_page_tables = host_tables == 1;
     s->n_nodes = n_nodes;
     s->n_tris = n_tris;
     s->n_lights = (uint32_t)ds.size();
@@ -270,6 +295,13 @@ int32_t cvx_scene_set_light_pick(cvx_scene* s, uint32_t light_pick) {
     return CVX_OK;
 }
 
+int32_t cvx_scene_set_host_access(cvx_scene* s, uint32_t mode, uint32_t* in_place) {
+    if (!s || mode > CVX_HOST_ACCESS_COPY) return set_error(CVX_ERR_INVALID, "bad host access mode");
+    s->host_access = mode;
+    if (in_place) *in_place = s->reads_host_in_place() ? 1u : 0u;
+    return CVX_OK;
+}
+
 int32_t cvx_scene_set_query_launch(cvx_scene* s, uint32_t blocks_per_sm) {
     if (!s || blocks_per_sm > 32) return set_error(CVX_ERR_INVALID, "bad launch shape");
     s->blocks_per_sm = blocks_per_sm;
@@ -284,8 +316,8 @@ int32_t cvx_intersect_nearest_device(cvx_scene* s, const float* rays, uint32_t n
     if (traversal > 1) return set_error(CVX_ERR_INVALID, "unknown traversal variant");
     if (n == 0) return CVX_OK;
     cudaStream_t st = (cudaStream_t)stream;
-    CK(launch_intersect(s->view(), rays, n, far_dist, traversal == CVX_TRAVERSE_PACKET, t_out, tri_out, counters,
-                        s->d_err, 0, s->blocks_per_sm, st),
+    CK(launch_intersect(s->view(), soa_cols(rays, n), n, far_dist, traversal == CVX_TRAVERSE_PACKET, t_out, tri_out,
+                        counters, s->d_err, 0, s->blocks_per_sm, st),
        "intersect launch");
     return CVX_OK;
 }
@@ -298,7 +330,11 @@ int32_t cvx_intersect_nearest(cvx_scene* s, const float* ox, const float* oy, co
     if (!ox || !oy || !oz || !dx || !dy || !dz || !t_out || !tri_out) return set_error(CVX_ERR_INVALID, "null buffer");
     if (traversal > 1) return set_error(CVX_ERR_INVALID, "unknown traversal variant");
     int32_t st = 0;
-    if (s->scratch_n < n) {
+    // In place: the kernel reads the caller's six arrays over the CPU-GPU
+    // link as it consumes them (a warp stages each batch of 32 rays one batch
+    // ahead), so the transfer overlaps traversal and no ray copy is made.
+    const bool in_place = s->reads_host_in_place();
+    if (s->scratch_n < n || (!in_place && !s->d_rays)) {
         cudaFree(s->d_rays);
         cudaFree(s->d_t);
         cudaFree(s->d_tri);
@@ -306,46 +342,61 @@ int32_t cvx_intersect_nearest(cvx_scene* s, const float* ox, const float* oy, co
         s->d_t = nullptr;
         s->d_tri = nullptr;
         s->scratch_n = 0;
-        if ((st = dalloc(&s->d_rays, (size_t)n * 6, "ray buffer"))) return st;
+        if (!in_place && (st = dalloc(&s->d_rays, (size_t)n * 6, "ray buffer"))) return st;
         if ((st = dalloc(&s->d_t, n, "hit buffer"))) return st;
         if ((st = dalloc(&s->d_tri, n, "hit buffer"))) return st;
         s->scratch_n = n;
     }
-    // Copy/compute pipeline: the rays are cut into chunks that go round-robin
-    // to three streams, so the copies of one chunk overlap the traversal of
-    // another (and a chunk's kernel starts on SMs the previous one has left).
-    // Up to four chunks of at least 2^19 rays (measured on 4M rays: 4 chunks
-    // beat 8 and 16, whose shorter launches and copies cost more than they overlap).
+    // Chunked pipeline: the rays are cut into chunks that go round-robin to
+    // three streams, so the copies of one chunk overlap the traversal of
+    // another (a chunk's kernel starts on the SMs the previous one leaves).
+    // Chunk counts, measured on 4M rays: 4 when rays are copied from page-locked
+    // memory (against 1, 2 and 8); 2 when they are read in place (only the hits
+    // remain to overlap); 1 when any buffer is pageable, as the driver stages
+    // each pageable copy through its own buffers and every extra chunk adds
+    // one such round trip.
     constexpr uint32_t kMaxChunks = 4, kMinChunk = 1u << 19;
     if (!s->d_qerr && (st = dalloc(&s->d_qerr, 2 * kMaxChunks, "status"))) return st;
+    if (!s->h_qerr) {
+        CK(cudaHostAlloc((void**)&s->h_qerr, 8 * kMaxChunks, cudaHostAllocDefault), "cudaHostAlloc status");
+    }
     for (cudaStream_t& q : s->qstreams)
         if (!q) CK(cudaStreamCreateWithFlags(&q, cudaStreamNonBlocking), "cudaStreamCreate");
+    const float* src[6] = {ox, oy, oz, dx, dy, dz};
+    bool locked = page_locked(t_out) && page_locked(tri_out);
+    for (int k = 0; k < 6 && locked && !in_place; k++) locked = page_locked(src[k]);
+    uint32_t max_chunks = !locked ? 1u : (in_place ? 2u : kMaxChunks);
     uint32_t chunks = n / kMinChunk;
-    chunks = chunks < 1 ? 1 : (chunks > kMaxChunks ? kMaxChunks : chunks);
+    chunks = chunks < 1 ? 1 : (chunks > max_chunks ? max_chunks : chunks);
     uint32_t per = (n + chunks - 1) / chunks;
     per = (per + 31u) & ~31u;
-    const float* src[6] = {ox, oy, oz, dx, dy, dz};
     uint32_t c = 0;
     for (uint32_t off = 0; off < n; off += per, c++) {
         uint32_t len = n - off < per ? n - off : per;
         cudaStream_t q = s->qstreams[c % 3];
-        float* rays = s->d_rays + (size_t)6 * off;
-        for (int k = 0; k < 6; k++)
-            CK(cudaMemcpyAsync(rays + (size_t)k * len, src[k] + off, (size_t)len * 4, cudaMemcpyHostToDevice, q),
-               "copy rays");
+        RayCols cols;
+        if (in_place) {
+            for (int k = 0; k < 6; k++) cols.c[k] = src[k] + off;
+        } else {
+            float* rays = s->d_rays + (size_t)6 * off;
+            for (int k = 0; k < 6; k++)
+                CK(cudaMemcpyAsync(rays + (size_t)k * len, src[k] + off, (size_t)len * 4, cudaMemcpyHostToDevice,
+                                   q),
+                   "copy rays");
+            cols = soa_cols(rays, len);
+        }
         CK(cudaMemsetAsync(s->d_qerr + 2 * c, 0, 8, q), "reset status");
-        CK(launch_intersect(s->view(), rays, len, far_dist, traversal == CVX_TRAVERSE_PACKET, s->d_t + off,
+        CK(launch_intersect(s->view(), cols, len, far_dist, traversal == CVX_TRAVERSE_PACKET, s->d_t + off,
                             s->d_tri + off, nullptr, s->d_qerr + 2 * c, 0, s->blocks_per_sm, q),
            "intersect launch");
         CK(cudaMemcpyAsync(t_out + off, s->d_t + off, (size_t)len * 4, cudaMemcpyDeviceToHost, q), "copy distances");
         CK(cudaMemcpyAsync(tri_out + off, s->d_tri + off, (size_t)len * 4, cudaMemcpyDeviceToHost, q),
            "copy indices");
+        CK(cudaMemcpyAsync(s->h_qerr + 2 * c, s->d_qerr + 2 * c, 8, cudaMemcpyDeviceToHost, q), "copy status");
     }
     for (cudaStream_t q : s->qstreams) CK(cudaStreamSynchronize(q), "intersect");
-    uint32_t err[2 * kMaxChunks] = {};
-    CK(cudaMemcpy(err, s->d_qerr, 8 * c, cudaMemcpyDeviceToHost), "copy status");
     for (uint32_t k = 0; k < c; k++)
-        if (err[2 * k]) return set_error(CVX_ERR_DEVICE, "traversal stack overflow reported by the kernel");
+        if (s->h_qerr[2 * k]) return set_error(CVX_ERR_DEVICE, "traversal stack overflow reported by the kernel");
     return CVX_OK;
 }
 

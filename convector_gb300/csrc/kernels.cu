@@ -78,7 +78,7 @@ __device__ __forceinline__ uint32_t octet_claim(uint32_t* counter, unsigned omas
 }
 
 template <bool PACKET>
-__global__ void __launch_bounds__(256) k_intersect(DeviceScene s, const float* __restrict__ rays, uint32_t n,
+__global__ void __launch_bounds__(256) k_intersect(DeviceScene s, const RayCols rays, uint32_t n,
                                                    float far_dist, float* __restrict__ t_out,
                                                    int32_t* __restrict__ tri_out, uint32_t* __restrict__ counters,
                                                    uint32_t* __restrict__ err) {
@@ -92,8 +92,8 @@ __global__ void __launch_bounds__(256) k_intersect(DeviceScene s, const float* _
         uint32_t i = pk * 8u + (uint32_t)k;
         bool active = i < n;
         uint32_t src = active ? i : (i & ~7u);
-        F3 o = f3(__ldg(rays + src), __ldg(rays + n + src), __ldg(rays + 2 * n + src));
-        F3 d = f3(__ldg(rays + 3 * n + src), __ldg(rays + 4 * n + src), __ldg(rays + 5 * n + src));
+        F3 o = f3(__ldg(rays.c[0] + src), __ldg(rays.c[1] + src), __ldg(rays.c[2] + src));
+        F3 d = f3(__ldg(rays.c[3] + src), __ldg(rays.c[4] + src), __ldg(rays.c[5] + src));
         Hit h{far_dist, 0.0f, 0.0f, -1};
         Counters c{0u, 0u};
         bool ok = true;
@@ -114,7 +114,7 @@ __global__ void __launch_bounds__(256) k_intersect(DeviceScene s, const float* _
 struct SoaRays {
     const float4* nodes;
     const float4* geom;
-    const float* rays;
+    RayCols rays;
     uint32_t n;
     float far_dist;
     float* t_out;
@@ -124,8 +124,8 @@ struct SoaRays {
                                          const float4*& gm) const {
         nd = nodes;
         gm = geom;
-        o = f3(__ldg(rays + r), __ldg(rays + n + r), __ldg(rays + 2 * n + r));
-        d = f3(__ldg(rays + 3 * n + r), __ldg(rays + 4 * n + r), __ldg(rays + 5 * n + r));
+        o = f3(__ldg(rays.c[0] + r), __ldg(rays.c[1] + r), __ldg(rays.c[2] + r));
+        d = f3(__ldg(rays.c[3] + r), __ldg(rays.c[4] + r), __ldg(rays.c[5] + r));
         far = far_dist;
         return true;
     }
@@ -158,7 +158,7 @@ struct StagedSoaClaim {
     __device__ __forceinline__ void issue(int which, uint32_t base, int lane) {
         uint32_t r = base + (uint32_t)lane;
         if (r < src.n)
-            for (int c = 0; c < 6; c++) cp_async4(&buf[which][c][lane], src.rays + (size_t)c * src.n + r);
+            for (int c = 0; c < 6; c++) cp_async4(&buf[which][c][lane], src.rays.c[c] + r);
         cp_async_commit();
     }
     __device__ __forceinline__ void init(int lane) {
@@ -422,7 +422,7 @@ cudaError_t launch_prep_lights(const cvx_triangle* tris, const uint32_t* ds, uin
     return cudaGetLastError();
 }
 
-cudaError_t launch_intersect(const DeviceScene& s, const float* rays, uint32_t n, float far_dist, bool packet,
+cudaError_t launch_intersect(const DeviceScene& s, const RayCols& rays, uint32_t n, float far_dist, bool packet,
                              float* t_out, int32_t* tri_out, uint32_t* counters, uint32_t* err, uint32_t block,
                              uint32_t blocks_per_sm, cudaStream_t st) {
     if (!packet) {

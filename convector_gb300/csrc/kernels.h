@@ -13,7 +13,19 @@ cudaError_t upload_tables_wave(const uint16_t* rcp, const uint16_t* rsqrt);
 cudaError_t launch_prep_geom(const cvx_triangle* tris, uint32_t n, float4* geom, TriShade* shade, cudaStream_t st);
 cudaError_t launch_prep_lights(const cvx_triangle* tris, const uint32_t* ds, uint32_t n, float4* lights,
                                cudaStream_t st);
-cudaError_t launch_intersect(const DeviceScene& s, const float* rays, uint32_t n, float far_dist, bool packet,
+// The six ray components of a nearest-hit query (origin x, y, z, direction
+// x, y, z), each an array of n floats. The pointers may be device memory or,
+// where the device shares the host's page tables, host memory read in place.
+struct RayCols {
+    const float* c[6];
+};
+inline RayCols soa_cols(const float* rays, uint32_t n) {  // one (6, n) device array
+    RayCols r;
+    for (int k = 0; k < 6; k++) r.c[k] = rays + (size_t)k * n;
+    return r;
+}
+
+cudaError_t launch_intersect(const DeviceScene& s, const RayCols& rays, uint32_t n, float far_dist, bool packet,
                              float* t_out, int32_t* tri_out, uint32_t* counters, uint32_t* err, uint32_t block,
                              uint32_t blocks_per_sm, cudaStream_t st);
 cudaError_t launch_render(const DeviceScene& s, const DeviceCamera& cam, uint32_t w, uint32_t h, uint32_t frame,

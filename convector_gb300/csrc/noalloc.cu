@@ -85,8 +85,9 @@ extern "C" int32_t cvx_intersect_nearest_noalloc(cvx_scene* scene, const float* 
         if ((e = cudaMemcpyAsync(rays + (size_t)k * n, src[k], (size_t)n * sizeof(float), cudaMemcpyHostToDevice,
                                  stream)) != cudaSuccess)
             return fail(e, "copy rays");
-    if ((e = cvx::launch_intersect(cvx::scene_view(scene), rays, n, far_dist, traversal == CVX_TRAVERSE_PACKET, t_dev,
-                                   tri_dev, nullptr, status, 0, 0, stream)) != cudaSuccess)
+    if ((e = cvx::launch_intersect(cvx::scene_view(scene), cvx::soa_cols(rays, n), n, far_dist,
+                                   traversal == CVX_TRAVERSE_PACKET, t_dev, tri_dev, nullptr, status, 0, 0,
+                                   stream)) != cudaSuccess)
         return fail(e, "intersect launch");
     if ((e = cudaMemcpyAsync(t_out, t_dev, (size_t)n * sizeof(float), cudaMemcpyDeviceToHost, stream)) != cudaSuccess)
         return fail(e, "copy distances");

@@ -130,6 +130,17 @@ int32_t cvx_scene_set_light_pick(cvx_scene* scene, uint32_t light_pick);
  * blocks per SM (0: default 8; the single-ray kernel is built for 8, 10 and
  * 12, trading registers for occupancy). Results do not depend on it. */
 int32_t cvx_scene_set_query_launch(cvx_scene* scene, uint32_t blocks_per_sm);
+/* How cvx_intersect_nearest brings the caller's host ray arrays to the device.
+ * AUTO (default): where the device translates addresses through the host's
+ * page tables (a coherent CPU-GPU link, as on Grace systems; pinned or pageable
+ * memory alike), the query kernel reads the six arrays in place while it
+ * traverses, and no copy of the rays is made; elsewhere, and always under
+ * COPY, each chunk of rays is copied to device memory first. Hits are copied
+ * back either way, and the results are the same. `in_place` (optional)
+ * receives 1 when this scene's calls will read in place. No counterpart in
+ * the reference, whose query reads its own memory (bvh.rs:659-662). */
+enum { CVX_HOST_ACCESS_AUTO = 0, CVX_HOST_ACCESS_COPY = 1 };
+int32_t cvx_scene_set_host_access(cvx_scene* scene, uint32_t mode, uint32_t* in_place);
 void cvx_scene_destroy(cvx_scene* scene);
 
 /* Traversal variants (flags of cvx_intersect_nearest, traversal of cvx_render_config). */
@@ -139,7 +150,8 @@ enum { CVX_TRAVERSE_PACKET = 0, CVX_TRAVERSE_SINGLE = 1 };
  * 8 per reference packet in input order; the hit record starts at
  * `far_dist` (MIntersection::with_max_distance, ray.rs:95-103). Outputs the
  * hit distance and the BVH-order triangle index (-1 for no hit). Host
- * buffers; copies in and out inside the call. */
+ * buffers, read in place or copied in (cvx_scene_set_host_access); hits are
+ * copied out inside the call. */
 int32_t cvx_intersect_nearest(cvx_scene* scene, const float* ox, const float* oy, const float* oz,
                               const float* dx, const float* dy, const float* dz, uint32_t n, float far_dist,
                               uint32_t traversal, float* t_out, int32_t* tri_out);

@@ -107,6 +107,61 @@ def test_intersect_negative_zero_bounds_bitexact(gpu, orc):
     assert (tri == otri).all() and (t.view(np.uint32) == ot.view(np.uint32)).all()
 
 
+@pytest.mark.parametrize("traversal", [0, 1])
+def test_intersect_host_access_modes_agree(gpu, icosphere, orc, traversal):
+    """The host-buffer query reading the caller's arrays in place (where the
+    device shares the host's page tables) and copying them first give the same
+    hits, bit for bit, over several chunks with a ragged last one; a sample
+    equals the oracle."""
+    bvh, scene, osc = icosphere
+    n = 3 * (1 << 19) + 123
+    o, d = scenes.random_rays(n, seed=17)
+    res = {}
+    try:
+        for mode in (gpu.HOST_ACCESS_COPY, gpu.HOST_ACCESS_AUTO):
+            scene.set_host_access(mode)
+            res[mode] = scene.intersect_nearest(o, d, traversal=traversal)
+    finally:
+        scene.set_host_access(gpu.HOST_ACCESS_AUTO)
+    (tc, ic), (ta, ia) = res[gpu.HOST_ACCESS_COPY], res[gpu.HOST_ACCESS_AUTO]
+    assert (ic == ia).all() and (tc.view(np.uint32) == ta.view(np.uint32)).all()
+    pick = np.r_[0:4096, n - 4096:n]
+    ot, otri = osc.intersect(o[pick], d[pick], mode=traversal)
+    assert (ia[pick] == otri).all() and (ta[pick].view(np.uint32) == ot.view(np.uint32)).all()
+
+
+def test_intersect_host_access_pinned_buffers(gpu, icosphere):
+    """Page-locked host buffers (as an application's staging memory) through
+    the C-ABI: in place and copied agree."""
+    torch = pytest.importorskip("torch")
+    import ctypes
+    bvh, scene, osc = icosphere
+    n = (1 << 20) + 77
+    o, d = scenes.random_rays(n, seed=19)
+    cols = [torch.from_numpy(np.ascontiguousarray(a)).pin_memory() for a in
+            (o[:, 0], o[:, 1], o[:, 2], d[:, 0], d[:, 1], d[:, 2])]
+    out = {}
+    try:
+        for mode in (gpu.HOST_ACCESS_COPY, gpu.HOST_ACCESS_AUTO):
+            scene.set_host_access(mode)
+            t = torch.empty(n, dtype=torch.float32).pin_memory()
+            tri = torch.empty(n, dtype=torch.int32).pin_memory()
+            gpu._check(gpu.lib().cvx_intersect_nearest(scene._h, *[ctypes.c_void_p(c.data_ptr()) for c in cols], n,
+                                                       1.0e5, 1, ctypes.c_void_p(t.data_ptr()),
+                                                       ctypes.c_void_p(tri.data_ptr())))
+            out[mode] = (t.numpy().copy(), tri.numpy().copy())
+    finally:
+        scene.set_host_access(gpu.HOST_ACCESS_AUTO)
+    assert (out[0][1] == out[1][1]).all() and (out[0][0].view(np.uint32) == out[1][0].view(np.uint32)).all()
+    ref_t, ref_tri = scene.intersect_nearest(o, d, traversal=1)
+    assert (out[1][1] == ref_tri).all()
+
+
+def test_host_access_rejects_bad_mode(gpu, icosphere):
+    with pytest.raises(gpu.CvxError):
+        icosphere[1].set_host_access(7)
+
+
 @pytest.mark.parametrize("launch", [8, 10, 12])
 def test_intersect_single_launch_shapes_bitexact(icosphere, orc, launch):
     """Every launch shape of the single-ray query (occupancy variants of the
