@@ -165,7 +165,9 @@ struct cvx_renderer {
     bool debug = false;
     uint32_t* d_patches = nullptr;  // patch origins of the patch entry points
     uint32_t patch_cap = 0;
+    uint32_t* d_group_em = nullptr;  // per 8-pixel group: lanes that hit an emitter at bounce 0
     ~cvx_renderer() {
+        cudaFree(d_group_em);
         cudaFree(d_patches);
         cudaFree(d_rgba);
         cudaFree(d_gbuf);
@@ -431,6 +433,7 @@ int32_t cvx_renderer_create(cvx_scene* scene, uint32_t w, uint32_t h, const cvx_
     if ((st = dalloc(&r->d_accum, npx * 3, "accumulator"))) return st;
     if ((st = dalloc(&r->d_rays, 1, "counters"))) return st;
     if ((st = dalloc(&r->d_err, 2, "status"))) return st;  // [0] status, [1] group counter
+    if ((st = dalloc(&r->d_group_em, ((size_t)(w + 15) / 16) * ((h + 3) / 4) * 8, "group counters"))) return st;
     CK(cudaStreamCreateWithFlags(&r->stream, cudaStreamNonBlocking), "cudaStreamCreate");
     CK(cudaEventCreate(&r->e0), "cudaEventCreate");
     CK(cudaEventCreate(&r->e1), "cudaEventCreate");
@@ -509,7 +512,7 @@ static int32_t run_frame(cvx_renderer* r, uint32_t frame, bool accumulate, uint3
     CK(launch_render(r->scene->view(), r->cam, r->w, r->h, frame, r->cfg.traversal == CVX_TRAVERSE_PACKET,
                      r->cfg.rng_order == CVX_RNG_PATCH, accumulate ? nullptr : r->d_rgba, r->d_gbuf, r->d_color,
                      accumulate ? r->d_accum : nullptr, r->d_rays, r->d_err, r->cfg.block_size, r->debug,
-                     r->stream),
+                     r->stream, 32, nullptr, 0, r->cfg.refill_mode == CVX_REFILL_NONE ? nullptr : r->d_group_em),
        "render launch");
     CK(cudaEventRecord(r->e1, r->stream), "event");
     if (rgba) CK(cudaMemcpyAsync(rgba, r->d_rgba, npx * 4, cudaMemcpyDeviceToHost, r->stream), "copy colour");

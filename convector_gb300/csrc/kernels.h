@@ -28,10 +28,13 @@ inline RayCols soa_cols(const float* rays, uint32_t n) {  // one (6, n) device a
 cudaError_t launch_intersect(const DeviceScene& s, const RayCols& rays, uint32_t n, float far_dist, bool packet,
                              float* t_out, int32_t* tri_out, uint32_t* counters, uint32_t* err, uint32_t block,
                              uint32_t blocks_per_sm, cudaStream_t st);
+// group_em: one word per 8-pixel group; given, a single-ray frame in the
+// per-group RNG order takes the per-lane path refill form (k_render_refill),
+// else one octet per group (k_render_group).
 cudaError_t launch_render(const DeviceScene& s, const DeviceCamera& cam, uint32_t w, uint32_t h, uint32_t frame,
                           bool packet, bool patch_order, uint32_t* rgba, uint32_t* gbuf, float* color, float* accum,
                           unsigned long long* rays, uint32_t* err, uint32_t block, bool debug, cudaStream_t st, uint32_t patch = 32,
-                          const uint32_t* patches = nullptr, uint32_t n_patches = 0);
+                          const uint32_t* patches = nullptr, uint32_t n_patches = 0, uint32_t* group_em = nullptr);
 cudaError_t launch_resolve(const float* accum, uint32_t npx, float factor, uint32_t* rgba, cudaStream_t st);
 // refill_from: first bounce whose single-ray traversal uses ray refill (the
 // earlier ones traverse one octet per group); packet traversal ignores it.

@@ -189,73 +189,46 @@ struct EachClaim {
     }
 };
 
-// Persistent single-ray traversal with ray refill over the rays of `claim`.
-// Every iteration each lane processes one node pair or one leaf; a lane whose
-// ray is finished takes the next unclaimed ray, so warps stay full while rays
-// of different lengths finish.
-// Decisions and their order are exactly those of traverse<false>: after a
-// pair test the child the reference would pop next is processed at once
-// (its cull test sees the same hit distance the pop would), the other one is
+// One lane's single-ray traversal in the refill form. step() does one
+// iteration: one node pair (and, LEAF_AFTER_PAIR, the leaf it leads to) or one
+// leaf. Decisions and their order are exactly those of traverse<false>: after a
+// pair test the child the reference would pop next is processed at once (its
+// cull test sees the same hit distance the pop would), the other one is
 // pushed, and culled entries are popped within the same iteration.
-// The whole warp must call this. `src` provides
-//   void store(r, const Hit&, uint32_t boxes, uint32_t triangles)
-// (box and triangle counts when COUNT, else 0). LEAF_AFTER_PAIR: a lane whose
-// pair test leads to a leaf tests that leaf in the same iteration (fewer
-// iterations for deep trees; the order of decisions is the same either way).
-// CLAIM_MIN: lanes without a ray wait until that many want one; results do
-// not depend on it (each ray's traversal is independent of when it starts).
-// Returns false if a ray overflowed the stack (its hit is then incomplete).
-template <bool COUNT, bool LEAF_AFTER_PAIR, int CLAIM_MIN, class Src, class Claim>
-__device__ __forceinline__ bool traverse_refill(const Src& src, Claim& claim, const ApproxTables& tab) {
-    const int lane = threadIdx.x & 31;
-    const float4* nodes = nullptr;
-    const float4* geom = nullptr;
-    // (ref, entry distance bits). The top entry lives in `top`, entries
-    // below it in local memory: a pop takes `top` at once and reloads the
-    // next one from memory, so that load's latency hides behind the work on
-    // the popped node.
-    uint2 stack[kStackDepth];
-    uint2 top = make_uint2(0u, 0u);
-    int sp = 0;
-    uint32_t ray = 0, na = 0, nt = 0;
-    uint32_t cur = 0;  // ref of the node to process; kNone: pop
-    const uint32_t kNone = 0xffffffffu;
-    bool have = false, done = false, overflow = false;
-    F3 o = f3(0, 0, 0), d = f3(0, 0, 0), inv = f3(0, 0, 0);
-    Hit h{0.0f, 0.0f, 0.0f, -1};
-    for (;;) {
-        bool want = !have && !done;
-        unsigned b = __ballot_sync(0xffffffffu, want);
-        // Claim only when CLAIM_MIN lanes want a ray (or none has work): the
-        // claim path then runs with many lanes at once instead of with one or
-        // two lanes in nearly every iteration.
-        if (CLAIM_MIN > 1 && b && __popc(b) < CLAIM_MIN && __any_sync(0xffffffffu, have)) b = 0u;
-        want = want && b;
-        if (b) {
-            uint32_t r = 0;
-            RayIn in;
-            int got = claim.claim(b, want, lane, r, in);
-            if (want) {
-                if (got == kClaimRay) {
-                    ray = r;
-                    o = in.o;
-                    d = in.d;
-                    nodes = in.nodes;
-                    geom = in.geom;
-                    inv = f3(x_rcp(d.x, tab), x_rcp(d.y, tab), x_rcp(d.z, tab));
-                    h = Hit{in.far, 0.0f, 0.0f, -1};
-                    sp = 0;
-                    na = 2;
-                    nt = 0;
-                    cur = 0;  // the root pair: internal ref with index 0
-                    have = true;
-                } else if (got == kClaimDone) {
-                    done = true;
-                }
-            }
-        }
-        if (__all_sync(0xffffffffu, done)) break;
-        if (!have) continue;
+struct RefillRay {
+    static constexpr uint32_t kNone = 0xffffffffu;
+    const float4* nodes;
+    const float4* geom;
+    F3 o, d, inv;
+    Hit h;
+    // The stack holds (ref, entry distance bits) entries. Its top entry lives
+    // in `top`, the entries below it in the caller's local array: a pop takes
+    // `top` at once and reloads the next one from memory, so that load's
+    // latency hides behind the work on the popped node.
+    uint2 top;
+    int sp;
+    uint32_t cur;  // ref of the node to process; kNone: pop
+    uint32_t na, nt;
+
+    __device__ __forceinline__ void start(F3 o_, F3 d_, float far, const float4* nodes_, const float4* geom_,
+                                          const ApproxTables& tab) {
+        o = o_;
+        d = d_;
+        nodes = nodes_;
+        geom = geom_;
+        inv = f3(x_rcp(d.x, tab), x_rcp(d.y, tab), x_rcp(d.z, tab));
+        h = Hit{far, 0.0f, 0.0f, -1};
+        sp = 0;
+        na = 2;
+        nt = 0;
+        cur = 0;  // the root pair: internal ref with index 0
+    }
+
+    // Returns true when the ray is finished (its stack is empty): h is then
+    // its nearest hit. Sets `overflow` (and finishes the ray) when the stack
+    // would overflow.
+    template <bool COUNT, bool LEAF_AFTER_PAIR>
+    __device__ __forceinline__ bool step(uint2 (&stack)[kStackDepth], bool& overflow) {
         if (cur == kNone) {
             // Pop until an entry survives the cull test (aabb.rs:171-177).
             while (sp > 0) {
@@ -266,11 +239,7 @@ __device__ __forceinline__ bool traverse_refill(const Src& src, Claim& claim, co
                     break;
                 }
             }
-            if (cur == kNone) {
-                src.store(ray, h, na, nt);
-                have = false;
-                continue;
-            }
+            if (cur == kNone) return true;
         }
         uint32_t len = cur & 31u, idx = cur >> 5;
         if (!LEAF_AFTER_PAIR && len != 0u) {  // a popped leaf; the pair loop continues next iteration
@@ -283,7 +252,7 @@ __device__ __forceinline__ bool traverse_refill(const Src& src, Claim& claim, co
             for (uint32_t i = idx; i < idx + len; i++) tri_test(geom, i, o, d, true, h);
             if (COUNT) nt += len;
             cur = kNone;
-            continue;
+            return false;
         }
         if (len == 0u) {
             // An internal node: test its two children.
@@ -305,7 +274,7 @@ __device__ __forceinline__ bool traverse_refill(const Src& src, Claim& claim, co
                 overflow = true;
                 sp = 0;
                 cur = kNone;
-                continue;
+                return false;
             }
             if (hit_first) {
                 if (sp > 0) stack[sp - 1] = top;
@@ -313,7 +282,7 @@ __device__ __forceinline__ bool traverse_refill(const Src& src, Claim& claim, co
                 sp++;
             }
             cur = (hit_second && !geq(t_second, h.t)) ? ref_second : kNone;
-            if (!LEAF_AFTER_PAIR || cur == kNone) continue;
+            if (!LEAF_AFTER_PAIR || cur == kNone) return false;
             len = cur & 31u;
             idx = cur >> 5;
         }
@@ -329,6 +298,64 @@ __device__ __forceinline__ bool traverse_refill(const Src& src, Claim& claim, co
             for (uint32_t i = idx; i < idx + len; i++) tri_test(geom, i, o, d, true, h);
             if (COUNT) nt += len;
             cur = kNone;
+        }
+        return false;
+    }
+};
+
+// Persistent single-ray traversal with ray refill over the rays of `claim`.
+// Every iteration each lane processes one node pair or one leaf (RefillRay);
+// a lane whose ray is finished takes the next unclaimed ray, so warps stay
+// full while rays of different lengths finish.
+// The whole warp must call this. `src` provides
+//   void store(r, const Hit&, uint32_t boxes, uint32_t triangles)
+// (box and triangle counts when COUNT, else 0). LEAF_AFTER_PAIR: a lane whose
+// pair test leads to a leaf tests that leaf in the same iteration (fewer
+// iterations for deep trees; the order of decisions is the same either way).
+// CLAIM_MIN: lanes without a ray wait until that many want one; results do
+// not depend on it (each ray's traversal is independent of when it starts).
+// Returns false if a ray overflowed the stack (its hit is then incomplete).
+template <bool COUNT, bool LEAF_AFTER_PAIR, int CLAIM_MIN, class Src, class Claim>
+__device__ __forceinline__ bool traverse_refill(const Src& src, Claim& claim, const ApproxTables& tab) {
+    const int lane = threadIdx.x & 31;
+    RefillRay ray;
+    uint2 stack[kStackDepth];
+    ray.top = make_uint2(0u, 0u);
+    ray.sp = 0;
+    ray.cur = 0;
+    ray.na = ray.nt = 0;
+    ray.nodes = ray.geom = nullptr;
+    ray.o = ray.d = ray.inv = f3(0, 0, 0);
+    ray.h = Hit{0.0f, 0.0f, 0.0f, -1};
+    uint32_t r_id = 0;
+    bool have = false, done = false, overflow = false;
+    for (;;) {
+        bool want = !have && !done;
+        unsigned b = __ballot_sync(0xffffffffu, want);
+        // Claim only when CLAIM_MIN lanes want a ray (or none has work): the
+        // claim path then runs with many lanes at once instead of with one or
+        // two lanes in nearly every iteration.
+        if (CLAIM_MIN > 1 && b && __popc(b) < CLAIM_MIN && __any_sync(0xffffffffu, have)) b = 0u;
+        want = want && b;
+        if (b) {
+            uint32_t r = 0;
+            RayIn in;
+            int got = claim.claim(b, want, lane, r, in);
+            if (want) {
+                if (got == kClaimRay) {
+                    r_id = r;
+                    ray.start(in.o, in.d, in.far, in.nodes, in.geom, tab);
+                    have = true;
+                } else if (got == kClaimDone) {
+                    done = true;
+                }
+            }
+        }
+        if (__all_sync(0xffffffffu, done)) break;
+        if (!have) continue;
+        if (ray.step<COUNT, LEAF_AFTER_PAIR>(stack, overflow)) {
+            src.store(r_id, ray.h, ray.na, ray.nt);
+            have = false;
         }
     }
     return !overflow;

@@ -192,19 +192,25 @@ enum { CVX_RNG_PATCH = 0, CVX_RNG_GROUP = 1 };
  * queues with compaction), optionally replayed as a CUDA graph. */
 enum { CVX_MODE_MEGAKERNEL = 0, CVX_MODE_WAVEFRONT = 1, CVX_MODE_AUTO = 2 };
 
-/* Wavefront single-ray traversal: which bounces fetch rays with refill
- * (persistent lanes take the next ray when theirs finishes) rather than one
- * octet per group (coherent camera rays share warps with their neighbours). */
+/* Ray refill in the single-ray traversal: persistent lanes take the next ray
+ * when theirs finishes, rather than one octet working through an 8-pixel group.
+ * Wavefront form: which bounces fetch rays with refill (the camera rays of a
+ * group are coherent and share warps well by octets).
+ * Single-launch form, per-group RNG order: CVX_REFILL_NONE renders one 8-pixel
+ * group per octet through all its bounces; the other two give each lane one
+ * path at a time, refilled ray by ray (a lane whose ray is finished shades it
+ * together with the others of its warp that are, then traces the next). The
+ * image is the same either way. */
 enum { CVX_REFILL_AFTER_CAMERA = 0, CVX_REFILL_ALL = 1, CVX_REFILL_NONE = 2 };
 
 typedef struct cvx_render_config {
     uint32_t rng_order;     /* CVX_RNG_* */
     uint32_t traversal;     /* CVX_TRAVERSE_* */
     uint32_t mode;          /* CVX_MODE_* */
-    uint32_t block_size;    /* megakernel: threads per block, 32, 64, 96 or 128 (0: 128) */
+    uint32_t block_size;    /* megakernel, octet groups: threads per block, 32, 64, 96 or 128 (0: 128) */
     uint32_t use_graph;     /* wavefront: capture the bounce loop in a CUDA graph */
     uint32_t blocks_per_sm; /* wavefront: persistent blocks per SM (0: 12) */
-    uint32_t refill_mode;   /* wavefront: CVX_REFILL_* */
+    uint32_t refill_mode;   /* CVX_REFILL_* */
 } cvx_render_config;
 
 /* Renderer::new (renderer.rs:121-130). Any width and height are accepted;

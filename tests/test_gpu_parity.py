@@ -366,6 +366,100 @@ def test_render_ragged_sizes_pad_and_crop(room, gpu, orc, w, h):
         assert (rgba == orgba).all() and (gb == ogb).all() and rays == orays
 
 
+def _render_refill_forms(gpu, scene, cam, w, h, frame, accumulate=0):
+    """The single-launch single-ray frame in its two forms: per-lane path
+    refill (default) and one octet per 8-pixel group (REFILL_NONE)."""
+    out = {}
+    for refill in (gpu.REFILL_AFTER_CAMERA, gpu.REFILL_NONE):
+        r = gpu.Renderer(scene, w, h, rng_order=gpu.RNG_GROUP, traversal=gpu.TRAVERSE_SINGLE, refill_mode=refill)
+        r.set_camera(cam)
+        if accumulate:
+            for s in range(accumulate):
+                r.accumulate_frame_f32(frame + s)
+            out[refill] = (r.read_accumulator(), None, None, r.stats()[0])
+        else:
+            rgba, gb = r.render_frame_u8(frame)
+            out[refill] = (rgba, gb, r.read_frame_f32(), r.stats()[0])
+    return out
+
+
+@pytest.mark.parametrize("eye,target,kind", [
+    ((0.0, 1.25, 1.0), (0.0, 1.25, 5.0), "sky"),
+    ((1.9, 1.25, 0.5), (3.5, 1.25, -1.5), "wall and sky"),
+    ((0.0, 0.8, -2.0), (0.05, 2.5, -2.05), "ceiling light"),
+])
+def test_refill_frame_emitter_groups_bitexact(room, gpu, orc, eye, target, kind):
+    """Per-lane path refill against the oracle where whole 8-pixel groups hit
+    an emitter (the sky or the ceiling light) at bounce 0: the reference exits
+    such a group before taking its gbuffer values (words 0), while mixed groups
+    keep each lane's own word. Every output equals the oracle's and the
+    octet-group form's."""
+    bvh, scene, osc = room
+    cam = scenes.default_camera(gpu.Camera(), eye=eye, target=target)
+    w, h = 160, 96
+    out = _render_refill_forms(gpu, scene, cam, w, h, 42)
+    orgba, ogb, ocol, orays = osc.render(cam.as_array(), w, h, 42, rng_order=1, traversal=1)
+    for rgba, gb, col, rays in out.values():
+        assert (rgba == orgba).all() and (gb == ogb).all() and rays == orays
+        assert (col.view(np.uint32) == ocol.view(np.uint32)).all()
+    if kind == "sky":
+        assert (ogb == 0).all()
+    else:
+        assert (ogb == 0).any() and (ogb != 0).any()
+
+
+def test_refill_full_frame_bitexact(room, gpu, orc):
+    """The interactive configuration (1280x736, 1 spp, frame 42) in the
+    per-lane path refill form against the oracle's single-ray frame."""
+    bvh, scene, osc = room
+    out = _render_refill_forms(gpu, scene, scene.camera, 1280, 736, 42)
+    orgba, ogb, ocol, orays = osc.render(scene.camera.as_array(), 1280, 736, 42, rng_order=1, traversal=1)
+    rgba, gb, col, rays = out[gpu.REFILL_AFTER_CAMERA]
+    assert (col.view(np.uint32) == ocol.view(np.uint32)).all()
+    assert (rgba == orgba).all() and (gb == ogb).all() and rays == orays
+    for a, b in zip(out[gpu.REFILL_AFTER_CAMERA][:3], out[gpu.REFILL_NONE][:3]):
+        assert (a.view(np.uint32) == b.view(np.uint32)).all()
+
+
+@pytest.mark.parametrize("w,h", [(1, 1), (7, 3), (100, 50), (33, 17)])
+def test_refill_ragged_sizes(room, gpu, orc, w, h):
+    """Groups partly outside the frame still trace all 8 lanes (ray count and
+    the bounce-0 emitter rule see them) but store only pixels inside."""
+    bvh, scene, osc = room
+    out = _render_refill_forms(gpu, scene, scene.camera, w, h, 7)
+    orgba, ogb, ocol, orays = osc.render(scene.camera.as_array(), w, h, 7, rng_order=1, traversal=1)
+    for rgba, gb, col, rays in out.values():
+        assert (rgba == orgba).all() and (gb == ogb).all() and rays == orays
+
+
+def test_refill_accumulate_bitexact(room, gpu, orc):
+    bvh, scene, osc = room
+    w, h, n = 128, 64, 3
+    out = _render_refill_forms(gpu, scene, scene.camera, w, h, 42, accumulate=n)
+    acc = np.zeros((h, w, 3), np.float32)
+    for s in range(n):
+        osc.render(scene.camera.as_array(), w, h, 42 + s, rng_order=1, traversal=1, color=False, accum=acc)
+    for a, *_ in out.values():
+        assert (a.view(np.uint32) == acc.view(np.uint32)).all()
+
+
+def test_refill_matches_octet_groups_on_larger_scenes(gpu):
+    """Path refill against the octet-group form on the 82k-triangle scene
+    (claim threshold 16) and on the 70-level tube (threshold 8): the same
+    frame bit for bit."""
+    tube_tris, _ = scenes.random_walk_tube(obj=False)
+    tube = gpu.Scene(gpu.Bvh.build(tube_tris))
+    assert tube.bvh.depth > 40
+    ico_tris, _ = scenes.displaced_icosphere(obj=False, light=True)
+    ico = gpu.Scene(gpu.Bvh.build(ico_tris))
+    for sc in (ico, tube):
+        cam = scenes.default_camera(gpu.Camera())
+        out = _render_refill_forms(gpu, sc, cam, 320, 184, 5)
+        for a, b in zip(out[gpu.REFILL_AFTER_CAMERA][:3], out[gpu.REFILL_NONE][:3]):
+            assert (a.view(np.uint32) == b.view(np.uint32)).all()
+        assert out[gpu.REFILL_AFTER_CAMERA][3] == out[gpu.REFILL_NONE][3]
+
+
 def test_accumulate_and_resolve(room, gpu, orc):
     bvh, scene, osc = room
     w, h, n = 128, 64, 4
