@@ -399,13 +399,17 @@ def bench_render(cg):
     scene = cg.Scene(bvh)
     scenes.default_camera(scene.camera)
     out = {}
-    variants = [("megakernel_packet8", cg.RNG_GROUP, 0, cg.MODE_MEGAKERNEL, 0),
-                ("megakernel_single", cg.RNG_GROUP, 1, cg.MODE_MEGAKERNEL, 0),
-                ("wavefront_single_graph", cg.RNG_GROUP, 1, cg.MODE_WAVEFRONT, 1),
-                ("wavefront_packet8_graph", cg.RNG_GROUP, 0, cg.MODE_WAVEFRONT, 1),
-                ("patch_exact_packet8", cg.RNG_PATCH, 0, cg.MODE_MEGAKERNEL, 0)]
-    for name, order, trav, mode, graph in variants:
-        r = cg.Renderer(scene, 1280, 736, rng_order=order, traversal=trav, mode=mode, use_graph=graph)
+    # single-launch single-ray: one octet per 8-pixel group (the default for
+    # this 19-level tree) and paths per lane with ray refill
+    variants = [("megakernel_packet8", cg.RNG_GROUP, 0, cg.MODE_MEGAKERNEL, 0, cg.REFILL_AFTER_CAMERA),
+                ("megakernel_single", cg.RNG_GROUP, 1, cg.MODE_MEGAKERNEL, 0, cg.REFILL_NONE),
+                ("megakernel_single_path_refill", cg.RNG_GROUP, 1, cg.MODE_MEGAKERNEL, 0, cg.REFILL_ALL),
+                ("wavefront_single_graph", cg.RNG_GROUP, 1, cg.MODE_WAVEFRONT, 1, cg.REFILL_AFTER_CAMERA),
+                ("wavefront_packet8_graph", cg.RNG_GROUP, 0, cg.MODE_WAVEFRONT, 1, cg.REFILL_AFTER_CAMERA),
+                ("patch_exact_packet8", cg.RNG_PATCH, 0, cg.MODE_MEGAKERNEL, 0, cg.REFILL_AFTER_CAMERA)]
+    for name, order, trav, mode, graph, refill in variants:
+        r = cg.Renderer(scene, 1280, 736, rng_order=order, traversal=trav, mode=mode, use_graph=graph,
+                        refill_mode=refill)
         out[name] = _frames(r, 10 if order == cg.RNG_PATCH else 30)
     from convector_gb300 import autotune
     best, table = autotune.tune(scene, 1280, 736, use_cache=False)
@@ -418,7 +422,9 @@ def bench_render(cg):
 
 def bench_large(cg):
     """Accumulative 1280x736, 64 spp, 5 bounces on the ~870k-triangle random-walk
-    tube (seed 11): wavefront + CUDA graph against the megakernel."""
+    tube (seed 11): wavefront + CUDA graph against the single launch (paths per
+    lane with ray refill, the default for this 70-level tree, and one octet per
+    group)."""
     from convector_gb300 import scenes
     tris, _ = scenes.random_walk_tube(obj=False)
     bvh = cg.Bvh.build(tris)
@@ -429,6 +435,8 @@ def bench_large(cg):
     best, table = autotune.tune(scene, 1280, 736, use_cache=False, frames=3)
     for name, kw in (("wavefront_single_graph", dict(traversal=1, mode=cg.MODE_WAVEFRONT, use_graph=1)),
                      ("megakernel_single", dict(traversal=1, mode=cg.MODE_MEGAKERNEL)),
+                     ("megakernel_single_octets", dict(traversal=1, mode=cg.MODE_MEGAKERNEL,
+                                                       refill_mode=cg.REFILL_NONE)),
                      ("autotuned", best)):
         kw = dict(kw)
         kw.setdefault("rng_order", cg.RNG_GROUP)
@@ -519,14 +527,16 @@ def _served_run(cg, scs, reqs, sequential, engine=None):
             "wavefront_busy_s": st["wavefront_busy_s"]}
 
 
-def _plain_renderer_run(cg, scs, bvhs, reqs):
+def _plain_renderer_run(cg, scs, bvhs, reqs, modes=None):
     """The plain method: the drop-in Renderer API, one request at a time in
     arrival order. Each request gets a Renderer at its resolution, spp
     accumulate_frame_f32 calls and a resolve_u8 read back to the host; the
     scene's kernel form is the server's default rule (wavefront for BVHs
-    deeper than 40 or above 200k triangles, else the single-launch form)."""
-    modes = [cg.MODE_WAVEFRONT if (b.depth > 40 or b.triangles.shape[0] > 200000) else cg.MODE_MEGAKERNEL
-             for b in bvhs]
+    deeper than 40 or above 200k triangles, else the single-launch form)
+    unless `modes` gives one per scene."""
+    if modes is None:
+        modes = [cg.MODE_WAVEFRONT if (b.depth > 40 or b.triangles.shape[0] > 200000) else cg.MODE_MEGAKERNEL
+                 for b in bvhs]
 
     def run(sc, w, h, spp, cam, base):
         r = cg.Renderer(scs[sc], w, h, rng_order=cg.RNG_GROUP, traversal=cg.TRAVERSE_SINGLE, mode=modes[sc],
@@ -598,9 +608,16 @@ def bench_served(cg, duration=2.0, rate=200.0, seed=4):
     served = _served_run(cg, scs, reqs, sequential=False, engine=engine)
     served_default = _served_run(cg, scs, reqs, sequential=False)
     sequential = _served_run(cg, scs, reqs, sequential=True)
-    plain = _plain_renderer_run(cg, scs, bvhs, reqs)
+    # The plain path is the Renderer's default for every scene: the single
+    # launch (paths per lane for the 28- and 70-level trees, one octet per
+    # group for the 19-level room). Beside it, the same requests with the deep
+    # scene in the wavefront form (the server's rule for its engines).
+    plain = _plain_renderer_run(cg, scs, bvhs, reqs, modes=[cg.MODE_MEGAKERNEL] * len(scs))
+    plain_wf = _plain_renderer_run(cg, scs, bvhs, reqs)
     return {"rate_per_s": rate, "duration_s": duration, "served": served, "served_engine": engine,
             "served_default_engine": served_default, "plain_renderer": plain,
+            "plain_renderer_wavefront_for_deep": plain_wf,
+            "throughput_ratio_vs_plain_wavefront_for_deep": served["mrays_per_s"] / plain_wf["mrays_per_s"],
             "server_one_at_a_time": sequential,
             "throughput_ratio": served["mrays_per_s"] / plain["mrays_per_s"],
             "throughput_ratio_default_engine": served_default["mrays_per_s"] / plain["mrays_per_s"],

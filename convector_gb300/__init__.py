@@ -59,7 +59,7 @@ class _ServerConfig(ctypes.Structure):
                 ("traversal", ctypes.c_uint32), ("use_graph", ctypes.c_uint32), ("sequential", ctypes.c_uint32),
                 ("blocks_per_sm", ctypes.c_uint32), ("refill_mode", ctypes.c_uint32),
                 ("kernel_mode", ctypes.c_uint32), ("fused_blocks_per_sm", ctypes.c_uint32),
-                ("wavefront_streams", ctypes.c_uint32)]
+                ("wavefront_streams", ctypes.c_uint32), ("deep_single_launch", ctypes.c_uint32)]
 
 
 class _Request(ctypes.Structure):
@@ -572,11 +572,11 @@ class Server:
 
     def __init__(self, scenes, framebuffer_bytes=4 << 30, max_groups=1 << 21, traversal=TRAVERSE_SINGLE,
                  use_graph=1, sequential=False, blocks_per_sm=0, refill_mode=REFILL_AFTER_CAMERA, kernel_mode=0,
-                 fused_blocks_per_sm=0, wavefront_streams=1):
+                 fused_blocks_per_sm=0, wavefront_streams=1, deep_single_launch=0):
         self.scenes = list(scenes)
         arr = (ctypes.c_void_p * len(self.scenes))(*[s._h.value for s in self.scenes])
         cfg = _ServerConfig(framebuffer_bytes, max_groups, traversal, use_graph, int(sequential), blocks_per_sm,
-                            refill_mode, kernel_mode, fused_blocks_per_sm, wavefront_streams)
+                            refill_mode, kernel_mode, fused_blocks_per_sm, wavefront_streams, deep_single_launch)
         out = ctypes.c_void_p()
         _check(lib().cvx_server_create(arr, len(self.scenes), ctypes.byref(cfg), ctypes.byref(out)))
         self._h = out

@@ -3,7 +3,8 @@ actual scene and frame size and keeps the fastest.
 
 Candidates (all give the same image for a given RNG order and traversal; the
 single-ray and packet traversals can differ only on t-ties and grazing rays):
-the fused megakernel at several block sizes, and the wavefront form with
+the fused megakernel at several block sizes with one octet per 8-pixel group,
+the fused megakernel with paths per lane and ray refill, and the wavefront form with
 CUDA-graph replay at several persistent grid sizes and ray-refill modes, each
 with the single-ray and the 8-ray packet traversal. The traversal stack holds
 128 entries; a scene needs BVH depth + 2 (checked at scene creation), so stack
@@ -31,7 +32,10 @@ def candidates(rng_order=RNG_GROUP, allow_packet=True):
     travs = [TRAVERSE_SINGLE, TRAVERSE_PACKET] if allow_packet else [TRAVERSE_SINGLE]
     for trav in travs:
         for block in (64, 128):  # the fused kernels are compiled for at most 128 threads per block
-            out.append(dict(rng_order=rng_order, traversal=trav, mode=MODE_MEGAKERNEL, block_size=block))
+            out.append(dict(rng_order=rng_order, traversal=trav, mode=MODE_MEGAKERNEL, block_size=block,
+                            refill_mode=REFILL_NONE))
+    if rng_order == RNG_GROUP:  # single launch with paths per lane (its block is fixed at 128)
+        out.append(dict(rng_order=rng_order, traversal=TRAVERSE_SINGLE, mode=MODE_MEGAKERNEL, refill_mode=REFILL_ALL))
     if rng_order == RNG_GROUP:
         for bps in (8, 12, 16):
             for refill in (REFILL_AFTER_CAMERA, REFILL_ALL, REFILL_NONE):

@@ -442,7 +442,7 @@ int32_t cvx_renderer_create(cvx_scene* scene, uint32_t w, uint32_t h, const cvx_
     if (c.mode == CVX_MODE_WAVEFRONT) {
         r->engine.reset(new WaveEngine());
         if ((st = r->engine->init(groups_of(w, h), 1, c.traversal == CVX_TRAVERSE_PACKET, c.use_graph != 0,
-                                  c.blocks_per_sm, refill_from(c.refill_mode))))
+                                  c.blocks_per_sm, c.refill_mode)))
             return st;
         cvx_scene* sc[1] = {scene};
         if ((st = r->engine->set_scenes(sc, 1))) return st;
@@ -512,7 +512,8 @@ static int32_t run_frame(cvx_renderer* r, uint32_t frame, bool accumulate, uint3
     CK(launch_render(r->scene->view(), r->cam, r->w, r->h, frame, r->cfg.traversal == CVX_TRAVERSE_PACKET,
                      r->cfg.rng_order == CVX_RNG_PATCH, accumulate ? nullptr : r->d_rgba, r->d_gbuf, r->d_color,
                      accumulate ? r->d_accum : nullptr, r->d_rays, r->d_err, r->cfg.block_size, r->debug,
-                     r->stream, 32, nullptr, 0, r->cfg.refill_mode == CVX_REFILL_NONE ? nullptr : r->d_group_em),
+                     r->stream, 32, nullptr, 0,
+                     path_refill_frames(r->cfg.refill_mode, r->scene->depth) ? r->d_group_em : nullptr),
        "render launch");
     CK(cudaEventRecord(r->e1, r->stream), "event");
     if (rgba) CK(cudaMemcpyAsync(rgba, r->d_rgba, npx * 4, cudaMemcpyDeviceToHost, r->stream), "copy colour");

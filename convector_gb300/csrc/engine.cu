@@ -59,8 +59,9 @@ WaveEngine::~WaveEngine() {
 }
 
 int32_t WaveEngine::init(uint32_t max_groups, uint32_t max_jobs, bool packet, bool use_graph,
-                         uint32_t blocks_per_sm, uint32_t refill_from, bool fused) {
-    refill_from_ = refill_from;
+                         uint32_t blocks_per_sm, uint32_t refill_mode, bool fused) {
+    refill_mode_ = refill_mode;
+    refill_from_ = refill_from(refill_mode);
     max_groups_ = max_groups;
     max_jobs_ = max_jobs;
     packet_ = packet;
@@ -113,13 +114,8 @@ int32_t WaveEngine::set_scenes(cvx_scene* const* scenes, uint32_t n) {
     }
     ECK(cudaMemcpy(d_scenes_, v.data(), n * sizeof(DeviceScene), cudaMemcpyHostToDevice), "upload scene table");
     n_scenes_ = n;
-    bool deep = false;
-    for (const DeviceScene& d : v) deep = deep || d.depth > 40;
-    if (deep != deep_) {  // captured graphs hold the other traversal variant
-        for (auto& g : graphs_) cudaGraphExecDestroy(g.exec);
-        graphs_.clear();
-        deep_ = deep;
-    }
+    scene_depth_.resize(n);
+    for (uint32_t i = 0; i < n; i++) scene_depth_[i] = v[i].depth;
     return CVX_OK;
 }
 
@@ -128,25 +124,27 @@ static bool same_out(const WaveOutputs& a, const WaveOutputs& b) { return std::m
 static cudaError_t launch_any(bool fused, const Job* jobs, const WaveHeader* hdr, const DeviceScene* scenes,
                               const WaveState& st, const WaveOutputs& out, bool packet, uint32_t bps,
                               uint32_t refill_from, bool deep, cudaStream_t stream) {
-    return fused ? launch_wave_fused(jobs, hdr, scenes, out, packet, bps, stream)
+    return fused ? launch_wave_fused(jobs, hdr, scenes, out, packet, bps, deep, stream)
                  : launch_wave(jobs, hdr, scenes, st, out, packet, bps, refill_from, deep, stream);
 }
 
-int32_t WaveEngine::launch(const WaveOutputs& out, cudaStream_t stream) {
+// deep: a scene of this wave is deeper than 40 levels (the traversal's claim
+// threshold; captured graphs are kept per value).
+int32_t WaveEngine::launch(const WaveOutputs& out, bool deep, cudaStream_t stream) {
     if (!use_graph_) {
-        ECK(launch_any(fused_, d_jobs_, d_hdr_, d_scenes_, st_, out, packet_, blocks_per_sm_, refill_from_, deep_, stream),
+        ECK(launch_any(fused_, d_jobs_, d_hdr_, d_scenes_, st_, out, packet_, blocks_per_sm_, refill_from_, deep, stream),
             "wave launch");
         return CVX_OK;
     }
     for (auto& g : graphs_)
-        if (same_out(g.out, out)) {
+        if (same_out(g.out, out) && g.deep == deep) {
             ECK(cudaGraphLaunch(g.exec, stream), "graph launch");
             return CVX_OK;
         }
     cudaGraph_t graph;
     ECK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal), "begin capture");
     cudaError_t e =
-        launch_any(fused_, d_jobs_, d_hdr_, d_scenes_, st_, out, packet_, blocks_per_sm_, refill_from_, deep_, stream);
+        launch_any(fused_, d_jobs_, d_hdr_, d_scenes_, st_, out, packet_, blocks_per_sm_, refill_from_, deep, stream);
     cudaError_t e2 = cudaStreamEndCapture(stream, &graph);
     if (e != cudaSuccess) return cuda_err(e, "capture wave");
     if (e2 != cudaSuccess) return cuda_err(e2, "end capture");
@@ -158,7 +156,7 @@ int32_t WaveEngine::launch(const WaveOutputs& out, cudaStream_t stream) {
         cudaGraphExecDestroy(graphs_.front().exec);
         graphs_.erase(graphs_.begin());
     }
-    graphs_.push_back(Graph{out, exec});
+    graphs_.push_back(Graph{out, deep, exec});
     ECK(cudaGraphLaunch(exec, stream), "graph launch");
     return CVX_OK;
 }
@@ -168,9 +166,13 @@ int32_t WaveEngine::submit(const std::vector<Job>& jobs_in, WaveOutputs out, cud
     last_jobs_ = 0;
     last_want_ = want_job_rays;
     if (jobs_in.size() > max_jobs_) return set_error(CVX_ERR_CAPACITY, "too many jobs for one wave");
-    uint32_t groups = 0;
+    uint32_t groups = 0, depth = 0, deep_groups = 0;
     for (size_t i = 0; i < jobs_in.size(); i++) {
         Job j = jobs_in[i];
+        if (j.scene >= n_scenes_) return set_error(CVX_ERR_INVALID, "job scene outside the scene table");
+        const uint32_t dj = scene_depth_[j.scene];
+        depth = dj > depth ? dj : depth;
+        if (dj >= kRefillMinDepth) deep_groups += groups_of(j.w, j.h);
         j.group_base = groups;
         j.n_groups = groups_of(j.w, j.h);
         groups += j.n_groups;
@@ -184,6 +186,26 @@ int32_t WaveEngine::submit(const std::vector<Job>& jobs_in, WaveOutputs out, cud
     out.rays = d_rays_;
     out.job_rays = want_job_rays ? d_job_rays_ : nullptr;
     out.err = d_err_;
+    const bool deep = depth > 40;
+    // Single-ray fused waves that take paths per lane (path_refill_wave):
+    // one counter word per group of the wave, grown on demand, zeroed per wave.
+    out.group_em = nullptr;
+    if (fused_ && !packet_ && path_refill_wave(refill_mode_, deep_groups, groups)) {
+        if (groups > group_em_cap_) {
+            uint32_t cap = groups > 2 * group_em_cap_ ? groups : 2 * group_em_cap_;
+            if (d_group_em_) {
+                cudaFree(d_group_em_);
+                owned_.erase(std::remove(owned_.begin(), owned_.end(), (void*)d_group_em_), owned_.end());
+                d_group_em_ = nullptr;
+                group_em_cap_ = 0;
+            }
+            int32_t st = alloc(&d_group_em_, cap, owned_);
+            if (st) return st;
+            group_em_cap_ = cap;
+        }
+        out.group_em = d_group_em_;
+        ECK(cudaMemsetAsync(d_group_em_, 0, (size_t)groups * 4, stream), "reset group counters");
+    }
     ECK(cudaMemcpyAsync(d_jobs_, h_jobs_, jobs_in.size() * sizeof(Job), cudaMemcpyHostToDevice, stream),
         "upload jobs");
     ECK(cudaMemcpyAsync(d_hdr_, h_hdr_, sizeof(WaveHeader), cudaMemcpyHostToDevice, stream), "upload jobs");
@@ -191,7 +213,7 @@ int32_t WaveEngine::submit(const std::vector<Job>& jobs_in, WaveOutputs out, cud
     ECK(cudaMemsetAsync(d_err_, 0, 8, stream), "reset status");
     if (want_job_rays) ECK(cudaMemsetAsync(d_job_rays_, 0, jobs_in.size() * 8, stream), "reset counters");
     ECK(cudaEventRecord(e0_, stream), "event");
-    int32_t st = launch(out, stream);
+    int32_t st = launch(out, deep, stream);
     if (st) return st;
     ECK(cudaEventRecord(e1_, stream), "event");
     ECK(cudaMemcpyAsync(&h_read_->rays, d_rays_, 8, cudaMemcpyDeviceToHost, stream), "read counters");
@@ -278,9 +300,10 @@ extern "C" int32_t cvx_batch_create(cvx_scene* const* scenes, uint32_t n_scenes,
     ECK(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking), "cudaStreamCreate");
     ECK(cudaStreamCreateWithFlags(&b->stream2, cudaStreamNonBlocking), "cudaStreamCreate");
     int32_t st = b->engine.init(max_groups, 4096, c.traversal == CVX_TRAVERSE_PACKET, c.use_graph != 0,
-                                c.blocks_per_sm, refill_from(c.refill_mode));
+                                c.blocks_per_sm, c.refill_mode);
     if (st) return st;
-    if ((st = b->fused.init(0xffffffffu, 4096, c.traversal == CVX_TRAVERSE_PACKET, c.use_graph != 0, 0, 1, true)))
+    if ((st = b->fused.init(0xffffffffu, 4096, c.traversal == CVX_TRAVERSE_PACKET, c.use_graph != 0, 0,
+                            c.refill_mode, true)))
         return st;
     if ((st = b->engine.set_scenes(scenes, n_scenes))) return st;
     if ((st = b->fused.set_scenes(scenes, n_scenes))) return st;
@@ -726,11 +749,12 @@ extern "C" int32_t cvx_server_create(cvx_scene* const* scenes, uint32_t n_scenes
     ECK(cudaDeviceGetStreamPriorityRange(&least, &greatest), "stream priorities");
     ECK(cudaStreamCreateWithPriority(&s->stream, cudaStreamNonBlocking, greatest), "cudaStreamCreate");
     ECK(cudaStreamCreateWithPriority(&s->stream2, cudaStreamNonBlocking, least), "cudaStreamCreate");
+    const bool deep_fused = cfg->deep_single_launch != 0;
     int32_t st = s->engine.init(cfg->max_groups, 1024, cfg->traversal == CVX_TRAVERSE_PACKET, cfg->use_graph != 0,
-                                cfg->blocks_per_sm, refill_from(cfg->refill_mode));
+                                cfg->blocks_per_sm, cfg->refill_mode, deep_fused);
     if (st) return st;
     if ((st = s->fused.init(0xffffffffu, 1024, cfg->traversal == CVX_TRAVERSE_PACKET, cfg->use_graph != 0,
-                            cfg->fused_blocks_per_sm, 1, true)))
+                            cfg->fused_blocks_per_sm, cfg->refill_mode, true)))
         return st;
     if ((st = s->engine.set_scenes(scenes, n_scenes))) return st;
     if ((st = s->fused.set_scenes(scenes, n_scenes))) return st;
@@ -740,7 +764,7 @@ extern "C" int32_t cvx_server_create(cvx_scene* const* scenes, uint32_t n_scenes
         ECK(cudaStreamCreateWithPriority(&s->extra_stream[k - 1], cudaStreamNonBlocking, greatest),
             "cudaStreamCreate");
         if ((st = s->extra_wf[k - 1].init(cfg->max_groups, 1024, cfg->traversal == CVX_TRAVERSE_PACKET,
-                                          cfg->use_graph != 0, cfg->blocks_per_sm, refill_from(cfg->refill_mode))))
+                                          cfg->use_graph != 0, cfg->blocks_per_sm, cfg->refill_mode, deep_fused)))
             return st;
         if ((st = s->extra_wf[k - 1].set_scenes(scenes, n_scenes))) return st;
         s->n_wf = (int)k + 1;

@@ -16,6 +16,7 @@ uint32_t scene_depth(const cvx_scene* s);
 uint32_t scene_num_lights(const cvx_scene* s);
 uint32_t groups_of(uint32_t w, uint32_t h);
 // First bounce traversed with ray refill for a CVX_REFILL_* mode.
+// First bounce of a wavefront wave whose traversal refills rays.
 inline uint32_t refill_from(uint32_t refill_mode) { return refill_mode == 1 ? 0u : refill_mode == 2 ? 5u : 1u; }
 
 class WaveEngine {
@@ -23,9 +24,10 @@ class WaveEngine {
     ~WaveEngine();
     // max_groups: ray-queue capacity (8-pixel groups) of one wave. fused: run
     // waves as one persistent fused kernel (no ray queues) instead of the
-    // wavefront kernels.
+    // wavefront kernels; refill_mode: CVX_REFILL_* (wavefront: which bounces
+    // refill; fused: path_refill_frames with the wave's deepest scene).
     int32_t init(uint32_t max_groups, uint32_t max_jobs, bool packet, bool use_graph, uint32_t blocks_per_sm,
-                 uint32_t refill_from = 1, bool fused = false);
+                 uint32_t refill_mode = CVX_REFILL_AFTER_CAMERA, bool fused = false);
     int32_t set_scenes(cvx_scene* const* scenes, uint32_t n);
     // Queues one wave on `stream` (asynchronous); group_base / n_groups of the
     // jobs are filled in here. collect() waits for it and reads its counters.
@@ -39,7 +41,7 @@ class WaveEngine {
     bool fused() const { return fused_; }
 
    private:
-    int32_t launch(const WaveOutputs& out, cudaStream_t stream);
+    int32_t launch(const WaveOutputs& out, bool deep, cudaStream_t stream);
     struct Readback {
         unsigned long long rays;
         uint32_t err;
@@ -50,6 +52,7 @@ class WaveEngine {
     bool last_want_ = false, fused_ = false;
     struct Graph {
         WaveOutputs out;
+        bool deep;
         cudaGraphExec_t exec;
     };
     WaveState st_{};
@@ -61,8 +64,12 @@ class WaveEngine {
     unsigned long long* d_rays_ = nullptr;
     unsigned long long* d_job_rays_ = nullptr;
     uint32_t* d_err_ = nullptr;
-    uint32_t n_scenes_ = 0, scene_cap_ = 0, max_groups_ = 0, max_jobs_ = 0, blocks_per_sm_ = 0, refill_from_ = 1;
-    bool packet_ = false, use_graph_ = false, deep_ = false;  // deep_: a scene deeper than 40 levels
+    uint32_t* d_group_em_ = nullptr;  // per group of a wave: the path refill's emitter counts
+    uint32_t group_em_cap_ = 0;
+    std::vector<uint32_t> scene_depth_;
+    uint32_t n_scenes_ = 0, scene_cap_ = 0, max_groups_ = 0, max_jobs_ = 0, blocks_per_sm_ = 0, refill_from_ = 1,
+             refill_mode_ = 0;
+    bool packet_ = false, use_graph_ = false;
     std::vector<void*> owned_;
     std::vector<Graph> graphs_;
     cudaEvent_t e0_ = nullptr, e1_ = nullptr;

@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 
 #include "kernels.h"
+#include "path_refill.cuh"
 #include "shade.cuh"
 
 namespace cvx {
@@ -340,30 +341,68 @@ __device__ __forceinline__ void path_pixel(uint32_t p, uint32_t bw, uint32_t& gx
     py = gy + (k >> 2);
 }
 
-// The path loop (renderer.rs:413-468) in per-lane refill form, for the
-// per-group RNG order and the single-ray traversal. Each lane takes one path
-// at a time from a counter (path p is lane p & 7 of group p >> 3) and carries
-// it through its bounces; every iteration a lane tracing a ray processes one
-// node pair or leaf of it (RefillRay). A lane whose ray is finished waits until
-// CLAIM_MIN lanes of its warp are in that state (or none is tracing); those
-// lanes then shade together: the hit record, continue_path, and either the
-// next bounce's ray or the pixel's store and a new path with its camera ray.
-// Warps thus stay busy while paths of 1 to 5 bounces and rays of different
-// lengths finish, and the long shading code runs with many lanes at once.
-//
-// A lane's results depend only on its own path: lane k of a group draws from
-// its own 64-bit generator state (LaneRng), a lane that hits an emitter keeps
-// its colour and ray from then on (material.rs:327-411: cm = 1), and the bounce
-// limit holds per lane. The one coupling in the reference is the group's exit
-// when all 8 lanes hit an emitter at bounce 0, before the gbuffer values are
-// taken: that group's gbuffer words are 0. A lane that hits an emitter at
-// bounce 0 writes its own word, then (after a fence) counts itself in
-// group_em[group]; the lane that counts the eighth writes 0 over the group.
-// Launch shape and loop form of k_render_refill, each measured on the room
-// (5k triangles), the 82k-triangle icosphere and the 870k-triangle tube at
+// The paths of one frame for path_refill (path p: lane p & 7 of group p >> 3,
+// groups numbered as in k_render_group).
+struct FramePaths {
+    struct PathRef {
+        uint32_t path;
+    };
+    const FrameArgs& a;
+    uint32_t bw, bh, rays;
+
+    __device__ __forceinline__ uint32_t n_paths() const { return bw * bh * 64u; }
+    __device__ __forceinline__ uint32_t claim(uint32_t n) { return atomicAdd(a.err + 1, n); }
+    __device__ __forceinline__ bool begin(uint32_t p, PathRef& r, F3& o, F3& d, LaneRng& rng,
+                                          const ApproxTables& tab) {
+        uint32_t gx, gy, px, py;
+        path_pixel(p, bw, gx, gy, px, py);
+        if (gx >= a.w || gy >= a.h) return false;
+        r.path = p;
+        const int k = (int)(p & 7u);
+        float x, y, scale;
+        block_coord(a.w, a.h, gx & ~15u, gy & ~3u, (int)((p >> 3) & 7u), k, &x, &y, &scale);
+        rng.seed(gx, gy, a.frame, k);
+        x = fmaf(unit_from(rng.next()), scale, x);
+        y = fmaf(unit_from(rng.next()), scale, y);
+        camera_ray(a.cam, x, y, unit_from(rng.next()), tab, o, d);
+        return true;
+    }
+    __device__ __forceinline__ DeviceScene scene(const PathRef&) const { return a.s; }
+    __device__ __forceinline__ void gbuffer(const PathRef& r, uint32_t word) {
+        uint32_t gx, gy, px, py;
+        path_pixel(r.path, bw, gx, gy, px, py);
+        if (a.gbuf && px < a.w && py < a.h) a.gbuf[(size_t)py * a.w + px] = word;
+    }
+    __device__ __forceinline__ void mark_emitter(const PathRef& r) {
+        if (a.gbuf) atomicOr(a.group_em + (r.path >> 3), 1u << (r.path & 7u));
+    }
+    __device__ __forceinline__ void store(const PathRef& r, F3 c) {
+        uint32_t gx, gy, px, py;
+        path_pixel(r.path, bw, gx, gy, px, py);
+        if (px >= a.w || py >= a.h) return;
+        const size_t idx = (size_t)py * a.w + px;
+        if (a.rgba) a.rgba[idx] = pack_color(c);
+        if (a.color) {
+            a.color[3 * idx] = c.x;
+            a.color[3 * idx + 1] = c.y;
+            a.color[3 * idx + 2] = c.z;
+        }
+        if (a.accum) {
+            a.accum[3 * idx] += c.x;
+            a.accum[3 * idx + 1] += c.y;
+            a.accum[3 * idx + 2] += c.z;
+        }
+    }
+    __device__ __forceinline__ void count_ray(const PathRef&) { rays++; }
+    __device__ __forceinline__ void finish() { flush_rays(a, rays); }
+};
+
+// Launch shape and loop form of the per-lane path refill, each measured on the
+// room (5k triangles), the 82k-triangle icosphere and the 870k-triangle tube at
 // 1280x736: 7 resident blocks per SM (72 registers, no spill; 8 blocks spill
-// and lose 2-7 %), two traversal steps per round of votes (1 and 3 are
-// 3-8 % slower), and a leaf reached from a pair tested in the same step.
+// and lose 2-7 %), two traversal steps per round of votes (1 and 3 are 3-8 %
+// slower), and a leaf reached from a pair tested in the same step. Claim
+// threshold: 16 lanes up to 40 levels, 8 beyond (measured 4 to 24).
 constexpr int kRefillFrameBlocksPerSm = 7;
 constexpr int kRefillFrameSteps = 2;
 
@@ -371,127 +410,25 @@ template <int CLAIM_MIN>
 __global__ void __launch_bounds__(128, kRefillFrameBlocksPerSm) k_render_refill(FrameArgs a) {
     __shared__ ApproxTables tab;
     load_tables(tab);
-    const int lane = threadIdx.x & 31;
-    const uint32_t bw = (a.w + 15u) / 16u, bh = (a.h + 3u) / 4u;
-    const uint32_t npaths = bw * bh * 64u;
-    RefillRay ray;
-    uint2 stack[kStackDepth];
-    ray.top = make_uint2(0u, 0u);
-    ray.sp = 0;
-    ray.cur = RefillRay::kNone;
-    ray.na = ray.nt = 0;
-    ray.nodes = a.s.nodes;
-    ray.geom = a.s.geom;
-    ray.o = ray.d = ray.inv = f3(0, 0, 0);
-    ray.h = Hit{0.0f, 0.0f, 0.0f, -1};
-    LaneRng rng;
-    rng.s = rng.f = 0ull;
-    rng.hi = 0u;
-    F3 color = f3(1.0f, 1.0f, 1.0f);
-    uint32_t path = 0, bounce = 0, rays = 0;
-    bool tracing = false, has_path = false, done = false, overflow = false;
-    for (;;) {
-        bool want = !tracing && !done;
-        unsigned b = __ballot_sync(0xffffffffu, want);
-        if (CLAIM_MIN > 1 && b && __popc(b) < CLAIM_MIN && __any_sync(0xffffffffu, tracing)) b = 0u;
-        want = want && b;
-        if (want && has_path) {
-            // Shade the finished ray of this bounce.
-            uint32_t gx, gy, px, py;
-            path_pixel(path, bw, gx, gy, px, py);
-            const bool inside = px < a.w && py < a.h;
-            const size_t idx = (size_t)py * a.w + px;
-            Isect I = make_isect(a.s, ray.h, ray.o, ray.d, tab);
-            const bool em = (I.mat >> 31) != 0u;
-            const bool ends = em || bounce == 4u;
-            F3 o = ray.o, d = ray.d;
-            if (bounce == 0u || !ends) {
-                bool act = true;
-                F3 cm;
-                float fr;
-                continue_path(a.s, o, d, act, I, rng, bounce == 0u, tab, cm, fr);
-                if (bounce == 0u && a.gbuf) {
-                    PixelOut g0;
-                    g0.tex = ((int32_t)I.mat >> 24) & 3;
-                    g0.tu = I.tu;
-                    g0.tv = I.tv;
-                    g0.fresnel = fr;
-                    if (inside) a.gbuf[idx] = pack_gbuffer(g0);
-                    if (em) {
-                        __threadfence();
-                        if (atomicAdd(a.group_em + (path >> 3), 1u) == 7u)
-                            for (uint32_t q = 0; q < 8u; q++) {
-                                uint32_t qx = gx + (q & 3u), qy = gy + (q >> 2);
-                                if (qx < a.w && qy < a.h) a.gbuf[(size_t)qy * a.w + qx] = 0u;
-                            }
-                    }
-                }
-                if (!ends) color = f3(color.x * cm.x, color.y * cm.y, color.z * cm.z);
-            }
-            if (ends) {
-                F3 sky = sky_intensity(ray.d);
-                F3 c = em ? f3(color.x * sky.x, color.y * sky.y, color.z * sky.z) : f3(0.0f, 0.0f, 0.0f);
-                if (inside) {
-                    if (a.rgba) a.rgba[idx] = pack_color(c);
-                    if (a.color) {
-                        a.color[3 * idx] = c.x;
-                        a.color[3 * idx + 1] = c.y;
-                        a.color[3 * idx + 2] = c.z;
-                    }
-                    if (a.accum) {
-                        a.accum[3 * idx] += c.x;
-                        a.accum[3 * idx + 1] += c.y;
-                        a.accum[3 * idx + 2] += c.z;
-                    }
-                }
-                has_path = false;
-            } else {
-                bounce++;
-                ray.start(o, d, 1.0e5f, a.s.nodes, a.s.geom, tab);
-                tracing = true;
-                rays++;
-            }
+    FramePaths P{a, (a.w + 15u) / 16u, (a.h + 3u) / 4u, 0u};
+    if (!path_refill<CLAIM_MIN, kRefillFrameSteps>(P, tab)) atomicOr(a.err, kErrStackOverflow);
+}
+
+// After k_render_refill: a group whose 8 lanes all hit an emitter at bounce 0
+// leaves the reference's path loop before its gbuffer values are taken
+// (renderer.rs:413-468), so its gbuffer words are 0.
+__global__ void __launch_bounds__(256) k_emitter_groups(const uint32_t* __restrict__ mask, uint32_t ngroups,
+                                                       uint32_t w, uint32_t h, uint32_t* __restrict__ gbuf) {
+    const uint32_t bw = (w + 15u) / 16u;
+    for (uint32_t gi = blockIdx.x * blockDim.x + threadIdx.x; gi < ngroups; gi += gridDim.x * blockDim.x) {
+        if (mask[gi] != 0xffu) continue;
+        uint32_t gx, gy, px, py;
+        path_pixel(gi << 3, bw, gx, gy, px, py);
+        for (uint32_t q = 0; q < 8u; q++) {
+            uint32_t qx = gx + (q & 3u), qy = gy + (q >> 2);
+            if (qx < w && qy < h) gbuf[(size_t)qy * w + qx] = 0u;
         }
-        // Lanes without a path take the next ones (one atomic per warp).
-        const bool need = want && !has_path;
-        const unsigned nb = __ballot_sync(0xffffffffu, need);
-        if (nb) {
-            uint32_t base = 0;
-            const int first = __ffs(nb) - 1;
-            if (lane == first) base = atomicAdd(a.err + 1, (uint32_t)__popc(nb));
-            base = __shfl_sync(0xffffffffu, base, first);
-            if (need) {
-                path = base + (uint32_t)__popc(nb & ((1u << lane) - 1u));
-                if (path >= npaths) {
-                    done = true;
-                } else {
-                    uint32_t gx, gy, px, py;
-                    path_pixel(path, bw, gx, gy, px, py);
-                    if (gx < a.w && gy < a.h) {  // else: a group outside the frame; take another path
-                        const int k = (int)(path & 7u);
-                        float x, y, scale;
-                        block_coord(a.w, a.h, gx & ~15u, gy & ~3u, (int)((path >> 3) & 7u), k, &x, &y, &scale);
-                        rng.seed(gx, gy, a.frame, k);
-                        x = fmaf(unit_from(rng.next()), scale, x);
-                        y = fmaf(unit_from(rng.next()), scale, y);
-                        F3 o, d;
-                        camera_ray(a.cam, x, y, unit_from(rng.next()), tab, o, d);
-                        ray.start(o, d, 1.0e5f, a.s.nodes, a.s.geom, tab);
-                        color = f3(1.0f, 1.0f, 1.0f);
-                        bounce = 0u;
-                        has_path = true;
-                        tracing = true;
-                        rays++;
-                    }
-                }
-            }
-        }
-        if (__all_sync(0xffffffffu, done)) break;
-        for (int st = 0; st < kRefillFrameSteps && tracing; st++)
-            if (ray.step<false, true>(stack, overflow)) tracing = false;
     }
-    if (overflow) atomicOr(a.err, kErrStackOverflow);
-    flush_rays(a, rays);
 }
 
 template <bool PACKET>
@@ -641,10 +578,12 @@ cudaError_t launch_render(const DeviceScene& s, const DeviceCamera& cam, uint32_
         if (e != cudaSuccess) return e;
         uint32_t need = (ngroups * 8u + 127u) / 128u, blocks = (uint32_t)num_sms() * kRefillFrameBlocksPerSm;
         if (blocks > need) blocks = need;
-        // Claim threshold: 16 lanes up to 40 levels, 8 beyond (measured: 4, 8,
-        // 12, 16, 20 and 24 on the three scenes above).
         if (s.depth > 40) k_render_refill<8><<<blocks, 128, 0, st>>>(a);
         else k_render_refill<16><<<blocks, 128, 0, st>>>(a);
+        if (gbuf) {
+            uint32_t fb = (ngroups + 255u) / 256u, cap = (uint32_t)num_sms() * 8u;
+            k_emitter_groups<<<fb < cap ? fb : cap, 256, 0, st>>>(group_em, ngroups, w, h, gbuf);
+        }
         return cudaGetLastError();
     }
     if (patch_order) {

@@ -28,6 +28,27 @@ inline RayCols soa_cols(const float* rays, uint32_t n) {  // one (6, n) device a
 cudaError_t launch_intersect(const DeviceScene& s, const RayCols& rays, uint32_t n, float far_dist, bool packet,
                              float* t_out, int32_t* tri_out, uint32_t* counters, uint32_t* err, uint32_t block,
                              uint32_t blocks_per_sm, cudaStream_t st);
+// Single-launch form of single-ray frames and waves in the per-group RNG
+// order: paths per lane with ray refill (k_render_refill, k_wave_refill), or
+// one octet per 8-pixel group (k_render_group, k_wave_fused). CVX_REFILL_ALL
+// and CVX_REFILL_NONE choose; by default the depth of the frame's scene
+// decides, and for a wave whether at least half of its groups belong to scenes
+// that deep. Measured at 1280x736 (octet against refill, ms per frame): the
+// 19-level room 0.81 / 0.76, the 28-level icosphere 1.87 / 1.53, the 70-level
+// tube 5.63 / 3.27; 256 scenes of 11 to 23 levels (median 16), batched: 57 / 69
+// ms, one at a time: 2,617 / 2,398 Mrays/s. Refill wins clearly from the
+// icosphere's depth on; the shallow open scenes, whose paths are mostly one or
+// two rays, keep warps of neighbouring camera rays together.
+constexpr uint32_t kRefillMinDepth = 25;
+inline bool path_refill_frames(uint32_t refill_mode, uint32_t depth) {
+    return refill_mode == CVX_REFILL_ALL || (refill_mode == CVX_REFILL_AFTER_CAMERA && depth >= kRefillMinDepth);
+}
+// deep_groups of a wave's groups belong to scenes of kRefillMinDepth levels or more.
+inline bool path_refill_wave(uint32_t refill_mode, uint32_t deep_groups, uint32_t groups) {
+    return refill_mode == CVX_REFILL_ALL ||
+           (refill_mode == CVX_REFILL_AFTER_CAMERA && 2ull * deep_groups >= (uint64_t)groups && groups > 0);
+}
+
 // group_em: one word per 8-pixel group; given, a single-ray frame in the
 // per-group RNG order takes the per-lane path refill form (k_render_refill),
 // else one octet per group (k_render_group).
@@ -42,8 +63,10 @@ cudaError_t launch_wave(const Job* jobs, const WaveHeader* hdr, const DeviceScen
                         const WaveOutputs& out, bool packet, uint32_t blocks_per_sm, uint32_t refill_from, bool deep,
                         cudaStream_t stream);
 // The fused (megakernel) form of a wave: one persistent launch.
+// deep: a scene of the wave is deeper than 40 levels (claim threshold 8, else 16)
 cudaError_t launch_wave_fused(const Job* jobs, const WaveHeader* hdr, const DeviceScene* scenes,
-                              const WaveOutputs& out, bool packet, uint32_t blocks_per_sm, cudaStream_t stream);
+                              const WaveOutputs& out, bool packet, uint32_t blocks_per_sm, bool deep,
+                              cudaStream_t stream);
 cudaError_t launch_resolve_multi(const ResolveItem* items, uint32_t n_items, const float* accum, uint32_t* rgba,
                                  cudaStream_t stream);
 

@@ -173,14 +173,17 @@ __device__ __forceinline__ float normal_dist(F3 h, F3 n, int32_t gloss) {  // ma
     return r;
 }
 
-// material.rs:327-411 for one lane. Advances the ray (unless the lane is or
-// becomes inactive) and returns the colour modulation and raw Fresnel value.
-__device__ __forceinline__ void continue_path(const DeviceScene& s, F3& ro, F3& rd, bool& active, const Isect& I,
-                                              LaneRng& rng, bool ignore_fresnel, const ApproxTables& tab, F3& cm,
-                                              float& fresnel) {
+// The ray continue_path samples next (material.rs:228-265 and the one-sample
+// pick of 327-411): a BRDF sample or a direct-light sample, chosen by the sixth
+// of six draws.
+struct NextRay {
+    F3 o, d;
+    bool direct;
+};
+__device__ __forceinline__ NextRay sample_next(const DeviceScene& s, const Isect& I, LaneRng& rng,
+                                               const ApproxTables& tab) {
     uint32_t dphi = rng.next(), dr = rng.next(), dsel = rng.next(), du = rng.next(), dv = rng.next(),
              drr = rng.next();
-    bool inactive = !active | ((I.mat >> 31) != 0u);
     // continue_path_brdf (material.rs:228-242)
     float phi = angle_from(dphi), r_sqr = unit_from(dr), r = sqrtf(r_sqr);
     F3 hv = f3(poly_sin(phi) * r, poly_cos(phi) * r, sqrtf(1.0f - r_sqr));
@@ -200,8 +203,25 @@ __device__ __forceinline__ void continue_path(const DeviceScene& s, F3& ro, F3& 
     // one-sample MIS between the two
     float rr = fmaf(I.normal.z, 0.8f, biunit_from(drr));
     bool pick_direct = sneg(rr);
-    F3 no = pick_direct ? org_d : org_b;
-    F3 nd = pick_direct ? dir_d : dir_b;
+    return NextRay{pick_direct ? org_d : org_b, pick_direct ? dir_d : dir_b, pick_direct};
+}
+
+// The raw Fresnel value of microfacet_fresnel (material.rs:453-469) for the
+// incoming direction rd and the sampled direction nd.
+__device__ __forceinline__ float fresnel_term(F3 nd, F3 rd, F3& h, const ApproxTables& tab) {
+    h = normalized(sub(nd, rd), tab);
+    float ct = 1.0f - fabs_bits(dot(h, nd));
+    float ct2 = ct * ct, ct3 = ct2 * ct;
+    return fabs_bits(ct2 * ct3);
+}
+
+// The colour modulation of continue_path (material.rs:327-411, microfacet_brdf
+// 415-469) for the sampled next ray n of a lane that continues, from the
+// incoming direction rd; returns the raw Fresnel value in `fresnel`.
+__device__ __forceinline__ F3 path_modulation(const DeviceScene& s, const Isect& I, const NextRay& n, F3 rd,
+                                              bool ignore_fresnel, const ApproxTables& tab, float& fresnel) {
+    const bool pick_direct = n.direct;
+    const F3 no = n.o, nd = n.d;
     float pd_b = xmax(dot(I.normal, nd), 0.0f) * (1.0f / kPi);
     float pd_d = pd_direct_sample(s, no, nd, tab);
     float wden = pd_b + pd_d + 0.01f;
@@ -213,24 +233,33 @@ __device__ __forceinline__ void continue_path(const DeviceScene& s, F3& ro, F3& 
     int32_t mi = (int32_t)I.mat;
     const float k255 = 1.0f / 255.0f;
     F3 col = f3((float)(mi & 0xff) * k255, (float)((mi >> 8) & 0xff) * k255, (float)((mi >> 16) & 0xff) * k255);
-    F3 h = normalized(sub(nd, rd), tab);
+    F3 h;
+    float ct5 = fresnel_term(nd, rd, h, tab);
     float D = normal_dist(h, I.normal, (mi >> 26) & 7);
-    float ct = 1.0f - fabs_bits(dot(h, nd));
-    float ct2 = ct * ct, ct3 = ct2 * ct, ct5 = fabs_bits(ct2 * ct3);
     F3 fcol = f3(fmaf(1.0f - col.x, ct5, col.x), fmaf(1.0f - col.y, ct5, col.y), fmaf(1.0f - col.z, ct5, col.z));
     bool has_tex = (((I.mat << 6) | (I.mat << 7)) >> 31) != 0u;
     if (ignore_fresnel && has_tex) fcol = f3(1.0f, 1.0f, 1.0f);
     float k = modulation * cos_theta;
     F3 c = f3((fcol.x * D) * k, (fcol.y * D) * k, (fcol.z * D) * k);
-    c = f3(xmin(c.x, 2.0f), xmin(c.y, 2.0f), xmin(c.z, 2.0f));
     fresnel = ct5;
+    return f3(xmin(c.x, 2.0f), xmin(c.y, 2.0f), xmin(c.z, 2.0f));
+}
+
+// material.rs:327-411 for one lane. Advances the ray (unless the lane is or
+// becomes inactive) and returns the colour modulation and raw Fresnel value.
+__device__ __forceinline__ void continue_path(const DeviceScene& s, F3& ro, F3& rd, bool& active, const Isect& I,
+                                              LaneRng& rng, bool ignore_fresnel, const ApproxTables& tab, F3& cm,
+                                              float& fresnel) {
+    bool inactive = !active | ((I.mat >> 31) != 0u);
+    NextRay n = sample_next(s, I, rng, tab);
+    F3 c = path_modulation(s, I, n, rd, ignore_fresnel, tab, fresnel);
     if (inactive) {
         cm = f3(1.0f, 1.0f, 1.0f);
         active = false;
     } else {
         cm = c;
-        ro = no;
-        rd = nd;
+        ro = n.o;
+        rd = n.d;
     }
 }
 

@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 
 #include "kernels.h"
+#include "path_refill.cuh"
 #include "shade.cuh"
 #include "wavefront.cuh"
 
@@ -397,8 +398,145 @@ __global__ void __launch_bounds__(128, 8) k_wave_fused(const Job* __restrict__ j
     if ((threadIdx.x & 31u) == 0u && v) atomicAdd(out.rays, v);
 }
 
+// The paths of a wave for path_refill: path p is lane p & 7 of wave group
+// p >> 3, which belongs to the job whose group range holds it. Ray counts per
+// job are kept per lane for the job of its current path and added to the job's
+// total when the lane moves to another job, and at the end.
+struct WavePaths {
+    struct PathRef {
+        uint32_t path, job;
+    };
+    const Job* __restrict__ jobs;
+    const DeviceScene* __restrict__ scenes;
+    const WaveOutputs& out;
+    uint32_t n_jobs, n_groups;
+    uint32_t rays, job_cur, job_acc;
+
+    __device__ __forceinline__ uint32_t n_paths() const { return n_groups * 8u; }
+    __device__ __forceinline__ uint32_t claim(uint32_t n) { return atomicAdd(out.err + 1, n); }
+    __device__ __forceinline__ void origin(const PathRef& r, const Job& j, uint32_t& gx, uint32_t& gy, uint32_t& px,
+                                           uint32_t& py) const {
+        uint32_t xb, yb;
+        int g;
+        group_origin(j, (r.path >> 3) - j.group_base, &xb, &yb, &g, &gx, &gy);
+        px = gx + (r.path & 3u);
+        py = gy + ((r.path >> 2) & 1u);
+    }
+    __device__ __forceinline__ bool begin(uint32_t p, PathRef& r, F3& o, F3& d, LaneRng& rng,
+                                          const ApproxTables& tab) {
+        // Paths are claimed in order, so the next one is mostly in the job of
+        // the last: search the job table only when it is not.
+        const uint32_t gi = p >> 3;
+        uint32_t ji = job_cur;
+        if (ji >= n_jobs || gi - __ldg(&jobs[ji].group_base) >= __ldg(&jobs[ji].n_groups))
+            ji = find_job(jobs, n_jobs, gi);
+        const Job& j = jobs[ji];
+        uint32_t xb, yb, gx, gy;
+        int g;
+        group_origin(j, gi - j.group_base, &xb, &yb, &g, &gx, &gy);
+        if (gx >= j.w || gy >= j.h) return false;
+        r.path = p;
+        r.job = ji;
+        if (ji != job_cur) {
+            if (out.job_rays && job_acc) atomicAdd(&out.job_rays[job_cur], (unsigned long long)job_acc);
+            job_cur = ji;
+            job_acc = 0;
+        }
+        const int k = (int)(p & 7u);
+        float x, y, scale;
+        block_coord_wf(j.w, j.h, xb, yb, g, k, &x, &y, &scale);
+        rng.seed(gx, gy, j.frame, k);
+        x = fmaf(unit_from(rng.next()), scale, x);
+        y = fmaf(unit_from(rng.next()), scale, y);
+        camera_ray(j.cam, x, y, unit_from(rng.next()), tab, o, d);
+        return true;
+    }
+    __device__ __forceinline__ DeviceScene scene(const PathRef& r) const { return scenes[__ldg(&jobs[r.job].scene)]; }
+    __device__ __forceinline__ void gbuffer(const PathRef& r, uint32_t word) {
+        if (!out.gbuf) return;
+        const Job& j = jobs[r.job];
+        uint32_t gx, gy, px, py;
+        origin(r, j, gx, gy, px, py);
+        if (px < j.w && py < j.h) out.gbuf[(size_t)j.out_offset + (size_t)py * j.w + px] = word;
+    }
+    __device__ __forceinline__ void mark_emitter(const PathRef& r) {
+        if (out.gbuf) atomicOr(out.group_em + (r.path >> 3), 1u << (r.path & 7u));
+    }
+    __device__ __forceinline__ void store(const PathRef& r, F3 c) {
+        const Job& j = jobs[r.job];
+        uint32_t gx, gy, px, py;
+        origin(r, j, gx, gy, px, py);
+        if (px >= j.w || py >= j.h) return;
+        const size_t idx = (size_t)j.out_offset + (size_t)py * j.w + px;
+        if (out.rgba) out.rgba[idx] = pack_color(c);
+        if (out.color) {
+            out.color[3 * idx] = c.x;
+            out.color[3 * idx + 1] = c.y;
+            out.color[3 * idx + 2] = c.z;
+        }
+        if (out.accum) {
+            out.accum[3 * idx] += c.x;
+            out.accum[3 * idx + 1] += c.y;
+            out.accum[3 * idx + 2] += c.z;
+        }
+    }
+    __device__ __forceinline__ void count_ray(const PathRef&) {
+        rays++;
+        job_acc++;
+    }
+    __device__ __forceinline__ void finish() {
+        if (out.job_rays && job_acc) atomicAdd(&out.job_rays[job_cur], (unsigned long long)job_acc);
+        unsigned long long v = rays;
+        for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+        if ((threadIdx.x & 31u) == 0u && v) atomicAdd(out.rays, v);
+    }
+};
+
+// A fused wave in per-lane path refill form (path_refill); launch shape and
+// loop form as the frame kernel's (k_render_refill).
+#ifndef CVX_WR_MINB
+#define CVX_WR_MINB 7
+#endif
+constexpr int kRefillWaveBlocksPerSm = CVX_WR_MINB;
+template <int CLAIM_MIN>
+__global__ void __launch_bounds__(128, kRefillWaveBlocksPerSm) k_wave_refill(const Job* __restrict__ jobs,
+                                                                          const WaveHeader* __restrict__ hdr,
+                                                                          const DeviceScene* __restrict__ scenes,
+                                                                          WaveOutputs out) {
+    __shared__ ApproxTables tab;
+    load_tables_wf(tab);
+    WavePaths P{jobs, scenes, out, hdr->n_jobs, hdr->n_groups, 0u, 0xffffffffu, 0u};
+    if (!path_refill<CLAIM_MIN, 2>(P, tab)) atomicOr(out.err, kErrStackOverflow);
+}
+
+// After k_wave_refill: the groups of the wave whose 8 lanes all hit an
+// emitter at bounce 0 get gbuffer words 0 (as k_emitter_groups for a frame).
+__global__ void __launch_bounds__(256) k_wave_emitter_groups(const Job* __restrict__ jobs,
+                                                            const WaveHeader* __restrict__ hdr, WaveOutputs out) {
+    const uint32_t n_groups = hdr->n_groups, n_jobs = hdr->n_jobs;
+    for (uint32_t gi = blockIdx.x * blockDim.x + threadIdx.x; gi < n_groups; gi += gridDim.x * blockDim.x) {
+        if (out.group_em[gi] != 0xffu) continue;
+        const Job& j = jobs[find_job(jobs, n_jobs, gi)];
+        uint32_t xb, yb, gx, gy;
+        int g;
+        group_origin(j, gi - j.group_base, &xb, &yb, &g, &gx, &gy);
+        for (uint32_t q = 0; q < 8u; q++) {
+            uint32_t qx = gx + (q & 3u), qy = gy + (q >> 2);
+            if (qx < j.w && qy < j.h) out.gbuf[(size_t)j.out_offset + (size_t)qy * j.w + qx] = 0u;
+        }
+    }
+}
+
 cudaError_t launch_wave_fused(const Job* jobs, const WaveHeader* hdr, const DeviceScene* scenes,
-                              const WaveOutputs& out, bool packet, uint32_t blocks_per_sm, cudaStream_t stream) {
+                              const WaveOutputs& out, bool packet, uint32_t blocks_per_sm, bool deep,
+                              cudaStream_t stream) {
+    if (!packet && out.group_em) {
+        uint32_t grid = (uint32_t)sms() * kRefillWaveBlocksPerSm;
+        if (deep) k_wave_refill<8><<<grid, 128, 0, stream>>>(jobs, hdr, scenes, out);
+        else k_wave_refill<16><<<grid, 128, 0, stream>>>(jobs, hdr, scenes, out);
+        if (out.gbuf) k_wave_emitter_groups<<<(uint32_t)sms() * 4u, 256, 0, stream>>>(jobs, hdr, out);
+        return cudaGetLastError();
+    }
     if (blocks_per_sm == 0) blocks_per_sm = 16;
     uint32_t grid = (uint32_t)sms() * blocks_per_sm;
     if (packet) k_wave_fused<true><<<grid, 128, 0, stream>>>(jobs, hdr, scenes, out);

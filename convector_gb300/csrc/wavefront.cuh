@@ -50,6 +50,9 @@ struct WaveOutputs {
     unsigned long long* rays;      // all rays of the wave
     unsigned long long* job_rays;  // per job of the wave, or null
     uint32_t* err;
+    // one word per group of the wave, zero at launch: given, a single-ray
+    // fused wave takes paths per lane (k_wave_refill)
+    uint32_t* group_em;
 };
 
 // One image to resolve from the accumulator (renderer.rs:378-410).

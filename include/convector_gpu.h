@@ -197,10 +197,12 @@ enum { CVX_MODE_MEGAKERNEL = 0, CVX_MODE_WAVEFRONT = 1, CVX_MODE_AUTO = 2 };
  * Wavefront form: which bounces fetch rays with refill (the camera rays of a
  * group are coherent and share warps well by octets).
  * Single-launch form, per-group RNG order: CVX_REFILL_NONE renders one 8-pixel
- * group per octet through all its bounces; the other two give each lane one
+ * group per octet through all its bounces; CVX_REFILL_ALL gives each lane one
  * path at a time, refilled ray by ray (a lane whose ray is finished shades it
- * together with the others of its warp that are, then traces the next). The
- * image is the same either way. */
+ * together with the others of its warp that are, then traces the next);
+ * CVX_REFILL_AFTER_CAMERA (default) takes the second for scenes of 25 levels
+ * and more (for a wave of a batch or server: when at least half of its groups
+ * belong to such scenes), the first below. The image is the same either way. */
 enum { CVX_REFILL_AFTER_CAMERA = 0, CVX_REFILL_ALL = 1, CVX_REFILL_NONE = 2 };
 
 typedef struct cvx_render_config {
@@ -314,6 +316,9 @@ typedef struct cvx_server_config {
     uint32_t wavefront_streams; /* wavefront engines, each on its own stream (0, 1: one; at most
                                    4): requests are spread over them and their waves, running
                                    out of phase, fill each other's bounce tails */
+    uint32_t deep_single_launch; /* 1: the engines of the deep scenes (those in wavefront mode)
+                                    run their waves as single launches instead of the wavefront
+                                    kernels, keeping their streams and priority */
 } cvx_server_config;
 
 typedef struct cvx_request {

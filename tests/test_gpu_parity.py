@@ -368,9 +368,9 @@ def test_render_ragged_sizes_pad_and_crop(room, gpu, orc, w, h):
 
 def _render_refill_forms(gpu, scene, cam, w, h, frame, accumulate=0):
     """The single-launch single-ray frame in its two forms: per-lane path
-    refill (default) and one octet per 8-pixel group (REFILL_NONE)."""
+    refill (REFILL_ALL) and one octet per 8-pixel group (REFILL_NONE)."""
     out = {}
-    for refill in (gpu.REFILL_AFTER_CAMERA, gpu.REFILL_NONE):
+    for refill in (gpu.REFILL_ALL, gpu.REFILL_NONE):
         r = gpu.Renderer(scene, w, h, rng_order=gpu.RNG_GROUP, traversal=gpu.TRAVERSE_SINGLE, refill_mode=refill)
         r.set_camera(cam)
         if accumulate:
@@ -414,10 +414,10 @@ def test_refill_full_frame_bitexact(room, gpu, orc):
     bvh, scene, osc = room
     out = _render_refill_forms(gpu, scene, scene.camera, 1280, 736, 42)
     orgba, ogb, ocol, orays = osc.render(scene.camera.as_array(), 1280, 736, 42, rng_order=1, traversal=1)
-    rgba, gb, col, rays = out[gpu.REFILL_AFTER_CAMERA]
+    rgba, gb, col, rays = out[gpu.REFILL_ALL]
     assert (col.view(np.uint32) == ocol.view(np.uint32)).all()
     assert (rgba == orgba).all() and (gb == ogb).all() and rays == orays
-    for a, b in zip(out[gpu.REFILL_AFTER_CAMERA][:3], out[gpu.REFILL_NONE][:3]):
+    for a, b in zip(out[gpu.REFILL_ALL][:3], out[gpu.REFILL_NONE][:3]):
         assert (a.view(np.uint32) == b.view(np.uint32)).all()
 
 
@@ -455,9 +455,9 @@ def test_refill_matches_octet_groups_on_larger_scenes(gpu):
     for sc in (ico, tube):
         cam = scenes.default_camera(gpu.Camera())
         out = _render_refill_forms(gpu, sc, cam, 320, 184, 5)
-        for a, b in zip(out[gpu.REFILL_AFTER_CAMERA][:3], out[gpu.REFILL_NONE][:3]):
+        for a, b in zip(out[gpu.REFILL_ALL][:3], out[gpu.REFILL_NONE][:3]):
             assert (a.view(np.uint32) == b.view(np.uint32)).all()
-        assert out[gpu.REFILL_AFTER_CAMERA][3] == out[gpu.REFILL_NONE][3]
+        assert out[gpu.REFILL_ALL][3] == out[gpu.REFILL_NONE][3]
 
 
 def test_accumulate_and_resolve(room, gpu, orc):

@@ -59,16 +59,22 @@ def test_wavefront_rejects_patch_order(two_scenes, gpu):
         gpu.Renderer(scene, 64, 64, rng_order=gpu.RNG_PATCH, mode=gpu.MODE_WAVEFRONT)
 
 
-def _alone(gpu, scene, view):
+def _alone(gpu, scene, view, rays=None):
     r = gpu.Renderer(scene, view.width, view.height, rng_order=gpu.RNG_GROUP, traversal=1)
     r.set_camera(view.camera)
+    n = 0
     for s in range(view.spp):
         r.accumulate_frame_f32(view.frame_base + s)
+        n += r.stats()[0]
+    if rays is not None:
+        rays.append(n)
     return r.resolve_u8(view.spp)
 
 
-@pytest.mark.parametrize("mode", ["fused", "wavefront", "mixed"])
-def test_batch_images_equal_alone(two_scenes, gpu, orc, mode):
+@pytest.mark.parametrize("mode,refill", [("fused", 0), ("fused", 1), ("wavefront", 0), ("mixed", 0), ("mixed", 1)])
+def test_batch_images_equal_alone(two_scenes, gpu, orc, mode, refill):
+    """refill 1 (REFILL_ALL): the single-launch waves take paths per lane
+    (k_wave_refill); 0: these shallow scenes keep one octet per group."""
     scs = [s for _, s, _ in two_scenes]
     views = []
     for i, (w, h, spp) in enumerate([(160, 96, 2), (33, 17, 3), (96, 64, 1), (320, 184, 4)]):
@@ -76,7 +82,7 @@ def test_batch_images_equal_alone(two_scenes, gpu, orc, mode):
         scenes.default_camera(cam, eye=(0.3 * i, 1.2, 1.6))
         views.append(gpu.View(i % 2, w, h, spp, 100 * i, cam))
     m = {"fused": gpu.MODE_MEGAKERNEL, "wavefront": gpu.MODE_WAVEFRONT, "mixed": gpu.MODE_MEGAKERNEL}[mode]
-    batch = gpu.Batch(scs, max_groups=1 << 16, max_pixels=1 << 20, mode=m)
+    batch = gpu.Batch(scs, max_groups=1 << 16, max_pixels=1 << 20, mode=m, refill_mode=refill)
     if mode == "mixed":  # scene 1 through the wavefront kernels, scene 0 fused, in the same waves
         gpu.lib().cvx_batch_set_scene_mode(batch._h, 1, 1)
     imgs, rays, ms = batch.render(views)
@@ -102,8 +108,12 @@ def test_batch_splits_waves_when_queue_is_small(two_scenes, gpu):
         assert (a == b).all()
 
 
-@pytest.mark.parametrize("kernel_mode", [1, 2])
-def test_server_mix_equals_alone(two_scenes, gpu, kernel_mode):
+@pytest.mark.parametrize("kernel_mode,refill", [(1, 0), (1, 1), (2, 0)])
+def test_server_mix_equals_alone(two_scenes, gpu, kernel_mode, refill):
+    """All requests in single-launch waves (kernel_mode 1; with REFILL_ALL as
+    paths per lane, whose ray counts per request are kept per lane and per job)
+    or in wavefront waves (2): each image and ray count equals the request
+    rendered alone."""
     scs = [s for _, s, _ in two_scenes]
     rng = np.random.default_rng(4)
     reqs = []
@@ -114,7 +124,7 @@ def test_server_mix_equals_alone(two_scenes, gpu, kernel_mode):
                      int(rng.integers(1, 5)), cam))
     for sequential in (False, True):
         srv = gpu.Server(scs, framebuffer_bytes=64 << 20, max_groups=1 << 14, sequential=sequential,
-                         kernel_mode=kernel_mode)
+                         kernel_mode=kernel_mode, refill_mode=refill)
         ids = []
         for i, (sc, w, h, spp, cam) in enumerate(reqs):
             ids.append(srv.submit(sc, w, h, spp, cam, frame_base=10 * i))
@@ -123,7 +133,9 @@ def test_server_mix_equals_alone(two_scenes, gpu, kernel_mode):
             st, img, info = srv.wait(rid)
             assert st == 0 and info["done_s"] >= info["start_s"] >= info["submit_s"]
             sc, w, h, spp, cam = reqs[i]
-            assert (img == _alone(gpu, scs[sc], gpu.View(sc, w, h, spp, 10 * i, cam))).all()
+            rays = []
+            assert (img == _alone(gpu, scs[sc], gpu.View(sc, w, h, spp, 10 * i, cam), rays)).all()
+            assert info["rays"] == rays[0]
         assert srv.stats()["waves"] > 0
         srv.close()
 
