@@ -216,15 +216,25 @@ struct StagedSoaClaim {
 // (shallow trees) gain from large batches of claims, long ones lose more to
 // the waiting: 16 for trees up to 40 levels, 8 beyond (measured on the
 // 82k-triangle icosphere and on the 70-level tube).
+// The first entries of each lane's traversal stack live in shared memory,
+// the deeper ones in local memory. Pops of local entries missed L1 about a
+// third of the time (68.7 % hit rate); measured on 4M rays: 0.905 ms with none
+// shared, 0.890 with 4, 0.878 with 8, 0.883 with 12. (The wavefront and the
+// path-refill traversals, whose larger working sets need the L1 that the
+// carve-out takes, measured no gain or a loss.)
+constexpr int kQueryStackShared = 8;
+
 template <int MINB, bool COUNT, int CLAIM>
 __global__ void __launch_bounds__(128, MINB) k_intersect_refill(SoaRays src, uint32_t* __restrict__ next_ray,
                                                                 uint32_t* __restrict__ err) {
     // The reciprocal table is read three times per ray: from global memory
     // (L1-resident), which leaves the shared-memory carve-out to L1.
     __shared__ float stage[4][2][6][32];
+    __shared__ uint2 sstack[4][kQueryStackShared][32];
     StagedSoaClaim claim{src, next_ray, stage[threadIdx.x >> 5], 0u, 0u, 0u, 0};
     claim.init(threadIdx.x & 31);
-    bool ok = traverse_refill<COUNT, false, CLAIM>(src, claim, g_tables);
+    bool ok = traverse_refill<COUNT, false, CLAIM, kQueryStackShared>(
+        src, claim, g_tables, &sstack[threadIdx.x >> 5][0][threadIdx.x & 31]);
     if (!ok) atomicOr(err, kErrStackOverflow);
 }
 

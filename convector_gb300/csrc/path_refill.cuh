@@ -45,7 +45,8 @@ __device__ __forceinline__ bool path_refill(Paths& P, const ApproxTables& tab) {
     const int lane = threadIdx.x & 31;
     const uint32_t npaths = P.n_paths();
     RefillRay ray;
-    uint2 stack[kStackDepth];
+    uint2 local_stack[kStackDepth];
+    LocalStack stack{local_stack};
     ray.top = make_uint2(0u, 0u);
     ray.sp = 0;
     ray.cur = RefillRay::kNone;

@@ -13,6 +13,8 @@
 //    triangles tie in t, or where the approximate-reciprocal box test is not
 //    conservative for a grazing ray.
 #pragma once
+#include <type_traits>
+
 #include "layout.cuh"
 #include "x86sem.cuh"
 
@@ -189,6 +191,26 @@ struct EachClaim {
     }
 };
 
+// Where a refill traversal keeps the stack entries below its top. LocalStack:
+// a local array. SharedLocalStack<N>: the first N entries in shared memory,
+// in this lane's column of a warp's [N][32] block (no bank conflicts, and pops
+// of those never miss the cache), the deeper ones in the local array.
+struct LocalStack {
+    uint2 (&a)[kStackDepth];
+    __device__ __forceinline__ uint2 load(int i) const { return a[i]; }
+    __device__ __forceinline__ void store(int i, uint2 v) { a[i] = v; }
+};
+template <int N>
+struct SharedLocalStack {
+    uint2* sm;  // entry i at sm[32 * i]
+    uint2 (&a)[kStackDepth];
+    __device__ __forceinline__ uint2 load(int i) const { return i < N ? sm[32 * i] : a[i]; }
+    __device__ __forceinline__ void store(int i, uint2 v) {
+        if (i < N) sm[32 * i] = v;
+        else a[i] = v;
+    }
+};
+
 // One lane's single-ray traversal in the refill form. step() does one
 // iteration: one node pair (and, LEAF_AFTER_PAIR, the leaf it leads to) or one
 // leaf. Decisions and their order are exactly those of traverse<false>: after a
@@ -227,13 +249,13 @@ struct RefillRay {
     // Returns true when the ray is finished (its stack is empty): h is then
     // its nearest hit. Sets `overflow` (and finishes the ray) when the stack
     // would overflow.
-    template <bool COUNT, bool LEAF_AFTER_PAIR>
-    __device__ __forceinline__ bool step(uint2 (&stack)[kStackDepth], bool& overflow) {
+    template <bool COUNT, bool LEAF_AFTER_PAIR, class Stack>
+    __device__ __forceinline__ bool step(Stack& stack, bool& overflow) {
         if (cur == kNone) {
             // Pop until an entry survives the cull test (aabb.rs:171-177).
             while (sp > 0) {
                 uint2 e = top;
-                if (--sp > 0) top = stack[sp - 1];
+                if (--sp > 0) top = stack.load(sp - 1);
                 if (!geq(__uint_as_float(e.y), h.t)) {
                     cur = e.x;
                     break;
@@ -277,7 +299,7 @@ struct RefillRay {
                 return false;
             }
             if (hit_first) {
-                if (sp > 0) stack[sp - 1] = top;
+                if (sp > 0) stack.store(sp - 1, top);
                 top = make_uint2(ref_first, __float_as_uint(t_first));
                 sp++;
             }
@@ -303,6 +325,13 @@ struct RefillRay {
     }
 };
 
+template <int N>
+__device__ __forceinline__ typename std::conditional<N == 0, LocalStack, SharedLocalStack<N>>::type make_stack(
+    uint2* sm, uint2 (&a)[kStackDepth]) {
+    if constexpr (N == 0) return LocalStack{a};
+    else return SharedLocalStack<N>{sm, a};
+}
+
 // Persistent single-ray traversal with ray refill over the rays of `claim`.
 // Every iteration each lane processes one node pair or one leaf (RefillRay);
 // a lane whose ray is finished takes the next unclaimed ray, so warps stay
@@ -315,11 +344,14 @@ struct RefillRay {
 // CLAIM_MIN: lanes without a ray wait until that many want one; results do
 // not depend on it (each ray's traversal is independent of when it starts).
 // Returns false if a ray overflowed the stack (its hit is then incomplete).
-template <bool COUNT, bool LEAF_AFTER_PAIR, int CLAIM_MIN, class Src, class Claim>
-__device__ __forceinline__ bool traverse_refill(const Src& src, Claim& claim, const ApproxTables& tab) {
+template <bool COUNT, bool LEAF_AFTER_PAIR, int CLAIM_MIN, int SHARED_STACK = 0, class Src, class Claim>
+__device__ __forceinline__ bool traverse_refill(const Src& src, Claim& claim, const ApproxTables& tab,
+                                                uint2* shared_stack = nullptr) {
     const int lane = threadIdx.x & 31;
     RefillRay ray;
-    uint2 stack[kStackDepth];
+    uint2 local_stack[kStackDepth];
+    typename std::conditional<SHARED_STACK == 0, LocalStack, SharedLocalStack<SHARED_STACK>>::type stack =
+        make_stack<SHARED_STACK>(shared_stack, local_stack);
     ray.top = make_uint2(0u, 0u);
     ray.sp = 0;
     ray.cur = 0;

@@ -494,10 +494,7 @@ struct WavePaths {
 
 // A fused wave in per-lane path refill form (path_refill); launch shape and
 // loop form as the frame kernel's (k_render_refill).
-#ifndef CVX_WR_MINB
-#define CVX_WR_MINB 7
-#endif
-constexpr int kRefillWaveBlocksPerSm = CVX_WR_MINB;
+constexpr int kRefillWaveBlocksPerSm = 7;  // 6 (80 registers, no spill) measured the same
 template <int CLAIM_MIN>
 __global__ void __launch_bounds__(128, kRefillWaveBlocksPerSm) k_wave_refill(const Job* __restrict__ jobs,
                                                                           const WaveHeader* __restrict__ hdr,
