@@ -172,25 +172,6 @@ struct RayIn {
     const float4* geom;
 };
 
-// One warp-aggregated atomic per claiming iteration; the source loads the ray.
-//   bool Src::load(r, F3& o, F3& d, float& far, const float4*& nodes, const float4*& geom)
-template <class Src>
-struct EachClaim {
-    const Src& src;
-    uint32_t n;
-    uint32_t* next_ray;
-    __device__ __forceinline__ int claim(unsigned b, bool want, int lane, uint32_t& r, RayIn& in) {
-        uint32_t base = 0;
-        int first = __ffs(b) - 1;
-        if (lane == first) base = atomicAdd(next_ray, (uint32_t)__popc(b));
-        base = __shfl_sync(0xffffffffu, base, first);
-        if (!want) return kClaimNone;
-        r = base + __popc(b & ((1u << lane) - 1u));
-        if (r >= n) return kClaimDone;
-        return src.load(r, in.o, in.d, in.far, in.nodes, in.geom) ? kClaimRay : kClaimNone;
-    }
-};
-
 // Where a refill traversal keeps the stack entries below its top. LocalStack:
 // a local array. SharedLocalStack<N>: the first N entries in shared memory,
 // in this lane's column of a warp's [N][32] block (no bank conflicts, and pops
