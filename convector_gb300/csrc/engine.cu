@@ -189,10 +189,12 @@ int32_t WaveEngine::submit(const std::vector<Job>& jobs_in, WaveOutputs out, cud
     const bool deep = depth > 40;
     // Single-ray fused waves that take paths per lane (path_refill_wave):
     // one counter word per group of the wave, grown on demand, zeroed per wave.
+    // (Path ids are 32-bit: waves of 2^29 groups or more keep the octet form.)
     out.group_em = nullptr;
-    if (fused_ && !packet_ && path_refill_wave(refill_mode_, deep_groups, groups)) {
+    if (fused_ && !packet_ && groups < (1u << 29) && path_refill_wave(refill_mode_, deep_groups, groups)) {
         if (groups > group_em_cap_) {
-            uint32_t cap = groups > 2 * group_em_cap_ ? groups : 2 * group_em_cap_;
+            uint64_t twice = 2ull * group_em_cap_;
+            uint32_t cap = (uint64_t)groups > twice ? groups : (uint32_t)(twice < (1ull << 29) ? twice : (1ull << 29));
             if (d_group_em_) {
                 cudaFree(d_group_em_);
                 owned_.erase(std::remove(owned_.begin(), owned_.end(), (void*)d_group_em_), owned_.end());
