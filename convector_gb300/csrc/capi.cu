@@ -2,6 +2,7 @@
 // nearest-hit queries and frame rendering.
 #include <cuda_runtime.h>
 
+#include <cmath>
 #include <cstring>
 #include <memory>
 #include <mutex>
@@ -96,6 +97,7 @@ struct cvx_scene {
     // translation over a coherent CPU-GPU link): the host-buffer query may
     // read the caller's ray arrays in place. host_access: CVX_HOST_ACCESS_*.
     bool host_page_tables = false;
+    bool slab_sel = false;  // DeviceScene::slab_sel
     uint32_t host_access = CVX_HOST_ACCESS_AUTO;
     bool reads_host_in_place() const { return host_page_tables && host_access == CVX_HOST_ACCESS_AUTO; }
     // scratch for the host-buffer query
@@ -121,6 +123,7 @@ struct cvx_scene {
         s.n_lights = n_lights;
         s.general_pick = general_pick;
         s.depth = depth;
+        s.slab_sel = slab_sel ? 1u : 0u;
         return s;
     }
     ~cvx_scene() {
@@ -246,6 +249,16 @@ int32_t cvx_scene_create(const cvx_triangle* tris, uint32_t n_tris, const cvx_bv
     if ((st = dalloc(&s->d_shade, n_tris, "shading data"))) return st;
     if ((st = dalloc(&s->d_lights, (size_t)s->n_lights * 5, "lights"))) return st;
     if ((st = dalloc(&s->d_err, 2, "status"))) return st;  // [0] status, [1] ray counter
+    // The select-form slab test (box_test_sel) needs every bound finite and
+    // ordered, and none -0.
+    s->slab_sel = true;
+    for (uint32_t i = 0; i < n_nodes && s->slab_sel; i++)
+        for (int c = 0; c < 3; c++) {
+            const float lo = nodes[i].origin[c], hi = nodes[i].far_[c];
+            if (!std::isfinite(lo) || !std::isfinite(hi) || !(lo <= hi) || (lo == 0.0f && std::signbit(lo)) ||
+                (hi == 0.0f && std::signbit(hi)))
+                s->slab_sel = false;
+        }
     // Node pairs: q0 = lo0 hi0.x | q1 = hi0.yz lo1.xy | q2 = lo1.z hi1 | q3 = index/len x2
     std::vector<float4> pairs((size_t)n_nodes / 2 * 4);
     for (uint32_t p = 0; p < n_nodes / 2; p++) {

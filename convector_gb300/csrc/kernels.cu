@@ -111,6 +111,8 @@ __global__ void __launch_bounds__(256) k_intersect(DeviceScene s, const RayCols 
     }
 }
 
+constexpr int32_t kDeferredRay = -2;  // never a hit index: -1 is the miss
+
 // Ray source of the isolated nearest-hit query: SoA rays in, (t, index) out.
 struct SoaRays {
     const float4* nodes;
@@ -130,6 +132,8 @@ struct SoaRays {
         far = far_dist;
         return true;
     }
+    // A ray left to k_intersect_deferred (its index word holds kDeferredRay).
+    __device__ __forceinline__ void defer(uint32_t r) const { tri_out[r] = kDeferredRay; }
     __device__ __forceinline__ void store(uint32_t r, const Hit& h, uint32_t na, uint32_t nt) const {
         t_out[r] = h.t;
         tri_out[r] = h.tri;
@@ -224,7 +228,10 @@ struct StagedSoaClaim {
 // carve-out takes, measured no gain or a loss.)
 constexpr int kQueryStackShared = 8;
 
-template <int MINB, bool COUNT, int CLAIM>
+// SELECT: the select-form slab test for the rays that meet its conditions
+// (on scenes that do); the others are marked kDeferredRay and traced by
+// k_intersect_deferred. Measured on 4M rays: 0.844 against 0.877 ms.
+template <int MINB, bool COUNT, int CLAIM, bool SELECT>
 __global__ void __launch_bounds__(128, MINB) k_intersect_refill(SoaRays src, uint32_t* __restrict__ next_ray,
                                                                 uint32_t* __restrict__ err) {
     // The reciprocal table is read three times per ray: from global memory
@@ -233,8 +240,34 @@ __global__ void __launch_bounds__(128, MINB) k_intersect_refill(SoaRays src, uin
     __shared__ uint2 sstack[4][kQueryStackShared][32];
     StagedSoaClaim claim{src, next_ray, stage[threadIdx.x >> 5], 0u, 0u, 0u, 0};
     claim.init(threadIdx.x & 31);
-    bool ok = traverse_refill<COUNT, false, CLAIM, kQueryStackShared>(
+    bool ok = traverse_refill<COUNT, false, CLAIM, kQueryStackShared, SELECT>(
         src, claim, g_tables, &sstack[threadIdx.x >> 5][0][threadIdx.x & 31]);
+    if (!ok) atomicOr(err, kErrStackOverflow);
+}
+
+// After k_intersect_refill<SELECT>: the rays it left (index word kDeferredRay:
+// a reciprocal infinite or below 0.75 in magnitude) with the x86-form slab
+// test, one thread per ray. Such rays are rare (axis-parallel or very long
+// directions), so the scan over the index words is most of the work.
+__global__ void __launch_bounds__(128) k_intersect_deferred(SoaRays src, uint32_t* __restrict__ err) {
+    bool ok = true;
+    for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < src.n; r += gridDim.x * blockDim.x) {
+        if (src.tri_out[r] != kDeferredRay) continue;
+        F3 o, d;
+        float far;
+        const float4 *nodes, *geom;
+        src.load(r, o, d, far, nodes, geom);
+        RefillRay ray;
+        uint2 local_stack[kStackDepth];
+        LocalStack stack{local_stack};
+        ray.top = make_uint2(0u, 0u);
+        ray.start(o, d, far, nodes, geom, g_tables);
+        bool overflow = false;
+        while (!ray.step<false, false>(stack, overflow)) {
+        }
+        ok &= !overflow;
+        src.store(r, ray.h, 0u, 0u);
+    }
     if (!ok) atomicOr(err, kErrStackOverflow);
 }
 
@@ -551,15 +584,23 @@ cudaError_t launch_intersect(const DeviceScene& s, const RayCols& rays, uint32_t
         if (blocks > need) blocks = need;
         SoaRays src{s.nodes, s.geom, rays, n, far_dist, t_out, tri_out, counters};
         bool deep = s.depth > 40;
-        if (counters) k_intersect_refill<8, true, 16><<<blocks, 128, 0, st>>>(src, err + 1, err);
-        else if (deep) {
-            if (bps >= 12) k_intersect_refill<12, false, 8><<<blocks, 128, 0, st>>>(src, err + 1, err);
-            else if (bps >= 10) k_intersect_refill<10, false, 8><<<blocks, 128, 0, st>>>(src, err + 1, err);
-            else k_intersect_refill<8, false, 8><<<blocks, 128, 0, st>>>(src, err + 1, err);
+        const bool sel = s.slab_sel != 0u && !counters;
+        if (counters) k_intersect_refill<8, true, 16, false><<<blocks, 128, 0, st>>>(src, err + 1, err);
+        else if (!sel) {  // x86-form slab test throughout
+            if (deep) k_intersect_refill<8, false, 8, false><<<blocks, 128, 0, st>>>(src, err + 1, err);
+            else k_intersect_refill<8, false, 16, false><<<blocks, 128, 0, st>>>(src, err + 1, err);
+        } else if (deep) {
+            if (bps >= 12) k_intersect_refill<12, false, 8, true><<<blocks, 128, 0, st>>>(src, err + 1, err);
+            else if (bps >= 10) k_intersect_refill<10, false, 8, true><<<blocks, 128, 0, st>>>(src, err + 1, err);
+            else k_intersect_refill<8, false, 8, true><<<blocks, 128, 0, st>>>(src, err + 1, err);
         } else {
-            if (bps >= 12) k_intersect_refill<12, false, 16><<<blocks, 128, 0, st>>>(src, err + 1, err);
-            else if (bps >= 10) k_intersect_refill<10, false, 16><<<blocks, 128, 0, st>>>(src, err + 1, err);
-            else k_intersect_refill<8, false, 16><<<blocks, 128, 0, st>>>(src, err + 1, err);
+            if (bps >= 12) k_intersect_refill<12, false, 16, true><<<blocks, 128, 0, st>>>(src, err + 1, err);
+            else if (bps >= 10) k_intersect_refill<10, false, 16, true><<<blocks, 128, 0, st>>>(src, err + 1, err);
+            else k_intersect_refill<8, false, 16, true><<<blocks, 128, 0, st>>>(src, err + 1, err);
+        }
+        if (sel) {
+            uint32_t db = (n + 127u) / 128u, cap = (uint32_t)num_sms() * 8u;
+            k_intersect_deferred<<<db < cap ? db : cap, 128, 0, st>>>(src, err);
         }
         return cudaGetLastError();
     }

@@ -34,6 +34,9 @@ struct DeviceScene {
     uint32_t n_nodes, n_tris, n_lights;
     uint32_t general_pick;  // 1: (bits * n) >> 32; 0: bits >> 29 (needs n == 8)
     uint32_t depth;         // BVH depth (launch choices only)
+    // Every node bound is finite, lo <= hi on each axis and none is -0: the
+    // ray-cast kernel may take the select-form slab test (box_test_sel).
+    uint32_t slab_sel;
 };
 
 struct DeviceCamera {

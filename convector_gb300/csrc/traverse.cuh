@@ -39,6 +39,34 @@ __device__ __forceinline__ BoxT box_test(float lx, float ly, float lz, float hx,
     return BoxT{tmin, tmax, geq(tmax, tmin)};
 }
 
+// The slab test in select form: the near and far plane of each axis are
+// picked by the sign of the ray's reciprocal instead of by the x86 min/max of
+// the two plane distances (one select for each compare-and-select). It gives
+// the bits of box_test when every bound is finite, lo <= hi and no bound is -0
+// (DeviceScene::slab_sel), and the reciprocals are finite with |1/d| >= 0.75
+// (select_form_ray). With a positive reciprocal, rounding keeps
+// (lo - o) / d <= (hi - o) / d; x86 min takes the first and max the second, and
+// on equal values the second, which then has the same bits: a zero difference
+// is +0 without -0 bounds, and a non-zero one does not round to a zero at
+// |1/d| >= 0.75. A negative reciprocal swaps the two.
+__device__ __forceinline__ BoxT box_test_sel(float lx, float ly, float lz, float hx, float hy, float hz, F3 o,
+                                             F3 inv) {
+    const bool px = inv.x > 0.0f, py = inv.y > 0.0f, pz = inv.z > 0.0f;
+    float tx1 = (lx - o.x) * inv.x, tx2 = (hx - o.x) * inv.x;
+    float ty1 = (ly - o.y) * inv.y, ty2 = (hy - o.y) * inv.y;
+    float tz1 = (lz - o.z) * inv.z, tz2 = (hz - o.z) * inv.z;
+    float nx = px ? tx1 : tx2, fx = px ? tx2 : tx1;
+    float ny = py ? ty1 : ty2, fy = py ? ty2 : ty1;
+    float nz = pz ? tz1 : tz2, fz = pz ? tz2 : tz1;
+    float tmin = xmax(nx, xmax(ny, nz));
+    float tmax = xmin(fx, xmin(fy, fz));
+    return BoxT{tmin, tmax, geq(tmax, tmin)};
+}
+__device__ __forceinline__ bool select_form_ray(F3 inv) {
+    return isfinite(inv.x) && isfinite(inv.y) && isfinite(inv.z) && fabsf(inv.x) >= 0.75f &&
+           fabsf(inv.y) >= 0.75f && fabsf(inv.z) >= 0.75f;
+}
+
 // One triangle against one lane; updates the hit when the reference would
 // pick the new intersection (triangle.rs:122-147).
 __device__ __forceinline__ void tri_test(const float4* __restrict__ geom, uint32_t i, F3 o, F3 d, bool active,
@@ -229,8 +257,9 @@ struct RefillRay {
 
     // Returns true when the ray is finished (its stack is empty): h is then
     // its nearest hit. Sets `overflow` (and finishes the ray) when the stack
-    // would overflow.
-    template <bool COUNT, bool LEAF_AFTER_PAIR, class Stack>
+    // would overflow. SELECT: the slab test in select form (box_test_sel; the
+    // scene and the ray must meet its conditions).
+    template <bool COUNT, bool LEAF_AFTER_PAIR, bool SELECT = false, class Stack>
     __device__ __forceinline__ bool step(Stack& stack, bool& overflow) {
         if (cur == kNone) {
             // Pop until an entry survives the cull test (aabb.rs:171-177).
@@ -262,8 +291,14 @@ struct RefillRay {
             if (COUNT && cur != 0u) na += 2;  // every pair but the root pair (bvh.rs:604-634)
             const float4* np = nodes + 4 * (idx >> 1);
             float4 q0 = __ldg(np), q1 = __ldg(np + 1), q2 = __ldg(np + 2), q3 = __ldg(np + 3);
-            BoxT b0 = box_test(q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, o, inv);
-            BoxT b1 = box_test(q1.z, q1.w, q2.x, q2.y, q2.z, q2.w, o, inv);
+            BoxT b0, b1;
+            if constexpr (SELECT) {
+                b0 = box_test_sel(q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, o, inv);
+                b1 = box_test_sel(q1.z, q1.w, q2.x, q2.y, q2.z, q2.w, o, inv);
+            } else {
+                b0 = box_test(q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, o, inv);
+                b1 = box_test(q1.z, q1.w, q2.x, q2.y, q2.z, q2.w, o, inv);
+            }
             bool first0 = !sneg(b0.tmin - b1.tmin);
             bool hit0 = b0.mask & !sneg(b0.tmax);
             bool hit1 = b1.mask & !sneg(b1.tmax);
@@ -325,7 +360,11 @@ __device__ __forceinline__ typename std::conditional<N == 0, LocalStack, SharedL
 // CLAIM_MIN: lanes without a ray wait until that many want one; results do
 // not depend on it (each ray's traversal is independent of when it starts).
 // Returns false if a ray overflowed the stack (its hit is then incomplete).
-template <bool COUNT, bool LEAF_AFTER_PAIR, int CLAIM_MIN, int SHARED_STACK = 0, class Src, class Claim>
+// SELECT: every ray whose reciprocals meet select_form_ray is traversed with
+// the select-form slab test; the others are handed to src.defer(r) untraced
+// (the caller traces them afterwards with the x86 form).
+template <bool COUNT, bool LEAF_AFTER_PAIR, int CLAIM_MIN, int SHARED_STACK = 0, bool SELECT = false, class Src,
+          class Claim>
 __device__ __forceinline__ bool traverse_refill(const Src& src, Claim& claim, const ApproxTables& tab,
                                                 uint2* shared_stack = nullptr) {
     const int lane = threadIdx.x & 31;
@@ -359,6 +398,12 @@ __device__ __forceinline__ bool traverse_refill(const Src& src, Claim& claim, co
                     r_id = r;
                     ray.start(in.o, in.d, in.far, in.nodes, in.geom, tab);
                     have = true;
+                    if constexpr (SELECT) {
+                        if (!select_form_ray(ray.inv)) {
+                            src.defer(r);
+                            have = false;
+                        }
+                    }
                 } else if (got == kClaimDone) {
                     done = true;
                 }
@@ -366,7 +411,7 @@ __device__ __forceinline__ bool traverse_refill(const Src& src, Claim& claim, co
         }
         if (__all_sync(0xffffffffu, done)) break;
         if (!have) continue;
-        if (ray.step<COUNT, LEAF_AFTER_PAIR>(stack, overflow)) {
+        if (ray.step<COUNT, LEAF_AFTER_PAIR, SELECT>(stack, overflow)) {
             src.store(r_id, ray.h, ray.na, ray.nt);
             have = false;
         }
