@@ -252,6 +252,13 @@ def run_ours(args):
     best = min(trial, key=trial.get)
     trav = 0 if best.startswith("packet8") else 1
     scene.set_query_launch(int(best.split("/")[1]))
+    # Kernels per step: the single-ray query on a scene whose node bounds are
+    # finite, ordered and free of -0 runs the select-form kernel and the pass
+    # over the rays it deferred (the library's check at scene creation).
+    nb = bvh.nodes_f32.reshape(-1, 8)[:, :6]
+    select_form = bool(np.isfinite(nb).all() and (nb[:, :3] <= nb[:, 3:]).all()
+                       and not ((nb == 0) & np.signbit(nb)).any())
+    launches_per_step = 2 if (trav == 1 and select_form) else 1
 
     for _ in range(args.warmup):
         flush.zero_()
@@ -351,7 +358,7 @@ def run_ours(args):
                          "kernel": kname},
             "cpu_baseline": cpu,
             "clocks": clocks.summary(),
-            "gpu_launches": args.steps,
+            "gpu_launches": args.steps * launches_per_step,
             "wall_s_timed": wall,
             "step_ms_p50": statistics.median(step_ms),
             "render": render,
