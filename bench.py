@@ -237,7 +237,12 @@ def run_ours(args):
 
     # Pick the faster traversal variant and launch shape on a short untimed trial.
     trial = {}
-    for trav, bps in ((0, 0), (1, 8), (1, 10), (1, 12)):
+    shapes = ((0, 0), (1, 8), (1, 10), (1, 12))
+    if args.launch:  # a fixed shape (reproducible profiles): no trial
+        shapes = tuple(x for x in shapes if "%s/%d" % ("packet8" if x[0] == 0 else "single", x[1]) == args.launch)
+        if not shapes:
+            raise SystemExit("--launch: one of packet8/0, single/8, single/10, single/12")
+    for trav, bps in shapes:
         scene.set_query_launch(bps)
         for _ in range(2):
             step(trav)
@@ -662,6 +667,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-render", action="store_true")
     ap.add_argument("--no-extra", action="store_true", help="skip the large, batched and served sections")
+    ap.add_argument("--launch", help="query launch shape (packet8/0, single/8, single/10, single/12) instead of "
+                                     "the fastest of a short timed trial")
     ap.add_argument("--section", choices=["render", "large", "batched", "served", "bvh"],
                     help="run one extra section alone and print its JSON (no headline line)")
     args = ap.parse_args()

@@ -247,12 +247,24 @@ __global__ void __launch_bounds__(128, MINB) k_intersect_refill(SoaRays src, uin
 
 // After k_intersect_refill<SELECT>: the rays it left (index word kDeferredRay:
 // a reciprocal infinite or below 0.75 in magnitude) with the x86-form slab
-// test, one thread per ray. Such rays are rare (axis-parallel or very long
-// directions), so the scan over the index words is most of the work.
-__global__ void __launch_bounds__(128) k_intersect_deferred(SoaRays src, uint32_t* __restrict__ err) {
+// test. Such rays are rare (axis-parallel or very long directions), so the
+// scan over the index words is most of the work: each thread reads
+// kDeferredScan words spread over the whole array, independent coalesced loads
+// in one round (a grid-stride loop of dependent loads took 16 us per 4M rays).
+constexpr uint32_t kDeferredScan = 4;
+__global__ void __launch_bounds__(256) k_intersect_deferred(SoaRays src, uint32_t* __restrict__ err) {
+    const uint32_t stride = gridDim.x * blockDim.x, t = blockIdx.x * blockDim.x + threadIdx.x;
+    int32_t w[kDeferredScan];
+#pragma unroll
+    for (uint32_t k = 0; k < kDeferredScan; k++) {
+        const uint64_t r = (uint64_t)t + (uint64_t)k * stride;
+        w[k] = r < src.n ? __ldg(src.tri_out + r) : 0;
+    }
     bool ok = true;
-    for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < src.n; r += gridDim.x * blockDim.x) {
-        if (src.tri_out[r] != kDeferredRay) continue;
+#pragma unroll 1
+    for (uint32_t k = 0; k < kDeferredScan; k++) {
+        if (w[k] != kDeferredRay) continue;
+        const uint32_t r = t + k * stride;
         F3 o, d;
         float far;
         const float4 *nodes, *geom;
@@ -599,8 +611,8 @@ cudaError_t launch_intersect(const DeviceScene& s, const RayCols& rays, uint32_t
             else k_intersect_refill<8, false, 16, true><<<blocks, 128, 0, st>>>(src, err + 1, err);
         }
         if (sel) {
-            uint32_t db = (n + 127u) / 128u, cap = (uint32_t)num_sms() * 8u;
-            k_intersect_deferred<<<db < cap ? db : cap, 128, 0, st>>>(src, err);
+            const uint32_t per_block = 256u * kDeferredScan;
+            k_intersect_deferred<<<(n + per_block - 1u) / per_block, 256, 0, st>>>(src, err);
         }
         return cudaGetLastError();
     }
