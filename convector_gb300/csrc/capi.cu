@@ -2,6 +2,7 @@
 // nearest-hit queries and frame rendering.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <memory>
@@ -85,7 +86,8 @@ bool page_locked(const void* p) {
 
 struct cvx_scene {
     int device = 0;
-    float4* d_nodes = nullptr;
+    float4* d_nodes = nullptr;  // escape slots (node_offset float4), then the node pairs
+    size_t node_offset = 0;
     float4* d_geom = nullptr;
     TriShade* d_shade = nullptr;
     float4* d_lights = nullptr;
@@ -114,7 +116,7 @@ struct cvx_scene {
 
     DeviceScene view() const {
         DeviceScene s;
-        s.nodes = d_nodes;
+        s.nodes = d_nodes + node_offset;
         s.geom = d_geom;
         s.shade = d_shade;
         s.lights = d_lights;
@@ -244,7 +246,6 @@ int32_t cvx_scene_create(const cvx_triangle* tris, uint32_t n_tris, const cvx_bv
     s->n_lights = (uint32_t)ds.size();
     s->depth = depth;
     CK(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking), "cudaStreamCreate");
-    if ((st = dalloc(&s->d_nodes, (size_t)n_nodes * 2, "nodes"))) return st;
     if ((st = dalloc(&s->d_geom, (size_t)n_tris * 3, "triangles"))) return st;
     if ((st = dalloc(&s->d_shade, n_tris, "shading data"))) return st;
     if ((st = dalloc(&s->d_lights, (size_t)s->n_lights * 5, "lights"))) return st;
@@ -260,6 +261,18 @@ int32_t cvx_scene_create(const cvx_triangle* tris, uint32_t n_tris, const cvx_bv
                 s->slab_sel = false;
         }
     // Node pairs: q0 = lo0 hi0.x | q1 = hi0.yz lo1.xy | q2 = lo1.z hi1 | q3 = index/len x2
+    // q3 holds the two children's stack references, the form the traversal
+    // pushes (traverse.cuh): (index << 5) | len for internal nodes (len 0, index =
+    // first child) and leaves of up to 30 triangles; (slot << 5) | 31 for larger
+    // leaves, whose (index, len) is escape slot `slot`, the float4 at
+    // nodes[-1 - slot] below the pairs (the region is padded to 8 float4, so the
+    // pairs keep their 128-byte alignment).
+    std::vector<uint2> esc;
+    auto child_ref = [&esc](const cvx_bvh_node& nd) -> uint32_t {
+        if (nd.len < 31u) return (nd.index << 5) | nd.len;
+        esc.push_back(make_uint2(nd.index, nd.len));
+        return ((uint32_t)(esc.size() - 1) << 5) | 31u;
+    };
     std::vector<float4> pairs((size_t)n_nodes / 2 * 4);
     for (uint32_t p = 0; p < n_nodes / 2; p++) {
         const cvx_bvh_node& a = nodes[2 * p];
@@ -268,10 +281,19 @@ int32_t cvx_scene_create(const cvx_triangle* tris, uint32_t n_tris, const cvx_bv
         q[0] = make_float4(a.origin[0], a.origin[1], a.origin[2], a.far_[0]);
         q[1] = make_float4(a.far_[1], a.far_[2], b.origin[0], b.origin[1]);
         q[2] = make_float4(b.origin[2], b.far_[0], b.far_[1], b.far_[2]);
-        uint32_t w[4] = {a.index, a.len, b.index, b.len};
+        uint32_t w[4] = {child_ref(a), child_ref(b), 0u, 0u};
         std::memcpy(&q[3], w, 16);
     }
-    CK(cudaMemcpyAsync(s->d_nodes, pairs.data(), pairs.size() * sizeof(float4), cudaMemcpyHostToDevice, s->stream),
+    s->node_offset = (esc.size() + 7) / 8 * 8;
+    std::vector<float4> node_buf(s->node_offset + pairs.size());
+    for (size_t k = 0; k < esc.size(); k++) {
+        uint32_t e[4] = {esc[k].x, esc[k].y, 0u, 0u};
+        std::memcpy(&node_buf[s->node_offset - 1 - k], e, 16);
+    }
+    std::copy(pairs.begin(), pairs.end(), node_buf.begin() + (std::ptrdiff_t)s->node_offset);
+    if ((st = dalloc(&s->d_nodes, node_buf.size(), "nodes"))) return st;
+    CK(cudaMemcpyAsync(s->d_nodes, node_buf.data(), node_buf.size() * sizeof(float4), cudaMemcpyHostToDevice,
+                       s->stream),
        "upload nodes");
     cvx_triangle* d_src = nullptr;
     uint32_t* d_ds = nullptr;

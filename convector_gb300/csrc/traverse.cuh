@@ -89,6 +89,24 @@ __device__ __forceinline__ void tri_test(const float4* __restrict__ geom, uint32
     }
 }
 
+// Node references: the two children's entries in a node pair's last float4
+// (q3.x, q3.y), as the scene upload writes them and the traversal stacks hold
+// them. (index << 5) | len: len 0 is an internal node (index = its first
+// child), len 1..30 a leaf of len triangles at index; len 31 escapes larger
+// leaves, index being the slot of their (index, len) in the float4 at
+// nodes[-1 - slot]. Indices are below 2^27 (checked at scene creation).
+// The escape is marked unlikely: as an ordinary branch in the packet
+// traversal's pop loop it made that traversal up to 1.6x slower, even never
+// taken (with the hint, and the stack holding references, the room frame runs
+// 0.823 against 0.840 ms with (index, len) pairs on the stack).
+__device__ __forceinline__ void leaf_range(const float4* __restrict__ nodes, uint32_t& idx, uint32_t& len) {
+    if (__builtin_expect(len == 31u, 0)) {
+        const float4 e = __ldg(nodes - 1 - (size_t)idx);
+        idx = __float_as_uint(e.x);
+        len = __float_as_uint(e.y);
+    }
+}
+
 __device__ __forceinline__ bool oct_all(unsigned m, bool p) { return (__ballot_sync(m, p) & m) == m; }
 __device__ __forceinline__ bool oct_any(unsigned m, bool p) { return (__ballot_sync(m, p) & m) != 0u; }
 
@@ -103,8 +121,7 @@ template <bool PACKET>
 __device__ __forceinline__ bool traverse(const DeviceScene& s, F3 o, F3 d, bool active, unsigned omask, Hit& h,
                                          const ApproxTables& tab, Counters* cnt) {
     F3 inv = f3(x_rcp(d.x, tab), x_rcp(d.y, tab), x_rcp(d.z, tab));
-    uint32_t st_idx[kStackDepth];
-    uint32_t st_len[kStackDepth];
+    uint32_t st_ref[kStackDepth];  // node references (leaf_range)
     float st_t[kStackDepth];
     int sp = 0;
     uint32_t na = 2, nt = 0;
@@ -128,25 +145,24 @@ __device__ __forceinline__ bool traverse(const DeviceScene& s, F3 o, F3 d, bool 
         // Lanes outside the box never block a cull (aabb.rs:171-177): +inf.
         float c0 = b0.mask ? b0.tmin : __int_as_float(0x7f800000);
         float c1 = b1.mask ? b1.tmin : __int_as_float(0x7f800000);
-        uint32_t i0 = __float_as_uint(q3.x), l0 = __float_as_uint(q3.y);
-        uint32_t i1 = __float_as_uint(q3.z), l1 = __float_as_uint(q3.w);
+        const uint32_t r0 = __float_as_uint(q3.x), r1 = __float_as_uint(q3.y);
         int need = (int)hit0 + (int)hit1;
         if (sp + need > kStackDepth) {
             ok = false;
             break;
         }
         if (first0) {
-            if (hit0) { st_idx[sp] = i0; st_len[sp] = l0; st_t[sp] = c0; sp++; }
-            if (hit1) { st_idx[sp] = i1; st_len[sp] = l1; st_t[sp] = c1; sp++; }
+            if (hit0) { st_ref[sp] = r0; st_t[sp] = c0; sp++; }
+            if (hit1) { st_ref[sp] = r1; st_t[sp] = c1; sp++; }
         } else {
-            if (hit1) { st_idx[sp] = i1; st_len[sp] = l1; st_t[sp] = c1; sp++; }
-            if (hit0) { st_idx[sp] = i0; st_len[sp] = l0; st_t[sp] = c0; sp++; }
+            if (hit1) { st_ref[sp] = r1; st_t[sp] = c1; sp++; }
+            if (hit0) { st_ref[sp] = r0; st_t[sp] = c0; sp++; }
         }
         // Pop until an internal node whose children must be tested.
         bool descend = false;
         while (sp > 0) {
             sp--;
-            uint32_t idx = st_idx[sp], len = st_len[sp];
+            uint32_t idx = st_ref[sp] >> 5, len = st_ref[sp] & 31u;
             bool skip = !active | geq(st_t[sp], h.t);
             if (PACKET) skip = oct_all(omask, skip);
             if (skip) continue;
@@ -156,6 +172,7 @@ __device__ __forceinline__ bool traverse(const DeviceScene& s, F3 o, F3 d, bool 
                 descend = true;
                 break;
             }
+            leaf_range(s.nodes, idx, len);
             for (uint32_t i = idx; i < idx + len; i++) tri_test(s.geom, i, o, d, active, h);
             nt += len;
         }
@@ -166,15 +183,6 @@ __device__ __forceinline__ bool traverse(const DeviceScene& s, F3 o, F3 d, bool 
         cnt->tri = nt;
     }
     return ok;
-}
-
-// Stack entry of the refill traversal: a packed node reference and the box's
-// entry distance, 8 bytes. ref = (index << 5) | len: len 0 is an internal node
-// (index = its first child), len 1..30 a leaf of len triangles at index; len
-// 31 escapes larger leaves (index = the node's own id, its (index, len) are
-// read from the node pair). Indices are below 2^27 (checked at scene creation).
-__device__ __forceinline__ uint32_t node_ref(uint32_t node_id, uint32_t index, uint32_t len) {
-    return len < 31u ? (index << 5) | len : (node_id << 5) | 31u;
 }
 
 // Asynchronous global-to-shared copies (cp.async) for staging rays.
@@ -255,6 +263,10 @@ struct RefillRay {
         cur = 0;  // the root pair: internal ref with index 0
     }
 
+    // The leaf loops are not unrolled: len is bounded by its 5 bits, and the
+    // compiler's unrolled copies of tri_test cost more in instruction fetch
+    // than the loop (4M-ray query 0.825 -> 0.808 ms, tube frame 3.24 -> 3.11 ms).
+    //
     // Returns true when the ray is finished (its stack is empty): h is then
     // its nearest hit. Sets `overflow` (and finishes the ray) when the stack
     // would overflow. SELECT: the slab test in select form (box_test_sel; the
@@ -275,12 +287,8 @@ struct RefillRay {
         }
         uint32_t len = cur & 31u, idx = cur >> 5;
         if (!LEAF_AFTER_PAIR && len != 0u) {  // a popped leaf; the pair loop continues next iteration
-            if (len == 31u) {  // escaped leaf: read its (index, len) from the node pair
-                uint32_t id = idx;
-                float4 q3 = __ldg(nodes + 4 * (id >> 1) + 3);
-                idx = __float_as_uint((id & 1u) ? q3.z : q3.x);
-                len = __float_as_uint((id & 1u) ? q3.w : q3.y);
-            }
+            leaf_range(nodes, idx, len);
+#pragma unroll 1
             for (uint32_t i = idx; i < idx + len; i++) tri_test(geom, i, o, d, true, h);
             if (COUNT) nt += len;
             cur = kNone;
@@ -302,8 +310,7 @@ struct RefillRay {
             bool first0 = !sneg(b0.tmin - b1.tmin);
             bool hit0 = b0.mask & !sneg(b0.tmax);
             bool hit1 = b1.mask & !sneg(b1.tmax);
-            uint32_t r0 = node_ref(idx, __float_as_uint(q3.x), __float_as_uint(q3.y));
-            uint32_t r1 = node_ref(idx + 1u, __float_as_uint(q3.z), __float_as_uint(q3.w));
+            const uint32_t r0 = __float_as_uint(q3.x), r1 = __float_as_uint(q3.y);
             // The reference pushes `first` then `second` and pops `second` first.
             bool hit_first = first0 ? hit0 : hit1, hit_second = first0 ? hit1 : hit0;
             uint32_t ref_first = first0 ? r0 : r1, ref_second = first0 ? r1 : r0;
@@ -327,12 +334,8 @@ struct RefillRay {
         // LEAF_AFTER_PAIR: a leaf, popped or reached from the pair just tested
         // (the reference would pop it next with no decision in between).
         if (len != 0u) {
-            if (len == 31u) {  // escaped leaf: read its (index, len) from the node pair
-                uint32_t id = idx;
-                float4 q3 = __ldg(nodes + 4 * (id >> 1) + 3);
-                idx = __float_as_uint((id & 1u) ? q3.z : q3.x);
-                len = __float_as_uint((id & 1u) ? q3.w : q3.y);
-            }
+            leaf_range(nodes, idx, len);
+#pragma unroll 1
             for (uint32_t i = idx; i < idx + len; i++) tri_test(geom, i, o, d, true, h);
             if (COUNT) nt += len;
             cur = kNone;
