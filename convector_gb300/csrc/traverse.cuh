@@ -297,7 +297,10 @@ struct RefillRay {
         if (len == 0u) {
             // An internal node: test its two children.
             if (COUNT && cur != 0u) na += 2;  // every pair but the root pair (bvh.rs:604-634)
-            const float4* np = nodes + 4 * (idx >> 1);
+            // The reference of an internal node is its first child's index (even:
+            // checked at scene creation) times 32, which is the byte offset of
+            // the child pair (64 bytes per pair).
+            const float4* np = reinterpret_cast<const float4*>(reinterpret_cast<const char*>(nodes) + cur);
             float4 q0 = __ldg(np), q1 = __ldg(np + 1), q2 = __ldg(np + 2), q3 = __ldg(np + 3);
             BoxT b0, b1;
             if constexpr (SELECT) {
