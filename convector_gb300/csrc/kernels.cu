@@ -449,7 +449,7 @@ struct FramePaths {
         }
     }
     __device__ __forceinline__ void count_ray(const PathRef&) { rays++; }
-    __device__ __forceinline__ void finish() { flush_rays(a, rays); }
+    __device__ __forceinline__ void finish(const PathRef&) { flush_rays(a, rays); }
 };
 
 // Launch shape and loop form of the per-lane path refill, each measured on the

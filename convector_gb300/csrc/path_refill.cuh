@@ -32,7 +32,7 @@
 //       registers through the shading code, which stores to the images)
 //   void gbuffer(const PathRef&, uint32_t word), void mark_emitter(const PathRef&)
 //   void store(const PathRef&, F3 colour)
-//   void count_ray(const PathRef&), void finish()  (finish: whole warp)
+//   void count_ray(const PathRef&), void finish(const PathRef& last)  (finish: whole warp)
 #pragma once
 #include "shade.cuh"
 #include "traverse.cuh"
@@ -135,7 +135,7 @@ __device__ __forceinline__ bool path_refill(Paths& P, const ApproxTables& tab) {
         for (int st = 0; st < STEPS && tracing; st++)
             if (ray.step<false, true>(stack, overflow)) tracing = false;
     }
-    P.finish();
+    P.finish(ref);
     return !overflow;
 }
 

@@ -400,8 +400,9 @@ __global__ void __launch_bounds__(128, 8) k_wave_fused(const Job* __restrict__ j
 
 // The paths of a wave for path_refill: path p is lane p & 7 of wave group
 // p >> 3, which belongs to the job whose group range holds it. Ray counts per
-// job are kept per lane for the job of its current path and added to the job's
-// total when the lane moves to another job, and at the end.
+// job are kept per lane for the job of its current path (the path reference's
+// job) and added to the job's total when the lane moves to another job, and at
+// the end.
 struct WavePaths {
     struct PathRef {
         uint32_t path, job;
@@ -410,7 +411,7 @@ struct WavePaths {
     const DeviceScene* __restrict__ scenes;
     const WaveOutputs& out;
     uint32_t n_jobs, n_groups;
-    uint32_t rays, job_cur, job_acc;
+    uint32_t rays, job_acc;
 
     __device__ __forceinline__ uint32_t n_paths() const { return n_groups * 8u; }
     __device__ __forceinline__ uint32_t claim(uint32_t n) { return atomicAdd(out.err + 1, n); }
@@ -427,7 +428,7 @@ struct WavePaths {
         // Paths are claimed in order, so the next one is mostly in the job of
         // the last: search the job table only when it is not.
         const uint32_t gi = p >> 3;
-        uint32_t ji = job_cur;
+        uint32_t ji = r.job;
         if (ji >= n_jobs || gi - __ldg(&jobs[ji].group_base) >= __ldg(&jobs[ji].n_groups))
             ji = find_job(jobs, n_jobs, gi);
         const Job& j = jobs[ji];
@@ -435,13 +436,12 @@ struct WavePaths {
         int g;
         group_origin(j, gi - j.group_base, &xb, &yb, &g, &gx, &gy);
         if (gx >= j.w || gy >= j.h) return false;
-        r.path = p;
-        r.job = ji;
-        if (ji != job_cur) {
-            if (out.job_rays && job_acc) atomicAdd(&out.job_rays[job_cur], (unsigned long long)job_acc);
-            job_cur = ji;
+        if (ji != r.job) {  // job_acc counts the rays of the previous path's job
+            if (out.job_rays && job_acc) atomicAdd(&out.job_rays[r.job], (unsigned long long)job_acc);
             job_acc = 0;
         }
+        r.path = p;
+        r.job = ji;
         const int k = (int)(p & 7u);
         float x, y, scale;
         block_coord_wf(j.w, j.h, xb, yb, g, k, &x, &y, &scale);
@@ -484,8 +484,8 @@ struct WavePaths {
         rays++;
         job_acc++;
     }
-    __device__ __forceinline__ void finish() {
-        if (out.job_rays && job_acc) atomicAdd(&out.job_rays[job_cur], (unsigned long long)job_acc);
+    __device__ __forceinline__ void finish(const PathRef& r) {
+        if (out.job_rays && job_acc) atomicAdd(&out.job_rays[r.job], (unsigned long long)job_acc);
         unsigned long long v = rays;
         for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
         if ((threadIdx.x & 31u) == 0u && v) atomicAdd(out.rays, v);
@@ -504,7 +504,7 @@ __global__ void __launch_bounds__(128, kRefillWaveBlocksPerSm) k_wave_refill(con
                                                                           WaveOutputs out) {
     __shared__ ApproxTables tab;
     load_tables_wf(tab);
-    WavePaths P{jobs, scenes, out, hdr->n_jobs, hdr->n_groups, 0u, 0xffffffffu, 0u};
+    WavePaths P{jobs, scenes, out, hdr->n_jobs, hdr->n_groups, 0u, 0u};
     if (!path_refill<CLAIM_MIN, 2>(P, tab)) atomicOr(out.err, kErrStackOverflow);
 }
 
