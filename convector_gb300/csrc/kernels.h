@@ -35,8 +35,8 @@ cudaError_t launch_intersect(const DeviceScene& s, const RayCols& rays, uint32_t
 // decides, and for a wave whether at least half of its groups belong to scenes
 // that deep. Measured at 1280x736 (octet against refill, ms per frame): the
 // 19-level room 0.82 / 0.73, the 28-level icosphere 1.87 / 1.45, the 70-level
-// tube 5.36 / 3.14; 256 scenes of 11 to 23 levels (median 16), batched: 57 / 69
-// ms, one at a time: 2,617 / 2,398 Mrays/s. Refill wins clearly from the
+// tube 5.36 / 3.14; 256 scenes of 11 to 23 levels (median 16), batched: 53 / 66
+// ms, one at a time: 2,808 / 2,546 Mrays/s. Refill wins clearly from the
 // icosphere's depth on; the shallow open scenes, whose paths are mostly one or
 // two rays, keep warps of neighbouring camera rays together.
 constexpr uint32_t kRefillMinDepth = 25;
