@@ -162,6 +162,42 @@ def test_host_access_rejects_bad_mode(gpu, icosphere):
         icosphere[1].set_host_access(7)
 
 
+def test_large_leaves_escape_bitexact(gpu, orc):
+    """Leaves of 31 or more triangles are stored as escape slots below the node
+    pairs. Coincident triangles share one barycentre and end in one leaf (300 and
+    40 of them among 2,000 random ones): hits through both traversals, with rays
+    aimed into those leaves and axis-parallel rays (the deferred x86-form pass),
+    equal the oracle's."""
+    rng = np.random.default_rng(21)
+    c = rng.uniform(-1.0, 1.0, (2000, 1, 3))
+    v = c + rng.normal(0.0, 0.05, (2000, 3, 3))
+    big = np.repeat(np.array([[[0.1, 0.2, 0.3], [0.4, 0.2, 0.3], [0.1, 0.6, 0.35]]]), 300, axis=0)
+    mid = np.repeat(np.array([[[-0.5, -0.4, 0.2], [-0.2, -0.4, 0.25], [-0.5, -0.1, 0.2]]]), 40, axis=0)
+    v = np.concatenate([v[:1000], big, v[1000:], mid]).astype(np.float32)
+    t16 = np.zeros((v.shape[0], 16), np.float32)
+    t16[:, :9] = v.reshape(-1, 9)
+    w = t16.view(np.uint32)
+    w[:, 15] = 0x00FFFFFF
+    bvh = gpu.Bvh.build(w)
+    lens = bvh.nodes.view(np.uint32).reshape(-1, 8)[:, 7]
+    assert (lens >= 31).sum() >= 2, "the scene must hold escaped leaves"
+    scene = gpu.Scene(bvh)
+    osc = orc.OracleScene.from_bvh(bvh)
+    n = 1 << 14
+    o = rng.uniform(-1.5, 1.5, (n, 3)).astype(np.float32)
+    targets = np.where(rng.random((n, 1)) < 0.5, big[0].mean(0), mid[0].mean(0))
+    d = np.where(rng.random((n, 1)) < 0.6, targets - o, rng.normal(size=(n, 3)))
+    d[:64] = np.eye(3)[rng.integers(0, 3, 64)] * np.sign(rng.normal(size=(64, 1)))  # axis-parallel
+    d = (d / np.linalg.norm(d, axis=1, keepdims=True)).astype(np.float32)
+    for traversal in (0, 1):
+        t, tri = scene.intersect_nearest(o, d, traversal=traversal)
+        ot, otri = osc.intersect(o, d, mode=traversal)
+        assert (tri == otri).all(), np.nonzero(tri != otri)[0][:10]
+        assert (t.view(np.uint32) == ot.view(np.uint32)).all()
+        coincident = np.nonzero(np.abs(bvh.triangles.view(np.float32)[:, :9] - big[0].reshape(9)).max(1) < 1e-6)[0]
+        assert np.isin(tri, coincident).any()  # rays reached the escaped leaves
+
+
 @pytest.mark.parametrize("launch", [8, 10, 12])
 def test_intersect_single_launch_shapes_bitexact(icosphere, orc, launch):
     """Every launch shape of the single-ray query (occupancy variants of the
