@@ -140,15 +140,18 @@ def test_server_mix_equals_alone(two_scenes, gpu, kernel_mode, refill):
         srv.close()
 
 
+@pytest.mark.parametrize("deep_single_launch", [0, 1])
 @pytest.mark.parametrize("wavefront_streams", [1, 2])
-def test_server_two_engines_concurrent_equal_alone(two_scenes, gpu, wavefront_streams):
-    """One scene in single-launch waves and one in wavefront waves, run
-    concurrently on two streams (the wavefront one at higher priority) with a
-    reduced single-launch block count: every image equals the same request
-    rendered alone, and both engines report device time."""
+def test_server_two_engines_concurrent_equal_alone(two_scenes, gpu, wavefront_streams, deep_single_launch):
+    """One scene in single-launch waves and one on the deep-scene engines
+    (wavefront waves, or with deep_single_launch single-launch waves with paths
+    per lane), run concurrently on their streams (the deep ones at higher
+    priority) with a reduced single-launch block count: every image equals the
+    same request rendered alone, and both engine kinds report device time."""
     scs = [s for _, s, _ in two_scenes]
     srv = gpu.Server(scs, framebuffer_bytes=64 << 20, max_groups=1 << 14, fused_blocks_per_sm=4,
-                     blocks_per_sm=10, refill_mode=gpu.REFILL_ALL, wavefront_streams=wavefront_streams)
+                     blocks_per_sm=10, refill_mode=gpu.REFILL_ALL, wavefront_streams=wavefront_streams,
+                     deep_single_launch=deep_single_launch)
     srv.set_scene_mode(0, gpu.MODE_MEGAKERNEL if wavefront_streams == 1 else gpu.MODE_WAVEFRONT)
     srv.set_scene_mode(1, gpu.MODE_WAVEFRONT)
     rng = np.random.default_rng(8)
