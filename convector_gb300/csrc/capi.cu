@@ -349,6 +349,7 @@ void cvx_scene_destroy(cvx_scene* s) { delete s; }
 
 int32_t cvx_intersect_nearest_device(cvx_scene* s, const float* rays, uint32_t n, float far_dist, uint32_t traversal,
                                      float* t_out, int32_t* tri_out, uint32_t* counters, void* stream) {
+    if (n > CVX_MAX_QUERY_RAYS) return set_error(CVX_ERR_INVALID, "a query takes at most 2^31 rays per call");
     if (!s || (!rays && n) || (!t_out && n) || (!tri_out && n)) return set_error(CVX_ERR_INVALID, "null argument");
     if (traversal > 1) return set_error(CVX_ERR_INVALID, "unknown traversal variant");
     if (n == 0) return CVX_OK;
@@ -362,6 +363,7 @@ int32_t cvx_intersect_nearest_device(cvx_scene* s, const float* rays, uint32_t n
 int32_t cvx_intersect_nearest(cvx_scene* s, const float* ox, const float* oy, const float* oz, const float* dx,
                               const float* dy, const float* dz, uint32_t n, float far_dist, uint32_t traversal,
                               float* t_out, int32_t* tri_out) {
+    if (n > CVX_MAX_QUERY_RAYS) return set_error(CVX_ERR_INVALID, "a query takes at most 2^31 rays per call");
     if (!s) return set_error(CVX_ERR_INVALID, "null scene");
     if (n == 0) return CVX_OK;
     if (!ox || !oy || !oz || !dx || !dy || !dz || !t_out || !tri_out) return set_error(CVX_ERR_INVALID, "null buffer");
@@ -440,7 +442,8 @@ int32_t cvx_intersect_nearest(cvx_scene* s, const float* ox, const float* oy, co
 int32_t cvx_renderer_create(cvx_scene* scene, uint32_t w, uint32_t h, const cvx_render_config* cfg,
                             cvx_renderer** out) {
     if (!scene || !out) return set_error(CVX_ERR_INVALID, "null argument");
-    if (w == 0 || h == 0 || w > 16384 || h > 16384) return set_error(CVX_ERR_INVALID, "frame size out of range");
+    if (w == 0 || h == 0 || w > kMaxImageSide || h > kMaxImageSide)
+        return set_error(CVX_ERR_INVALID, "frame size out of range");
     if (scene->n_lights == 0)
         return set_error(CVX_ERR_INVALID, "rendering needs at least one direct-sample triangle (scene.rs:143-161)");
     cvx_render_config c{};

@@ -166,19 +166,23 @@ int32_t WaveEngine::submit(const std::vector<Job>& jobs_in, WaveOutputs out, cud
     last_jobs_ = 0;
     last_want_ = want_job_rays;
     if (jobs_in.size() > max_jobs_) return set_error(CVX_ERR_CAPACITY, "too many jobs for one wave");
-    uint32_t groups = 0, depth = 0, deep_groups = 0;
+    uint64_t total = 0, deep_total = 0;
+    uint32_t depth = 0;
     for (size_t i = 0; i < jobs_in.size(); i++) {
         Job j = jobs_in[i];
         if (j.scene >= n_scenes_) return set_error(CVX_ERR_INVALID, "job scene outside the scene table");
+        if (j.w == 0 || j.h == 0 || j.w > kMaxImageSide || j.h > kMaxImageSide)
+            return set_error(CVX_ERR_INVALID, "job image size out of range");
         const uint32_t dj = scene_depth_[j.scene];
         depth = dj > depth ? dj : depth;
-        if (dj >= kRefillMinDepth) deep_groups += groups_of(j.w, j.h);
-        j.group_base = groups;
         j.n_groups = groups_of(j.w, j.h);
-        groups += j.n_groups;
+        if (dj >= kRefillMinDepth) deep_total += j.n_groups;
+        if (total + j.n_groups > max_groups_) return set_error(CVX_ERR_CAPACITY, "wave exceeds the ray-queue capacity");
+        j.group_base = (uint32_t)total;
+        total += j.n_groups;
         h_jobs_[i] = j;
     }
-    if (groups > max_groups_) return set_error(CVX_ERR_CAPACITY, "wave exceeds the ray-queue capacity");
+    const uint32_t groups = (uint32_t)total, deep_groups = (uint32_t)deep_total;
     h_hdr_->n_jobs = (uint32_t)jobs_in.size();
     h_hdr_->n_groups = groups;
     if (jobs_in.empty()) return CVX_OK;
@@ -189,12 +193,12 @@ int32_t WaveEngine::submit(const std::vector<Job>& jobs_in, WaveOutputs out, cud
     const bool deep = depth > 40;
     // Single-ray fused waves that take paths per lane (path_refill_wave):
     // one counter word per group of the wave, grown on demand, zeroed per wave.
-    // (Path ids are 32-bit: waves of 2^29 groups or more keep the octet form.)
+    // (Waves of kMaxRefillGroups groups or more keep the octet form.)
     out.group_em = nullptr;
-    if (fused_ && !packet_ && groups < (1u << 29) && path_refill_wave(refill_mode_, deep_groups, groups)) {
+    if (fused_ && !packet_ && groups < kMaxRefillGroups && path_refill_wave(refill_mode_, deep_groups, groups)) {
         if (groups > group_em_cap_) {
             uint64_t twice = 2ull * group_em_cap_;
-            uint32_t cap = (uint64_t)groups > twice ? groups : (uint32_t)(twice < (1ull << 29) ? twice : (1ull << 29));
+            uint32_t cap = (uint64_t)groups > twice ? groups : (uint32_t)(twice < kMaxRefillGroups ? twice : kMaxRefillGroups);
             if (d_group_em_) {
                 cudaFree(d_group_em_);
                 owned_.erase(std::remove(owned_.begin(), owned_.end(), (void*)d_group_em_), owned_.end());
@@ -330,7 +334,8 @@ extern "C" int32_t cvx_batch_render(cvx_batch* b, const cvx_view* views, uint32_
     uint32_t max_spp = 0;
     for (uint32_t i = 0; i < n; i++) {
         const cvx_view& v = views[i];
-        if (v.scene >= b->scenes.size() || v.width == 0 || v.height == 0 || v.spp == 0)
+        if (v.scene >= b->scenes.size() || v.width == 0 || v.height == 0 || v.spp == 0 ||
+            v.width > kMaxImageSide || v.height > kMaxImageSide)
             return set_error(CVX_ERR_INVALID, "bad view");
         if (b->mode[v.scene] == 1 && groups_of(v.width, v.height) > b->engine.max_groups())
             return set_error(CVX_ERR_CAPACITY, "a view is larger than the ray-queue capacity");
@@ -786,7 +791,8 @@ extern "C" int32_t cvx_server_create(cvx_scene* const* scenes, uint32_t n_scenes
 
 extern "C" int32_t cvx_server_submit(cvx_server* s, const cvx_request* req, uint32_t* rgba, uint64_t* id) {
     if (!s || !req || !id) return set_error(CVX_ERR_INVALID, "null argument");
-    if (req->scene >= s->scenes.size() || req->width == 0 || req->height == 0 || req->spp == 0)
+    if (req->scene >= s->scenes.size() || req->width == 0 || req->height == 0 || req->spp == 0 ||
+        req->width > kMaxImageSide || req->height > kMaxImageSide)
         return set_error(CVX_ERR_INVALID, "bad request");
     auto q = std::make_shared<Request>();
     q->r = *req;

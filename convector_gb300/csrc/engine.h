@@ -14,9 +14,17 @@ DeviceScene scene_view(const cvx_scene* s);
 cudaStream_t scene_stream(const cvx_scene* s);
 uint32_t scene_depth(const cvx_scene* s);
 uint32_t scene_num_lights(const cvx_scene* s);
+// Largest image width and height of a renderer, batch view or server request
+// (an image of 16384 x 16384 is 2^25 groups, so group and path indices of
+// one image stay far inside 32 bits).
+constexpr uint32_t kMaxImageSide = CVX_MAX_IMAGE_SIDE;
+// Waves with per-lane path refill hold fewer groups than this: path ids and
+// the path counter are 32-bit, and the counter runs past the last path by at
+// most one claim per lane of the grid.
+constexpr uint32_t kMaxRefillGroups = 1u << 28;
 uint32_t groups_of(uint32_t w, uint32_t h);
-// First bounce traversed with ray refill for a CVX_REFILL_* mode.
-// First bounce of a wavefront wave whose traversal refills rays.
+// First bounce of a wavefront wave whose traversal refills rays, for a
+// CVX_REFILL_* mode.
 inline uint32_t refill_from(uint32_t refill_mode) { return refill_mode == 1 ? 0u : refill_mode == 2 ? 5u : 1u; }
 
 class WaveEngine {

@@ -151,7 +151,10 @@ enum { CVX_TRAVERSE_PACKET = 0, CVX_TRAVERSE_SINGLE = 1 };
  * `far_dist` (MIntersection::with_max_distance, ray.rs:95-103). Outputs the
  * hit distance and the BVH-order triangle index (-1 for no hit). Host
  * buffers, read in place or copied in (cvx_scene_set_host_access); hits are
- * copied out inside the call. */
+ * copied out inside the call. Both query forms take at most
+ * CVX_MAX_QUERY_RAYS rays per call (CVX_ERR_INVALID beyond: split the rays
+ * over several calls). */
+#define CVX_MAX_QUERY_RAYS 2147483648u
 int32_t cvx_intersect_nearest(cvx_scene* scene, const float* ox, const float* oy, const float* oz,
                               const float* dx, const float* dy, const float* dz, uint32_t n, float far_dist,
                               uint32_t traversal, float* t_out, int32_t* tri_out);
@@ -215,8 +218,11 @@ typedef struct cvx_render_config {
     uint32_t refill_mode;   /* CVX_REFILL_* */
 } cvx_render_config;
 
-/* Renderer::new (renderer.rs:121-130). Any width and height are accepted;
- * sizes off the reference tiling are padded and cropped. */
+/* Renderer::new (renderer.rs:121-130). Widths and heights from 1 to
+ * CVX_MAX_IMAGE_SIDE are accepted (CVX_ERR_INVALID beyond; the same bound
+ * holds for batch views and server requests); sizes off the reference tiling
+ * are padded and cropped. */
+#define CVX_MAX_IMAGE_SIDE 16384u
 int32_t cvx_renderer_create(cvx_scene* scene, uint32_t width, uint32_t height, const cvx_render_config* config,
                             cvx_renderer** out);
 void cvx_renderer_destroy(cvx_renderer* r);

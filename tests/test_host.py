@@ -153,6 +153,25 @@ def test_bvh_needs_a_root_split(cvx):
         cvx.Bvh.from_meshes([m])
 
 
+def test_query_ray_limit_is_checked_first(cvx):
+    # Counts above 2^31 would let the 32-bit ray counters of the query kernels
+    # wrap; both query forms refuse them before touching the scene or a buffer.
+    L = cvx.lib()
+    n = 2**31 + 1
+    st = L.cvx_intersect_nearest(None, None, None, None, None, None, None, n, 1e5, 1, None, None)
+    assert st == 1
+    with pytest.raises(cvx.CvxError, match="2\\^31"):
+        cvx._check(st)
+    st = L.cvx_intersect_nearest_device(None, None, n, 1e5, 1, None, None, None, None)
+    assert st == 1
+    with pytest.raises(cvx.CvxError, match="2\\^31"):
+        cvx._check(st)
+    # At the limit the next check (the null scene) answers instead.
+    st = L.cvx_intersect_nearest(None, None, None, None, None, None, None, 2**31, 1e5, 1, None, None)
+    with pytest.raises(cvx.CvxError, match="null"):
+        cvx._check(st)
+
+
 def test_icosphere_counts():
     from convector_gb300 import scenes
     v, f = scenes.icosphere(6)
