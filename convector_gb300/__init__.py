@@ -169,6 +169,35 @@ def _ptr(a):
     return None if a is None else ctypes.c_void_p(a.ctypes.data)
 
 
+def _host_rays(origins, directions):
+    """(n, 3) float32 origin and direction arrays, each as six contiguous columns."""
+    o = np.ascontiguousarray(origins, dtype=np.float32)
+    d = np.ascontiguousarray(directions, dtype=np.float32)
+    if o.ndim != 2 or o.shape[1] != 3 or d.shape != o.shape:
+        raise ValueError("origins and directions must be (n, 3) arrays of the same n, got %s and %s"
+                         % (o.shape, d.shape))
+    return o.shape[0], [np.ascontiguousarray(o[:, k]) for k in range(3)] + \
+        [np.ascontiguousarray(d[:, k]) for k in range(3)]
+
+
+def _frame_buffer(a, height, width, name):
+    """A caller's output image, written in place: it must be (height, width) C-contiguous uint32."""
+    if not isinstance(a, np.ndarray) or a.dtype != np.uint32 or a.shape != (height, width) or \
+            not a.flags.c_contiguous or not a.flags.writeable:
+        raise ValueError("%s must be a writeable C-contiguous (%d, %d) uint32 array" % (name, height, width))
+    return a
+
+
+def _device_tensor(x, name, count, floating):
+    """A CUDA tensor the device query reads or writes: contiguous, 4-byte
+    elements of the expected kind, and at least `count` of them."""
+    if not getattr(x, "is_cuda", False) or not x.is_contiguous() or x.element_size() != 4 or \
+            x.dtype.is_floating_point != floating or x.numel() < count:
+        raise ValueError("%s must be a contiguous CUDA tensor of at least %d 4-byte %s elements"
+                         % (name, count, "float" if floating else "integer"))
+    return ctypes.c_void_p(x.data_ptr())
+
+
 class SMaterial:
     """The reference's 32-bit material (material.rs:10-31, 84-136)."""
 
@@ -375,10 +404,7 @@ class Scene:
 
     def intersect_nearest(self, origins, directions, far=1.0e5, traversal=TRAVERSE_PACKET):
         """Bvh::intersect_nearest over rays (n x 3 arrays); returns (t, triangle index in BVH order)."""
-        o = np.ascontiguousarray(origins, dtype=np.float32)
-        d = np.ascontiguousarray(directions, dtype=np.float32)
-        n = o.shape[0]
-        cols = [np.ascontiguousarray(o[:, k]) for k in range(3)] + [np.ascontiguousarray(d[:, k]) for k in range(3)]
+        n, cols = _host_rays(origins, directions)
         t = np.empty(n, dtype=np.float32)
         tri = np.empty(n, dtype=np.int32)
         _check(lib().cvx_intersect_nearest(self._h, *[_ptr(c) for c in cols], n, far, traversal, _ptr(t), _ptr(tri)))
@@ -387,10 +413,7 @@ class Scene:
     def intersect_nearest_noalloc(self, origins, directions, far=1.0e5, traversal=TRAVERSE_PACKET):
         """intersect_nearest without any device allocation: stages through the
         library's static 16 MiB device buffer (at most 524,288 rays per call)."""
-        o = np.ascontiguousarray(origins, dtype=np.float32)
-        d = np.ascontiguousarray(directions, dtype=np.float32)
-        n = o.shape[0]
-        cols = [np.ascontiguousarray(o[:, k]) for k in range(3)] + [np.ascontiguousarray(d[:, k]) for k in range(3)]
+        n, cols = _host_rays(origins, directions)
         t = np.empty(n, dtype=np.float32)
         tri = np.empty(n, dtype=np.int32)
         _check(lib().cvx_intersect_nearest_noalloc(self._h, *[_ptr(c) for c in cols], n, far, traversal, _ptr(t),
@@ -399,12 +422,18 @@ class Scene:
 
     def intersect_nearest_device(self, rays_soa, t_out, tri_out, far=1.0e5, traversal=TRAVERSE_PACKET,
                                  counters=None, stream=None):
-        """Device form over torch CUDA tensors: rays_soa is a (6, n) float32 tensor."""
+        """Device form over torch CUDA tensors: rays_soa is a (6, n) float32
+        tensor, t_out n float32, tri_out n int32 and counters (optional) 2n
+        32-bit integers."""
+        if len(rays_soa.shape) != 2 or rays_soa.shape[0] != 6:
+            raise ValueError("rays_soa must be a (6, n) tensor, got %s" % (tuple(rays_soa.shape),))
         n = rays_soa.shape[1]
-        _check(lib().cvx_intersect_nearest_device(
-            self._h, ctypes.c_void_p(rays_soa.data_ptr()), n, far, traversal, ctypes.c_void_p(t_out.data_ptr()),
-            ctypes.c_void_p(tri_out.data_ptr()), None if counters is None else ctypes.c_void_p(counters.data_ptr()),
-            None if stream is None else ctypes.c_void_p(stream)))
+        rays = _device_tensor(rays_soa, "rays_soa", 6 * n, True)
+        t = _device_tensor(t_out, "t_out", n, True)
+        tri = _device_tensor(tri_out, "tri_out", n, False)
+        cnt = None if counters is None else _device_tensor(counters, "counters", 2 * n, False)
+        _check(lib().cvx_intersect_nearest_device(self._h, rays, n, far, traversal, t, tri, cnt,
+                                                  None if stream is None else ctypes.c_void_p(stream)))
 
     def __del__(self):
         if getattr(self, "_h", None) and self._h.value and _LIB is not None:
@@ -452,8 +481,10 @@ class Renderer:
         `origins`, into full-frame uint32 buffers (created when None; pixels
         outside the patches are left as they are). Returns (rgba, gbuffer)."""
         xy = np.ascontiguousarray(np.asarray(origins, dtype=np.uint32).reshape(-1, 2))
-        rgba = np.zeros((self.height, self.width), np.uint32) if rgba is None else rgba
-        gbuffer = np.zeros((self.height, self.width), np.uint32) if gbuffer is None else gbuffer
+        rgba = np.zeros((self.height, self.width), np.uint32) if rgba is None else \
+            _frame_buffer(rgba, self.height, self.width, "rgba")
+        gbuffer = np.zeros((self.height, self.width), np.uint32) if gbuffer is None else \
+            _frame_buffer(gbuffer, self.height, self.width, "gbuffer")
         _check(lib().cvx_render_patches_u8(self._h, patch_width, _ptr(xy), xy.shape[0], frame_number, _ptr(rgba),
                                            _ptr(gbuffer)))
         return rgba, gbuffer
@@ -461,6 +492,8 @@ class Renderer:
     def accumulate_patches_f32(self, patch_width, origins, frame_number, gbuffer=None):
         """Renderer::accumulate_patch_f32 (renderer.rs:339-362) for every (x, y) in `origins`."""
         xy = np.ascontiguousarray(np.asarray(origins, dtype=np.uint32).reshape(-1, 2))
+        if gbuffer is not None:
+            _frame_buffer(gbuffer, self.height, self.width, "gbuffer")
         _check(lib().cvx_accumulate_patches_f32(self._h, patch_width, _ptr(xy), xy.shape[0], frame_number,
                                                 _ptr(gbuffer)))
         return gbuffer
@@ -519,6 +552,8 @@ class Display:
         out = np.empty((self.height, self.width), dtype=np.uint32)
         a = np.ascontiguousarray(rgba, dtype=np.uint32)
         g = np.ascontiguousarray(gbuffer, dtype=np.uint32)
+        if a.size != self.width * self.height or g.size != self.width * self.height:
+            raise ValueError("rgba and gbuffer must hold %d x %d words" % (self.height, self.width))
         _check(lib().cvx_display_frame(self._h, _ptr(a), _ptr(g), int(self.enable_blend), int(self.enable_median),
                                        _ptr(out)))
         return out

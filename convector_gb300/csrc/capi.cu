@@ -579,7 +579,9 @@ int32_t cvx_renderer_set_debug_view(cvx_renderer* r, uint32_t enable) {
 static int32_t run_patches(cvx_renderer* r, uint32_t pw, const uint32_t* xy, uint32_t n, uint32_t frame,
                            bool accumulate, uint32_t* rgba, uint32_t* gbuf) {
     if (!r) return set_error(CVX_ERR_INVALID, "null renderer");
-    if (pw == 0 || (pw & 15u)) return set_error(CVX_ERR_INVALID, "patch width must be a positive multiple of 16");
+    if (pw == 0 || (pw & 15u) || pw > kMaxImageSide)
+        return set_error(CVX_ERR_INVALID, "patch width must be a positive multiple of 16, at most " +
+                                              std::to_string(kMaxImageSide));
     if (n && !xy) return set_error(CVX_ERR_INVALID, "null patch list");
     for (uint32_t i = 0; i < n; i++) {
         uint32_t x = xy[2 * i], y = xy[2 * i + 1];

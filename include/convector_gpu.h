@@ -247,7 +247,8 @@ int32_t cvx_render_frame_u8(cvx_renderer* r, uint32_t frame_number, uint32_t* rg
 int32_t cvx_accumulate_frame_f32(cvx_renderer* r, uint32_t frame_number, uint32_t* gbuffer);
 /* Renderer::render_patch_u8 (renderer.rs:306-327) for a list of patches in
  * one call: origins holds n_patches (x, y) pairs, each patch patch_width
- * pixels square (a multiple of 16) with its own generator seeded (x, y,
+ * pixels square (a multiple of 16, at most CVX_MAX_IMAGE_SIDE; pixels of a
+ * patch beyond the frame are not stored) with its own generator seeded (x, y,
  * frame_number), as in the reference whatever the renderer's rng_order.
  * x must be a multiple of 16 and y of 4, inside the frame. Only the patches'
  * pixels of the full-frame rgba / gbuffer buffers (either may be NULL) are

@@ -172,6 +172,28 @@ def test_query_ray_limit_is_checked_first(cvx):
         cvx._check(st)
 
 
+def test_wrapper_buffer_checks(cvx):
+    # The Python mirror refuses buffers the library would read or write past
+    # their end, before any call into it.
+    o = np.zeros((10, 3), np.float32)
+    n, cols = cvx._host_rays(o, np.ones((10, 3)))
+    assert n == 10 and len(cols) == 6 and all(c.dtype == np.float32 and c.shape == (10,) for c in cols)
+    for bad in (np.ones((9, 3)), np.ones((10, 2)), np.ones(30)):
+        with pytest.raises(ValueError):
+            cvx._host_rays(o, bad)
+    with pytest.raises(ValueError):
+        cvx._host_rays(np.zeros(30), np.zeros(30))
+    good = np.zeros((4, 16), np.uint32)
+    assert cvx._frame_buffer(good, 4, 16, "rgba") is good
+    for bad in (np.zeros((4, 15), np.uint32), np.zeros((4, 16), np.int64), np.zeros((16, 4), np.uint32).T,
+                np.zeros(64, np.uint32)):
+        with pytest.raises(ValueError):
+            cvx._frame_buffer(bad, 4, 16, "rgba")
+    torch = pytest.importorskip("torch")
+    with pytest.raises(ValueError):  # a host tensor
+        cvx._device_tensor(torch.zeros(8), "t_out", 8, True)
+
+
 def test_icosphere_counts():
     from convector_gb300 import scenes
     v, f = scenes.icosphere(6)
