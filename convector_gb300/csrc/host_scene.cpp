@@ -804,6 +804,9 @@ int32_t bvh_from_interim(const std::vector<InterimNode>& t, const std::vector<ui
 
 static int32_t build(const cvx_triangle* tris, uint32_t n, cvx_bvh** out) {
     if (n == 0) return set_error(CVX_ERR_INVALID, "cannot build a BVH of zero triangles");
+    // Node and triangle indices are 32-bit, and a scene holds fewer than 2^27
+    // triangles (cvx_scene_create).
+    if (n >= (1u << 27)) return set_error(CVX_ERR_INVALID, "a BVH holds fewer than 2^27 triangles");
     std::vector<cvx_triangle> src(tris, tris + n);
     std::vector<TriRef> refs(n);
     const float third = 1.0f / 3.0f;  // 3.0f32.recip()

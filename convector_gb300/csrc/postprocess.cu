@@ -220,6 +220,10 @@ int32_t cvx_display_create(uint32_t width, uint32_t height, const uint8_t* tex1_
                            uint32_t tex_w, uint32_t tex_h, cvx_display** out) {
     if (!out || !width || !height || !tex1_rgb || !tex2_rgb || !tex_w || !tex_h)
         return cvx::set_error(CVX_ERR_INVALID, "bad display arguments");
+    // Pixel and texel indices are 32-bit in the kernels.
+    if (width > CVX_MAX_IMAGE_SIDE || height > CVX_MAX_IMAGE_SIDE || tex_w > CVX_MAX_IMAGE_SIDE ||
+        tex_h > CVX_MAX_IMAGE_SIDE)
+        return cvx::set_error(CVX_ERR_INVALID, "display and texture sides are limited to 16384 pixels");
     std::unique_ptr<cvx_display> d(new cvx_display());
     d->w = width;
     d->h = height;

@@ -85,7 +85,8 @@ uint32_t cvx_mesh_num_triangles(const cvx_mesh* mesh);
 void cvx_mesh_destroy(cvx_mesh* mesh);
 
 /* Bvh::from_meshes (bvh.rs:547-568) and Bvh::build (bvh.rs:488-545): the
- * reference's binned tree-SAH build, node order and triangle order. */
+ * reference's binned tree-SAH build, node order and triangle order. Fewer
+ * than 2^27 triangles (CVX_ERR_INVALID beyond). */
 int32_t cvx_bvh_from_meshes(const cvx_mesh* const* meshes, uint32_t n_meshes, cvx_bvh** out);
 int32_t cvx_bvh_build(const cvx_triangle* triangles, uint32_t n, cvx_bvh** out);
 /* Bvh::build (bvh.rs:488-545) run on the device: the same nodes, triangle
@@ -369,7 +370,8 @@ void cvx_server_destroy(cvx_server* s);
  * composite of the material textures into a ring of 8 frames, the mean of the
  * ring (or the newest frame), the 5-tap median in CIE XYZ (or the identity),
  * and the sRGB encode of the window's framebuffer. Textures are RGB8 sRGB,
- * tex_w x tex_h, for texture indices 1 and 2. */
+ * tex_w x tex_h, for texture indices 1 and 2. Every side is at most
+ * CVX_MAX_IMAGE_SIDE. */
 typedef struct cvx_display cvx_display;
 int32_t cvx_display_create(uint32_t width, uint32_t height, const uint8_t* texture1_rgb, const uint8_t* texture2_rgb,
                            uint32_t tex_w, uint32_t tex_h, cvx_display** out);

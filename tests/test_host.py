@@ -172,6 +172,20 @@ def test_query_ray_limit_is_checked_first(cvx):
         cvx._check(st)
 
 
+def test_size_limits_refused_before_work(cvx):
+    # Checked on the host before any triangle is read or any device call is made.
+    L = cvx.lib()
+    tri = np.zeros(16, np.uint32)
+    out = ctypes.c_void_p()
+    with pytest.raises(cvx.CvxError, match="2\\^27"):
+        cvx._check(L.cvx_bvh_build(cvx._ptr(tri), 1 << 27, ctypes.byref(out)))
+    tex = np.zeros(3, np.uint8)
+    for w, h, tw, th in ((16385, 16, 1, 1), (16, 16385, 1, 1), (16, 16, 16385, 1), (16, 16, 1, 16385)):
+        with pytest.raises(cvx.CvxError, match="16384"):
+            cvx._check(L.cvx_display_create(w, h, cvx._ptr(tex), cvx._ptr(tex), tw, th, ctypes.byref(out)))
+    assert not out.value
+
+
 def test_wrapper_buffer_checks(cvx):
     # The Python mirror refuses buffers the library would read or write past
     # their end, before any call into it.
