@@ -21,7 +21,7 @@ LIB = os.path.join(PKG, "lib", "libconvector_gpu.so")
 CU_SOURCES = ["kernels.cu", "wavefront.cu", "engine.cu", "capi.cu", "noalloc.cu", "postprocess.cu", "bvh_build.cu"]
 CPP_SOURCES = ["host_scene.cpp"]
 HEADERS = ["x86sem.cuh", "layout.cuh", "traverse.cuh", "shade.cuh", "path_refill.cuh", "kernels.h", "internal.h",
-           "x86_approx_tables.h", "wavefront.cuh", "engine.h"]
+           "x86_approx_tables.h", "wavefront.cuh", "engine.h", "device_guard.cuh"]
 
 NVCC_FLAGS = [
     "-gencode", "arch=compute_103a,code=sm_103a",

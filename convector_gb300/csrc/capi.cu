@@ -10,6 +10,7 @@
 #include <string>
 #include <vector>
 
+#include "device_guard.cuh"
 #include "engine.h"
 #include "internal.h"
 #include "kernels.h"
@@ -149,10 +150,12 @@ DeviceScene cvx::scene_view(const cvx_scene* s) { return s->view(); }
 cudaStream_t cvx::scene_stream(const cvx_scene* s) { return s->stream; }
 uint32_t cvx::scene_depth(const cvx_scene* s) { return s->depth; }
 uint32_t cvx::scene_num_lights(const cvx_scene* s) { return s->n_lights; }
+int cvx::scene_device(const cvx_scene* s) { return s->device; }
 
 struct cvx_renderer {
     std::unique_ptr<WaveEngine> engine;  // wavefront mode
     cvx_scene* scene = nullptr;
+    int device = 0;  // the scene's
     uint32_t w = 0, h = 0;
     cvx_render_config cfg{};
     DeviceCamera cam{};
@@ -345,7 +348,11 @@ int32_t cvx_scene_set_query_launch(cvx_scene* s, uint32_t blocks_per_sm) {
     return CVX_OK;
 }
 
-void cvx_scene_destroy(cvx_scene* s) { delete s; }
+void cvx_scene_destroy(cvx_scene* s) {
+    if (!s) return;
+    DeviceGuard g(s->device);
+    delete s;
+}
 
 int32_t cvx_intersect_nearest_device(cvx_scene* s, const float* rays, uint32_t n, float far_dist, uint32_t traversal,
                                      float* t_out, int32_t* tri_out, uint32_t* counters, void* stream) {
@@ -353,6 +360,7 @@ int32_t cvx_intersect_nearest_device(cvx_scene* s, const float* rays, uint32_t n
     if (!s || (!rays && n) || (!t_out && n) || (!tri_out && n)) return set_error(CVX_ERR_INVALID, "null argument");
     if (traversal > 1) return set_error(CVX_ERR_INVALID, "unknown traversal variant");
     if (n == 0) return CVX_OK;
+    CVX_ON_DEVICE(s->device);
     cudaStream_t st = (cudaStream_t)stream;
     CK(launch_intersect(s->view(), soa_cols(rays, n), n, far_dist, traversal == CVX_TRAVERSE_PACKET, t_out, tri_out,
                         counters, s->d_err, 0, s->blocks_per_sm, st),
@@ -368,6 +376,7 @@ int32_t cvx_intersect_nearest(cvx_scene* s, const float* ox, const float* oy, co
     if (n == 0) return CVX_OK;
     if (!ox || !oy || !oz || !dx || !dy || !dz || !t_out || !tri_out) return set_error(CVX_ERR_INVALID, "null buffer");
     if (traversal > 1) return set_error(CVX_ERR_INVALID, "unknown traversal variant");
+    CVX_ON_DEVICE(s->device);
     int32_t st = 0;
     // In place: the kernel reads the caller's six arrays over the CPU-GPU
     // link as it consumes them (a warp stages each batch of 32 rays one batch
@@ -442,6 +451,7 @@ int32_t cvx_intersect_nearest(cvx_scene* s, const float* ox, const float* oy, co
 int32_t cvx_renderer_create(cvx_scene* scene, uint32_t w, uint32_t h, const cvx_render_config* cfg,
                             cvx_renderer** out) {
     if (!scene || !out) return set_error(CVX_ERR_INVALID, "null argument");
+    CVX_ON_DEVICE(scene->device);
     if (w == 0 || h == 0 || w > kMaxImageSide || h > kMaxImageSide)
         return set_error(CVX_ERR_INVALID, "frame size out of range");
     if (scene->n_lights == 0)
@@ -457,6 +467,7 @@ int32_t cvx_renderer_create(cvx_scene* scene, uint32_t w, uint32_t h, const cvx_
                          "per patch)");
     std::unique_ptr<cvx_renderer> r(new cvx_renderer());
     r->scene = scene;
+    r->device = scene->device;
     r->w = w;
     r->h = h;
     r->cfg = c;
@@ -489,7 +500,11 @@ int32_t cvx_renderer_create(cvx_scene* scene, uint32_t w, uint32_t h, const cvx_
     return CVX_OK;
 }
 
-void cvx_renderer_destroy(cvx_renderer* r) { delete r; }
+void cvx_renderer_destroy(cvx_renderer* r) {
+    if (!r) return;
+    DeviceGuard g(r->device);
+    delete r;
+}
 
 int32_t cvx_renderer_set_time(cvx_renderer* r, float time, float time_delta) {
     if (!r) return set_error(CVX_ERR_INVALID, "null renderer");
@@ -579,6 +594,7 @@ int32_t cvx_renderer_set_debug_view(cvx_renderer* r, uint32_t enable) {
 static int32_t run_patches(cvx_renderer* r, uint32_t pw, const uint32_t* xy, uint32_t n, uint32_t frame,
                            bool accumulate, uint32_t* rgba, uint32_t* gbuf) {
     if (!r) return set_error(CVX_ERR_INVALID, "null renderer");
+    CVX_ON_DEVICE(r->device);
     if (pw == 0 || (pw & 15u) || pw > kMaxImageSide)
         return set_error(CVX_ERR_INVALID, "patch width must be a positive multiple of 16, at most " +
                                               std::to_string(kMaxImageSide));
@@ -644,17 +660,20 @@ int32_t cvx_accumulate_patches_f32(cvx_renderer* r, uint32_t patch_width, const 
 
 int32_t cvx_render_frame_u8(cvx_renderer* r, uint32_t frame, uint32_t* rgba, uint32_t* gbuffer) {
     if (!r) return set_error(CVX_ERR_INVALID, "null renderer");
+    CVX_ON_DEVICE(r->device);
     return run_frame(r, frame, false, rgba, gbuffer);
 }
 
 int32_t cvx_accumulate_frame_f32(cvx_renderer* r, uint32_t frame, uint32_t* gbuffer) {
     if (!r) return set_error(CVX_ERR_INVALID, "null renderer");
+    CVX_ON_DEVICE(r->device);
     return run_frame(r, frame, true, nullptr, gbuffer);
 }
 
 int32_t cvx_resolve_u8(cvx_renderer* r, uint32_t n, uint32_t* rgba) {
     if (!r || !rgba) return set_error(CVX_ERR_INVALID, "null argument");
     if (n == 0) return set_error(CVX_ERR_INVALID, "number of samples must be positive");
+    CVX_ON_DEVICE(r->device);
     size_t npx = (size_t)r->w * r->h;
     CK(launch_resolve(r->d_accum, (uint32_t)npx, 1.0f / (float)n, r->d_rgba, r->stream), "resolve launch");
     CK(cudaMemcpyAsync(rgba, r->d_rgba, npx * 4, cudaMemcpyDeviceToHost, r->stream), "copy colour");
@@ -664,12 +683,14 @@ int32_t cvx_resolve_u8(cvx_renderer* r, uint32_t n, uint32_t* rgba) {
 
 int32_t cvx_read_accumulator(cvx_renderer* r, float* out) {
     if (!r || !out) return set_error(CVX_ERR_INVALID, "null argument");
+    CVX_ON_DEVICE(r->device);
     CK(cudaMemcpy(out, r->d_accum, (size_t)r->w * r->h * 12, cudaMemcpyDeviceToHost), "copy accumulator");
     return CVX_OK;
 }
 
 int32_t cvx_clear_accumulator(cvx_renderer* r) {
     if (!r) return set_error(CVX_ERR_INVALID, "null renderer");
+    CVX_ON_DEVICE(r->device);
     CK(cudaMemsetAsync(r->d_accum, 0, (size_t)r->w * r->h * 12, r->stream), "clear accumulator");
     CK(cudaStreamSynchronize(r->stream), "clear accumulator");
     return CVX_OK;
@@ -677,6 +698,7 @@ int32_t cvx_clear_accumulator(cvx_renderer* r) {
 
 int32_t cvx_read_frame_f32(cvx_renderer* r, float* out) {
     if (!r || !out) return set_error(CVX_ERR_INVALID, "null argument");
+    CVX_ON_DEVICE(r->device);
     CK(cudaMemcpy(out, r->d_color, (size_t)r->w * r->h * 12, cudaMemcpyDeviceToHost), "copy frame");
     return CVX_OK;
 }

@@ -1,0 +1,62 @@
+// Every handle of the library belongs to the device that was current when it
+// was created. A call on a handle runs on that device whatever device is
+// current in the calling thread: the guard selects it for the call and gives
+// the thread its previous device back afterwards (on a one-device system, and
+// whenever the devices agree, it does nothing).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <string>
+
+#include "internal.h"
+
+namespace cvx {
+
+class DeviceGuard {
+   public:
+    explicit DeviceGuard(int dev) : dev_(dev) {
+        if (cudaGetDevice(&prev_) != cudaSuccess) {
+            cudaGetLastError();
+            return;
+        }
+        if (prev_ == dev) {
+            ok_ = true;
+        } else if (cudaSetDevice(dev) == cudaSuccess) {
+            ok_ = restore_ = true;
+        } else {
+            cudaGetLastError();
+        }
+    }
+    ~DeviceGuard() {
+        if (restore_) cudaSetDevice(prev_);
+    }
+    DeviceGuard(const DeviceGuard&) = delete;
+    DeviceGuard& operator=(const DeviceGuard&) = delete;
+    // The handle's device is current; otherwise the error status to return.
+    bool ok() const { return ok_; }
+    int32_t fail() const {
+        return set_error(CVX_ERR_CUDA, "cannot select device " + std::to_string(dev_) + " of the handle");
+    }
+
+   private:
+    int dev_ = 0, prev_ = 0;
+    bool ok_ = false, restore_ = false;
+};
+
+// The device current in the calling thread (-1 when none can be had).
+inline int current_device() {
+    int d = -1;
+    if (cudaGetDevice(&d) != cudaSuccess) {
+        cudaGetLastError();
+        return -1;
+    }
+    return d;
+}
+
+}  // namespace cvx
+
+// Selects handle device `dev` for the rest of the enclosing entry point, or
+// returns the error status from it.
+#define CVX_ON_DEVICE(dev)                              \
+    ::cvx::DeviceGuard cvx_device_guard_(dev);          \
+    if (!cvx_device_guard_.ok()) return cvx_device_guard_.fail()

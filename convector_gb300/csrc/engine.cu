@@ -17,6 +17,7 @@
 #include <unordered_map>
 #include <vector>
 
+#include "device_guard.cuh"
 #include "engine.h"
 #include "internal.h"
 #include "kernels.h"
@@ -270,7 +271,17 @@ static uint32_t default_scene_mode(const cvx_scene* s) {
     return (scene_depth(s) > 40 || v.n_tris > 200000) ? 1u : 0u;
 }
 
+// The device of a batch's or server's scenes, which must all be on one.
+static int32_t common_device(cvx_scene* const* scenes, uint32_t n, int* dev) {
+    *dev = scene_device(scenes[0]);
+    for (uint32_t i = 1; i < n; i++)
+        if (scene_device(scenes[i]) != *dev)
+            return set_error(CVX_ERR_INVALID, "the scenes of a batch or server must be on one device");
+    return CVX_OK;
+}
+
 struct cvx_batch {
+    int device = 0;  // its scenes'
     std::vector<cvx_scene*> scenes;
     std::vector<uint32_t> mode;  // per scene: 0 fused, 1 wavefront
     WaveEngine engine;           // wavefront
@@ -300,12 +311,17 @@ extern "C" int32_t cvx_batch_create(cvx_scene* const* scenes, uint32_t n_scenes,
     for (uint32_t i = 0; i < n_scenes; i++)
         if (!scenes[i] || scene_num_lights(scenes[i]) == 0)
             return set_error(CVX_ERR_INVALID, "every batch scene needs a direct-sample triangle");
+    int dev = 0;
+    int32_t st = common_device(scenes, n_scenes, &dev);
+    if (st) return st;
+    CVX_ON_DEVICE(dev);
     std::unique_ptr<cvx_batch> b(new cvx_batch());
+    b->device = dev;
     b->scenes.assign(scenes, scenes + n_scenes);
     b->max_pixels = max_pixels;
     ECK(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking), "cudaStreamCreate");
     ECK(cudaStreamCreateWithFlags(&b->stream2, cudaStreamNonBlocking), "cudaStreamCreate");
-    int32_t st = b->engine.init(max_groups, 4096, c.traversal == CVX_TRAVERSE_PACKET, c.use_graph != 0,
+    st = b->engine.init(max_groups, 4096, c.traversal == CVX_TRAVERSE_PACKET, c.use_graph != 0,
                                 c.blocks_per_sm, c.refill_mode);
     if (st) return st;
     if ((st = b->fused.init(0xffffffffu, 4096, c.traversal == CVX_TRAVERSE_PACKET, c.use_graph != 0, 0,
@@ -328,6 +344,7 @@ extern "C" int32_t cvx_batch_create(cvx_scene* const* scenes, uint32_t n_scenes,
 extern "C" int32_t cvx_batch_render(cvx_batch* b, const cvx_view* views, uint32_t n, uint32_t* const* rgba,
                                     uint64_t* rays_out, float* ms_out) {
     if (!b || (!views && n)) return set_error(CVX_ERR_INVALID, "null argument");
+    CVX_ON_DEVICE(b->device);
     if (n > b->max_items) return set_error(CVX_ERR_CAPACITY, "too many views in one batch call");
     std::vector<uint64_t> offset(n);
     uint64_t total = 0;
@@ -418,7 +435,11 @@ extern "C" int32_t cvx_batch_set_scene_mode(cvx_batch* b, uint32_t scene, uint32
     return CVX_OK;
 }
 
-extern "C" void cvx_batch_destroy(cvx_batch* b) { delete b; }
+extern "C" void cvx_batch_destroy(cvx_batch* b) {
+    if (!b) return;
+    DeviceGuard g(b->device);
+    delete b;
+}
 
 // ---------------------------------------------------------------------------
 // Request server
@@ -476,6 +497,7 @@ struct RangeAlloc {
 }  // namespace
 
 struct cvx_server {
+    int device = 0;  // its scenes'; the worker thread selects it
     std::vector<cvx_scene*> scenes;
     std::vector<uint32_t> mode;  // per scene: 0 fused, 1 wavefront
     cvx_server_config cfg{};
@@ -652,6 +674,9 @@ struct cvx_server {
             std::vector<std::shared_ptr<Request>> reqs;
             cudaEvent_t done = nullptr;
         } fl[kMaxEngines];
+        // The thread starts on device 0: take the server's device. (If that
+        // fails, every wave fails and its requests end with the error.)
+        cudaSetDevice(device);
         for (auto& f : fl) cudaEventCreateWithFlags(&f.done, cudaEventDisableTiming);
         int n_busy = 0;
         double busy_from = 0.0;
@@ -746,7 +771,12 @@ extern "C" int32_t cvx_server_create(cvx_scene* const* scenes, uint32_t n_scenes
     for (uint32_t i = 0; i < n_scenes; i++)
         if (!scenes[i] || scene_num_lights(scenes[i]) == 0)
             return set_error(CVX_ERR_INVALID, "every served scene needs a direct-sample triangle");
+    int dev = 0;
+    int32_t st = common_device(scenes, n_scenes, &dev);
+    if (st) return st;
+    CVX_ON_DEVICE(dev);
     std::unique_ptr<cvx_server> s(new cvx_server());
+    s->device = dev;
     s->scenes.assign(scenes, scenes + n_scenes);
     s->cfg = *cfg;
     // The wavefront waves (deep scenes) are the longer part of a wave: their
@@ -757,7 +787,7 @@ extern "C" int32_t cvx_server_create(cvx_scene* const* scenes, uint32_t n_scenes
     ECK(cudaStreamCreateWithPriority(&s->stream, cudaStreamNonBlocking, greatest), "cudaStreamCreate");
     ECK(cudaStreamCreateWithPriority(&s->stream2, cudaStreamNonBlocking, least), "cudaStreamCreate");
     const bool deep_fused = cfg->deep_single_launch != 0;
-    int32_t st = s->engine.init(cfg->max_groups, 1024, cfg->traversal == CVX_TRAVERSE_PACKET, cfg->use_graph != 0,
+    st = s->engine.init(cfg->max_groups, 1024, cfg->traversal == CVX_TRAVERSE_PACKET, cfg->use_graph != 0,
                                 cfg->blocks_per_sm, cfg->refill_mode, deep_fused);
     if (st) return st;
     if ((st = s->fused.init(0xffffffffu, 1024, cfg->traversal == CVX_TRAVERSE_PACKET, cfg->use_graph != 0,
@@ -874,4 +904,8 @@ extern "C" int32_t cvx_server_set_scene_mode(cvx_server* s, uint32_t scene, uint
     return CVX_OK;
 }
 
-extern "C" void cvx_server_destroy(cvx_server* s) { delete s; }
+extern "C" void cvx_server_destroy(cvx_server* s) {
+    if (!s) return;
+    DeviceGuard g(s->device);
+    delete s;
+}

@@ -14,6 +14,7 @@ DeviceScene scene_view(const cvx_scene* s);
 cudaStream_t scene_stream(const cvx_scene* s);
 uint32_t scene_depth(const cvx_scene* s);
 uint32_t scene_num_lights(const cvx_scene* s);
+int scene_device(const cvx_scene* s);  // the device the scene was created on
 // Largest image width and height of a renderer, batch view or server request
 // (an image of 16384 x 16384 is 2^25 groups, so group and path indices of
 // one image stay far inside 32 bits).

@@ -8,6 +8,7 @@
 #include <string>
 #include <vector>
 
+#include "device_guard.cuh"
 #include "engine.h"
 #include "internal.h"
 #include "kernels.h"
@@ -65,6 +66,7 @@ extern "C" int32_t cvx_intersect_nearest_noalloc(cvx_scene* scene, const float* 
     if (!ox || !oy || !oz || !dx || !dy || !dz || !t_out || !tri_out)
         return cvx::set_error(CVX_ERR_INVALID, "null buffer");
     if (traversal > 1) return cvx::set_error(CVX_ERR_INVALID, "unknown traversal variant");
+    CVX_ON_DEVICE(cvx::scene_device(scene));
     if (n > kNoAllocMaxRays)
         return cvx::set_error(CVX_ERR_INVALID, "cvx_intersect_nearest_noalloc takes at most " +
                                                    std::to_string(kNoAllocMaxRays) + " rays per call, got " +

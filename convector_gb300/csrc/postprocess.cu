@@ -19,6 +19,7 @@
 #include <string>
 #include <vector>
 
+#include "device_guard.cuh"
 #include "internal.h"
 
 namespace {
@@ -172,6 +173,7 @@ __global__ void k_post_median(const uint32_t* __restrict__ in, uint32_t w, uint3
 }  // namespace
 
 struct cvx_display {
+    int device = 0;  // current at creation
     uint32_t w = 0, h = 0, slot = 0;
     uint32_t *d_frame = nullptr, *d_gbuf = nullptr, *d_ring = nullptr, *d_scratch = nullptr, *d_out = nullptr;
     uint8_t *d_tex1 = nullptr, *d_tex2 = nullptr;
@@ -225,6 +227,8 @@ int32_t cvx_display_create(uint32_t width, uint32_t height, const uint8_t* tex1_
         tex_h > CVX_MAX_IMAGE_SIDE)
         return cvx::set_error(CVX_ERR_INVALID, "display and texture sides are limited to 16384 pixels");
     std::unique_ptr<cvx_display> d(new cvx_display());
+    d->device = cvx::current_device();
+    if (d->device < 0) return cvx::set_error(CVX_ERR_CUDA, "no CUDA device available");
     d->w = width;
     d->h = height;
     d->tw = tex_w;
@@ -252,6 +256,7 @@ int32_t cvx_display_create(uint32_t width, uint32_t height, const uint8_t* tex1_
 int32_t cvx_display_frame(cvx_display* d, const uint32_t* rgba, const uint32_t* gbuffer, uint32_t enable_blend,
                           uint32_t enable_median, uint32_t* out_srgb) {
     if (!d || !rgba || !gbuffer || !out_srgb) return cvx::set_error(CVX_ERR_INVALID, "null argument");
+    CVX_ON_DEVICE(d->device);
     uint32_t npx = d->w * d->h;
     PCK(cudaMemcpyAsync(d->d_frame, rgba, (size_t)npx * 4, cudaMemcpyHostToDevice, d->stream), "upload frame");
     PCK(cudaMemcpyAsync(d->d_gbuf, gbuffer, (size_t)npx * 4, cudaMemcpyHostToDevice, d->stream), "upload gbuffer");
@@ -270,6 +275,10 @@ int32_t cvx_display_frame(cvx_display* d, const uint32_t* rgba, const uint32_t* 
     return CVX_OK;
 }
 
-void cvx_display_destroy(cvx_display* d) { delete d; }
+void cvx_display_destroy(cvx_display* d) {
+    if (!d) return;
+    cvx::DeviceGuard g(d->device);
+    delete d;
+}
 
 }  // extern "C"

@@ -12,6 +12,13 @@
  * time; distinct handles may be used concurrently. Calls that take host
  * buffers are synchronous. Nothing here falls back to the CPU: without a
  * usable CUDA device the GPU entry points return CVX_ERR_CUDA.
+ *
+ * Devices: a scene or display belongs to the device current in the calling
+ * thread when it is created; a renderer, batch or server to its scenes' device
+ * (the scenes of one batch or server must share it). Every call on a handle
+ * runs on the handle's device, whatever device is current in the calling
+ * thread, and leaves the thread's current device as it found it. Device
+ * pointers and streams passed in must belong to that device.
  */
 #ifndef CONVECTOR_GPU_H
 #define CONVECTOR_GPU_H
