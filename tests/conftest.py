@@ -34,5 +34,3 @@ def gpu(cvx):
         pytest.fail("GPU test run without a CUDA device")
     return cvx
 
-
-REFERENCE_MODELS = "/root/reference/models"
