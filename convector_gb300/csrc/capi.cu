@@ -410,6 +410,7 @@ int32_t cvx_intersect_nearest(cvx_scene* s, const float* ox, const float* oy, co
     }
     for (cudaStream_t& q : s->qstreams)
         if (!q) CK(cudaStreamCreateWithFlags(&q, cudaStreamNonBlocking), "cudaStreamCreate");
+    StreamSync sync(s->qstreams[0], s->qstreams[1], s->qstreams[2]);
     const float* src[6] = {ox, oy, oz, dx, dy, dz};
     bool locked = page_locked(t_out) && page_locked(tri_out);
     for (int k = 0; k < 6 && locked && !in_place; k++) locked = page_locked(src[k]);
@@ -546,6 +547,7 @@ static int32_t run_frame_wavefront(cvx_renderer* r, uint32_t frame, bool accumul
     out.accum = accumulate ? r->d_accum : nullptr;
     uint64_t rays = 0;
     float ms = 0.0f;
+    StreamSync sync(r->stream);
     int32_t st = r->engine->run(std::vector<Job>{j}, out, r->stream, &rays, nullptr, &ms);
     if (st) return st;
     r->last_rays = rays;
@@ -559,6 +561,9 @@ static int32_t run_frame_wavefront(cvx_renderer* r, uint32_t frame, bool accumul
 static int32_t run_frame(cvx_renderer* r, uint32_t frame, bool accumulate, uint32_t* rgba, uint32_t* gbuf) {
     if (r->engine && !r->debug) return run_frame_wavefront(r, frame, accumulate, rgba, gbuf);
     size_t npx = (size_t)r->w * r->h;
+    unsigned long long rays = 0;
+    uint32_t err = 0;
+    StreamSync sync(r->stream);
     CK(cudaMemsetAsync(r->d_rays, 0, 8, r->stream), "reset counters");
     CK(cudaMemsetAsync(r->d_err, 0, 8, r->stream), "reset status");
     CK(cudaEventRecord(r->e0, r->stream), "event");
@@ -571,8 +576,6 @@ static int32_t run_frame(cvx_renderer* r, uint32_t frame, bool accumulate, uint3
     CK(cudaEventRecord(r->e1, r->stream), "event");
     if (rgba) CK(cudaMemcpyAsync(rgba, r->d_rgba, npx * 4, cudaMemcpyDeviceToHost, r->stream), "copy colour");
     if (gbuf) CK(cudaMemcpyAsync(gbuf, r->d_gbuf, npx * 4, cudaMemcpyDeviceToHost, r->stream), "copy gbuffer");
-    unsigned long long rays = 0;
-    uint32_t err = 0;
     CK(cudaMemcpyAsync(&rays, r->d_rays, 8, cudaMemcpyDeviceToHost, r->stream), "copy counters");
     CK(cudaMemcpyAsync(&err, r->d_err, 4, cudaMemcpyDeviceToHost, r->stream), "copy status");
     CK(cudaStreamSynchronize(r->stream), "render");
@@ -607,6 +610,9 @@ static int32_t run_patches(cvx_renderer* r, uint32_t pw, const uint32_t* xy, uin
     }
     if (n == 0) return CVX_OK;
     int32_t st = 0;
+    unsigned long long rays = 0;
+    uint32_t err = 0;
+    StreamSync sync(r->stream);
     if (n > r->patch_cap) {
         cudaFree(r->d_patches);
         r->d_patches = nullptr;
@@ -637,8 +643,6 @@ static int32_t run_patches(cvx_renderer* r, uint32_t pw, const uint32_t* xy, uin
                                  r->stream),
                "copy gbuffer");
     }
-    unsigned long long rays = 0;
-    uint32_t err = 0;
     CK(cudaMemcpyAsync(&rays, r->d_rays, 8, cudaMemcpyDeviceToHost, r->stream), "copy counters");
     CK(cudaMemcpyAsync(&err, r->d_err, 4, cudaMemcpyDeviceToHost, r->stream), "copy status");
     CK(cudaStreamSynchronize(r->stream), "render");
@@ -675,6 +679,7 @@ int32_t cvx_resolve_u8(cvx_renderer* r, uint32_t n, uint32_t* rgba) {
     if (n == 0) return set_error(CVX_ERR_INVALID, "number of samples must be positive");
     CVX_ON_DEVICE(r->device);
     size_t npx = (size_t)r->w * r->h;
+    StreamSync sync(r->stream);
     CK(launch_resolve(r->d_accum, (uint32_t)npx, 1.0f / (float)n, r->d_rgba, r->stream), "resolve launch");
     CK(cudaMemcpyAsync(rgba, r->d_rgba, npx * 4, cudaMemcpyDeviceToHost, r->stream), "copy colour");
     CK(cudaStreamSynchronize(r->stream), "resolve");

@@ -43,6 +43,25 @@ class DeviceGuard {
     bool ok_ = false, restore_ = false;
 };
 
+// Waits, whichever way the enclosing call returns, for the work it queued on
+// its streams. Copies into the caller's buffers (or into locals of the call)
+// and kernels reading the caller's memory in place must not outlive the call,
+// and an error return halfway through would otherwise leave them in flight.
+// Declare it after the locals that copies write to, so that it runs first.
+class StreamSync {
+   public:
+    StreamSync(cudaStream_t a, cudaStream_t b = nullptr, cudaStream_t c = nullptr) : s_{a, b, c} {}
+    ~StreamSync() {
+        for (cudaStream_t s : s_)
+            if (s) cudaStreamSynchronize(s);
+    }
+    StreamSync(const StreamSync&) = delete;
+    StreamSync& operator=(const StreamSync&) = delete;
+
+   private:
+    cudaStream_t s_[3];
+};
+
 // The device current in the calling thread (-1 when none can be had).
 inline int current_device() {
     int d = -1;

@@ -361,6 +361,7 @@ extern "C" int32_t cvx_batch_render(cvx_batch* b, const cvx_view* views, uint32_
         max_spp = std::max(max_spp, v.spp);
     }
     if (total > b->max_pixels) return set_error(CVX_ERR_CAPACITY, "views exceed the batch framebuffer");
+    StreamSync sync(b->stream, b->stream2);
     ECK(cudaMemsetAsync(b->d_accum, 0, total * 12, b->stream), "clear accumulator");
     uint64_t rays = 0;
     float ms = 0.0f;
@@ -652,7 +653,11 @@ struct cvx_server {
             for (auto& q : done)
                 if (ce == cudaSuccess && q->host_rgba)
                     ce = cudaMemcpyAsync(q->host_rgba, d_rgba + q->offset, q->npx * 4, cudaMemcpyDeviceToHost, rs);
-            if (ce == cudaSuccess) ce = cudaStreamSynchronize(rs);
+            // Wait even after a failed enqueue: copies queued before it still
+            // write into the requests' buffers, which their callers may free
+            // once the requests are finished.
+            cudaError_t se = cudaStreamSynchronize(rs);
+            if (ce == cudaSuccess) ce = se;
             std::lock_guard<std::mutex> lk(mu);
             for (auto& q : done) {
                 finish(q, ce == cudaSuccess ? CVX_OK : CVX_ERR_CUDA);

@@ -79,6 +79,8 @@ extern "C" int32_t cvx_intersect_nearest_noalloc(cvx_scene* scene, const float* 
     float* t_dev = reinterpret_cast<float*>(base + kHeaderBytes + kRayBytes);
     int32_t* tri_dev = reinterpret_cast<int32_t*>(base + kHeaderBytes + kRayBytes + kTBytes);
     cudaStream_t stream = cvx::scene_stream(scene);
+    uint32_t err = 0;
+    cvx::StreamSync sync(stream);
     cudaError_t e;
     // The array keeps the previous call's contents: the status word must start at zero.
     if ((e = cudaMemsetAsync(status, 0, 2 * sizeof(uint32_t), stream)) != cudaSuccess) return fail(e, "clear status");
@@ -96,7 +98,6 @@ extern "C" int32_t cvx_intersect_nearest_noalloc(cvx_scene* scene, const float* 
     if ((e = cudaMemcpyAsync(tri_out, tri_dev, (size_t)n * sizeof(int32_t), cudaMemcpyDeviceToHost, stream)) !=
         cudaSuccess)
         return fail(e, "copy indices");
-    uint32_t err = 0;
     if ((e = cudaMemcpyAsync(&err, status, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream)) != cudaSuccess)
         return fail(e, "copy status");
     if ((e = cudaStreamSynchronize(stream)) != cudaSuccess) return fail(e, "intersect");

@@ -257,6 +257,7 @@ int32_t cvx_display_frame(cvx_display* d, const uint32_t* rgba, const uint32_t* 
                           uint32_t enable_median, uint32_t* out_srgb) {
     if (!d || !rgba || !gbuffer || !out_srgb) return cvx::set_error(CVX_ERR_INVALID, "null argument");
     CVX_ON_DEVICE(d->device);
+    cvx::StreamSync sync(d->stream);
     uint32_t npx = d->w * d->h;
     PCK(cudaMemcpyAsync(d->d_frame, rgba, (size_t)npx * 4, cudaMemcpyHostToDevice, d->stream), "upload frame");
     PCK(cudaMemcpyAsync(d->d_gbuf, gbuffer, (size_t)npx * 4, cudaMemcpyHostToDevice, d->stream), "upload gbuffer");
