@@ -350,14 +350,18 @@ typedef struct cvx_request_result {
 typedef struct cvx_server cvx_server;
 int32_t cvx_server_create(cvx_scene* const* scenes, uint32_t n_scenes, const cvx_server_config* config,
                           cvx_server** out);
-/* Queues a request; rgba (host, width*height words) must stay valid until the
- * request completes. CVX_ERR_CAPACITY if it can never be admitted. */
+/* Queues a request; rgba (host, width*height words, may be NULL) must stay
+ * valid until cvx_server_wait has returned the request's result (or the
+ * server is destroyed): a cancelled request whose image was already being
+ * copied out still writes it. CVX_ERR_CAPACITY if it can never be admitted. */
 int32_t cvx_server_submit(cvx_server* s, const cvx_request* req, uint32_t* rgba, uint64_t* id);
 /* Waits up to timeout_ms (0: just polls) for a request; CVX_ERR_TIMEOUT if
  * it is not done yet. The result is returned once and then forgotten. */
 int32_t cvx_server_wait(cvx_server* s, uint64_t id, uint32_t timeout_ms, cvx_request_result* result);
-/* Cancels a queued or running request (its result status becomes
- * CVX_ERR_CANCELLED). */
+/* Cancels a queued or running request: its result status becomes
+ * CVX_ERR_CANCELLED, unless its last sample had already finished (then the
+ * request completes normally). Returns at once; wait for the result before
+ * releasing the request's image buffer. */
 int32_t cvx_server_cancel(cvx_server* s, uint64_t id);
 /* Overrides one scene's kernel organisation (0 fused, 1 wavefront); only
  * while the server has no queued or admitted request. */
