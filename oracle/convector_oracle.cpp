@@ -1045,7 +1045,6 @@ void orc_resolve(const float* accum, uint32_t w, uint32_t h, uint32_t n, uint32_
         rgba[i] = pack_color(v3(accum[3 * i] * factor, accum[3 * i + 1] * factor, accum[3 * i + 2] * factor));
 }
 
-// renderer.rs:378-410 on a row-major w*h*3 accumulation buffer.
 // ---- element functions for the ported unit tests ----
 float orc_rcp(float x) { return rcp(x); }
 float orc_rsqrt(float x) { return rsqrt(x); }
@@ -1055,6 +1054,19 @@ float orc_cos(float x) { return poly_cos(x); }
 float orc_acos(float x) { return poly_acos(x); }
 float orc_acos_fast(float x) { return poly_acos_fast(x); }
 int32_t orc_cvtps(float x) { return cvtps(x); }
+// Mf32::mul_add / mul_sub / neg_mul_add (simd.rs:82-95) for kind 0 / 1 / 2.
+float orc_fma3(int kind, float a, float b, float c) {
+    return kind == 0 ? fmadd(a, b, c) : kind == 1 ? fmsub(a, b, c) : fnmadd(a, b, c);
+}
+// Mf32::abs (simd.rs:291-299): the sign bit cleared.
+float orc_abs(float x) { return fabs_bits(x); }
+// Mf32::any_sign_bit_positive_masked (simd.rs:355-371): not testc(a, mask),
+// on raw sign bits: some lane whose mask sign bit is set has its own clear.
+int orc_any_sign_bit_positive_masked(const float* a, const float* mask) {
+    for (int k = 0; k < 8; k++)
+        if ((fbits(mask[k]) >> 31) != 0u && (fbits(a[k]) >> 31) == 0u) return 1;
+    return 0;
+}
 
 void orc_rng_draws(uint32_t x, uint32_t y, uint32_t i, uint32_t n, uint32_t* out) {
     Rng r = Rng::with_seed(x, y, i);

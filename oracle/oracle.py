@@ -40,6 +40,8 @@ def lib():
             "orc_rcp": (F32, [F32]), "orc_rsqrt": (F32, [F32]), "orc_recip_precise": (F32, [F32]),
             "orc_sin": (F32, [F32]), "orc_cos": (F32, [F32]), "orc_acos": (F32, [F32]),
             "orc_acos_fast": (F32, [F32]), "orc_cvtps": (I32, [F32]),
+            "orc_fma3": (F32, [ctypes.c_int, F32, F32, F32]), "orc_abs": (F32, [F32]),
+            "orc_any_sign_bit_positive_masked": (ctypes.c_int, [P, P]),
             "orc_rng_draws": (None, [U32, U32, U32, U32, P]),
             "orc_rng_samples": (None, [U32, U32, U32, ctypes.c_int, U32, P]),
             "orc_rotate_hemisphere": (None, [P, P, P]),

@@ -229,3 +229,40 @@ def test_sky_intensity(orc):  # material.rs:205-215
     assert out.tolist() == [2.5, 2.5, 2.5]
     orc.lib().orc_sky_intensity(down.ctypes.data, out.ctypes.data)
     assert out.tolist() == [0.5, 0.5, 0.5]
+
+
+@pytest.mark.parametrize("kind,expected", [  # simd.rs:661-686 (mf32_fmadd_ps, fmsub_ps, fnmadd_ps)
+    (0, [5.0, 12.0, 7.0, 24.0, 1.0, 5.0, 11.0, 19.0]),
+    (1, [-5.0, 0.0, -7.0, 8.0, -1.0, -1.0, 1.0, 5.0]),
+    (2, [5.0, 0.0, 7.0, -8.0, 1.0, 1.0, -1.0, -5.0]),
+])
+def test_fused_multiply_add_forms(orc, kind, expected):
+    L = orc.lib()
+    a = [0.0, 1.0, 0.0, 2.0, 1.0, 2.0, 3.0, 4.0]
+    b = [5.0, 6.0, 7.0, 8.0, 0.0, 1.0, 2.0, 3.0]
+    c = [5.0, 6.0, 7.0, 8.0, 1.0, 3.0, 5.0, 7.0]
+    assert [L.orc_fma3(kind, x, y, z) for x, y, z in zip(a, b, c)] == expected
+
+
+def test_any_sign_bit_positive_masked(orc):  # simd.rs:695-707
+    L = orc.lib()
+    a = f32(-2.0, -1.0, -0.0, 0.0, 1.0, 2.0, 3.0, 4.0)
+    on = np.array([0xFFFFFFFF], np.uint32).view(np.float32)[0]
+
+    def mask(*bits):
+        return np.array([on if b else 0.0 for b in bits], np.float32)
+
+    cases = [((1, 0, 1, 1, 1, 0, 0, 0), True), ((1, 0, 1, 1, 0, 0, 0, 0), True),
+             ((1, 0, 1, 0, 0, 0, 0, 0), False), ((1, 1, 0, 0, 0, 0, 0, 0), False),
+             ((1, 0, 0, 1, 0, 0, 0, 0), True)]
+    for bits, want in cases:
+        m = mask(*bits)
+        assert bool(L.orc_any_sign_bit_positive_masked(a.ctypes.data, m.ctypes.data)) == want, bits
+
+
+def test_abs(orc):  # simd.rs:813-817
+    L = orc.lib()
+    x = [1.0, -1.0, 0.0, -0.0, 2.0, 3.0, 5.0, -7.0]
+    y = [L.orc_abs(v) for v in x]
+    assert y == [1.0, 1.0, 0.0, 0.0, 2.0, 3.0, 5.0, 7.0]
+    assert all(math.copysign(1.0, v) == 1.0 for v in y)  # -0 loses its sign too
