@@ -107,6 +107,9 @@ def _check_bvh(bvh, n_src):
             for c in (idx, idx + 1):
                 assert (f[c, 0:3] >= lo).all() and (f[c, 3:6] <= hi).all()
                 stack.append(c)
+            # an internal box encloses its children exactly (Aabb::enclose_aabbs, aabb.rs:185-192)
+            assert (np.minimum(f[idx, 0:3], f[idx + 1, 0:3]) == lo).all()
+            assert (np.maximum(f[idx, 3:6], f[idx + 1, 3:6]) == hi).all()
         else:
             covered[idx:idx + ln] += 1
             v = tf[idx:idx + ln, 0:9].reshape(-1, 3)
@@ -120,6 +123,10 @@ def _check_bvh(bvh, n_src):
 def _area(lo, hi):
     s = (hi - lo).astype(np.float32)
     return np.float32(2.0) * (s[1] * s[2] + s[2] * s[0] + s[0] * s[1])
+
+
+def test_area_known_answer():  # aabb.rs:194-199: width 4, height 5, depth 6
+    assert _area(np.array([1, 2, 3], np.float32), np.array([5, 7, 9], np.float32)) == 40.0 + 60.0 + 48.0
 
 
 def test_bvh_invariants_room_sphere(cvx):
