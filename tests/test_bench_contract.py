@@ -1,0 +1,41 @@
+"""bench.py's reference arm (the oracle's restatement of the reference's AVX
+packet traversal on the host cores) runs without a GPU: its JSON line carries
+the keys the benchmark contract asks for, and under several ranks only rank 0
+does work and prints."""
+
+import json
+import os
+import subprocess
+import sys
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _run(env_extra):
+    env = dict(os.environ)
+    env.update(env_extra)
+    p = subprocess.run([sys.executable, "bench.py", "--impl", "reference", "--steps", "3", "--warmup", "3"],
+                       cwd=ROOT, env=env, capture_output=True, text=True, timeout=600)
+    assert p.returncode == 0, p.stderr[-2000:]
+    return [ln for ln in p.stdout.splitlines() if ln.startswith("{")]
+
+
+def test_reference_arm_json_line():
+    lines = _run({"RANK": "0", "WORLD_SIZE": "1"})
+    assert len(lines) == 1
+    r = json.loads(lines[0])
+    for key in ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "higher_is_better",
+                "scaling", "vs_baseline", "dtype", "data", "config", "cpu_baseline", "e2e"):
+        assert key in r, key
+    assert r["impl"] == "reference" and r["steps"] == 3 and r["warmup"] == 3 and r["n_gpus"] == 1
+    assert r["value"] > 0 and r["unit"] == "Mrays/s" and r["higher_is_better"] is True
+    assert "workload" in r["config"]
+    cb = r["cpu_baseline"]
+    assert cb["kind"] == "port" and cb["cores"] >= 1 and cb["value"] == r["value"] and cb["sample"]
+    e = r["e2e"]
+    assert e["value"] == r["value"] and e["unit"] == r["unit"]
+    assert e["h2d_bytes_per_step"] == 0 and e["d2h_bytes_per_step"] == 0
+
+
+def test_reference_arm_other_ranks_do_nothing():
+    assert _run({"RANK": "1", "WORLD_SIZE": "2", "LOCAL_RANK": "1"}) == []
