@@ -91,6 +91,7 @@ def lib(build=False):
     P, U32, I32, F32, SZ = ctypes.c_void_p, ctypes.c_uint32, ctypes.c_int32, ctypes.c_float, ctypes.c_size_t
     sig = {
         "cvx_last_error": (I32, [ctypes.c_char_p, SZ]),
+        "cvx_device_info": (I32, [P, ctypes.c_char_p, SZ]),
         "cvx_mesh_load_obj": (I32, [ctypes.c_char_p, P, P, U32, P]),
         "cvx_mesh_parse_obj": (I32, [ctypes.c_char_p, SZ, P, P, U32, P]),
         "cvx_mesh_num_triangles": (U32, [P]),
@@ -167,6 +168,13 @@ def _check(status):
 
 def _ptr(a):
     return None if a is None else ctypes.c_void_p(a.ctypes.data)
+
+
+def device_info():
+    """(ordinal, name) of the device new handles of this thread belong to."""
+    ordinal, name = ctypes.c_int32(), ctypes.create_string_buffer(256)
+    _check(lib().cvx_device_info(ctypes.byref(ordinal), name, 256))
+    return ordinal.value, name.value.decode(errors="replace")
 
 
 def _host_rays(origins, directions):

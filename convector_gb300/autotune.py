@@ -10,20 +10,28 @@ with the single-ray and the 8-ray packet traversal. The traversal stack holds
 128 entries; a scene needs BVH depth + 2 (checked at scene creation), so stack
 depth is not a tuning knob: untouched entries cost nothing.
 
-Results are cached per (scene size, BVH depth, frame size, RNG order) in a
-JSON file (CONVECTOR_AUTOTUNE_CACHE, default ~/.cache/convector_gb300/autotune.json).
+Results are cached per (GPU model, library build, scene size, BVH depth, frame
+size, RNG order) in a JSON file (CONVECTOR_AUTOTUNE_CACHE, default
+~/.cache/convector_gb300/autotune.json), so a choice timed on another GPU model
+or with other kernels is not reused.
 """
 
 import json
 import os
 
 from . import (MODE_MEGAKERNEL, MODE_WAVEFRONT, REFILL_AFTER_CAMERA, REFILL_ALL, REFILL_NONE, RNG_GROUP,
-               TRAVERSE_PACKET, TRAVERSE_SINGLE, Renderer)
+               TRAVERSE_PACKET, TRAVERSE_SINGLE, Renderer, _build, device_info)
 
 
 def _cache_path():
     return os.environ.get("CONVECTOR_AUTOTUNE_CACHE",
                           os.path.join(os.path.expanduser("~"), ".cache", "convector_gb300", "autotune.json"))
+
+
+def _build_key():
+    """The GPU model and the identity (size, modification time) of the loaded library."""
+    st = os.stat(_build.LIB)
+    return "gpu=%s lib=%d:%d" % (device_info()[1], st.st_size, int(st.st_mtime))
 
 
 def candidates(rng_order=RNG_GROUP, allow_packet=True):
@@ -63,8 +71,8 @@ def measure(scene, width, height, config, frames=5, warmup=2, first_frame=1000):
 def tune(scene, width, height, rng_order=RNG_GROUP, allow_packet=True, frames=5, use_cache=True):
     """Returns (best config dict, {config key: ms}) for this scene and frame size."""
     b = scene.bvh
-    key = "tris=%d nodes=%d depth=%d %dx%d rng=%d packet=%d" % (
-        b.triangles.shape[0], b.nodes.shape[0], b.depth, width, height, rng_order, int(allow_packet))
+    key = "%s tris=%d nodes=%d depth=%d %dx%d rng=%d packet=%d" % (
+        _build_key(), b.triangles.shape[0], b.nodes.shape[0], b.depth, width, height, rng_order, int(allow_packet))
     path = _cache_path()
     cache = {}
     if use_cache and os.path.exists(path):

@@ -216,6 +216,24 @@ static int32_t validate_tree(const cvx_bvh_node* nodes, uint32_t n_nodes, uint32
 
 extern "C" {
 
+int32_t cvx_device_info(int32_t* ordinal, char* name, size_t name_len) {
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) {
+        cudaGetLastError();
+        return set_error(CVX_ERR_CUDA, "no CUDA device available");
+    }
+    int dev = 0;
+    CK(cudaGetDevice(&dev), "cudaGetDevice");
+    cudaDeviceProp prop{};
+    CK(cudaGetDeviceProperties(&prop, dev), "cudaGetDeviceProperties");
+    if (ordinal) *ordinal = dev;
+    if (name && name_len) {
+        std::strncpy(name, prop.name, name_len - 1);
+        name[name_len - 1] = '\0';
+    }
+    return CVX_OK;
+}
+
 int32_t cvx_scene_create(const cvx_triangle* tris, uint32_t n_tris, const cvx_bvh_node* nodes, uint32_t n_nodes,
                          cvx_scene** out) {
     if (!tris || !nodes || !out || n_tris == 0) return set_error(CVX_ERR_INVALID, "null argument or empty scene");

@@ -123,6 +123,11 @@ void cvx_camera_set_interactive(cvx_camera* cam, float time, float time_delta);
 
 /* ---- device: scenes ------------------------------------------------------ */
 
+/* The device that handles created now by the calling thread would belong to:
+ * its ordinal and its name (NUL-terminated, truncated to name_len). No
+ * counterpart in the reference; the autotuner keys its cache on it. */
+int32_t cvx_device_info(int32_t* ordinal, char* name, size_t name_len);
+
 /* Scene::from_meshes (scene.rs:114-129) given a built BVH: uploads nodes and
  * triangles in BVH order and the direct-sample list (triangles with material
  * bit 30). Rejects trees deeper than the device traversal stack and

@@ -530,3 +530,10 @@ def test_reference_light_pick_with_eight_lights(gpu, orc):
     osc = orc.OracleScene.from_bvh(bvh, general_pick=False)
     (rgba, gb, col, rays), (orgba, ogb, ocol, orays) = _render_both(gpu, orc, scene, osc, 160, 96, 42, 0, 0)
     assert (col.view(np.uint32) == ocol.view(np.uint32)).all() and rays == orays
+
+
+def test_device_info(gpu):
+    import torch
+    ordinal, name = gpu.device_info()
+    assert ordinal == torch.cuda.current_device()
+    assert name == torch.cuda.get_device_name(ordinal)

@@ -368,3 +368,13 @@ def test_interactive_camera_path(cvx, time, delta):
     assert np.array(c._c.orientation, np.float32).tobytes() == np.array(r._c.orientation, np.float32).tobytes()
     assert np.array(c._c.orientation_delta, np.float32).tobytes() == \
         np.array(r._c.orientation_delta, np.float32).tobytes()
+
+
+def test_device_info_without_a_device(cvx):
+    # Nothing falls back to the CPU: without a usable device the call reports CVX_ERR_CUDA.
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a CUDA device is present")
+    with pytest.raises(cvx.CvxError) as e:
+        cvx.device_info()
+    assert e.value.status == 5
