@@ -71,8 +71,11 @@ def measure(scene, width, height, config, frames=5, warmup=2, first_frame=1000):
 def tune(scene, width, height, rng_order=RNG_GROUP, allow_packet=True, frames=5, use_cache=True):
     """Returns (best config dict, {config key: ms}) for this scene and frame size."""
     b = scene.bvh
-    key = "%s tris=%d nodes=%d depth=%d %dx%d rng=%d packet=%d" % (
-        _build_key(), b.triangles.shape[0], b.nodes.shape[0], b.depth, width, height, rng_order, int(allow_packet))
+    key = None
+    if use_cache:
+        key = "%s tris=%d nodes=%d depth=%d %dx%d rng=%d packet=%d" % (
+            _build_key(), b.triangles.shape[0], b.nodes.shape[0], b.depth, width, height, rng_order,
+            int(allow_packet))
     path = _cache_path()
     cache = {}
     if use_cache and os.path.exists(path):
