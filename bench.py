@@ -461,15 +461,22 @@ def bench_large(cg):
     return out
 
 
+def _c3_plan(rng, n):
+    """Triangle counts (log-uniform 500..20,000) and resolutions (one of
+    320x184, 640x368, 1280x736) of the batch's n scenes."""
+    counts = np.exp(rng.uniform(np.log(500), np.log(20000), n)).astype(int)
+    sizes = [(320, 184), (640, 368), (1280, 736)]
+    res = [sizes[i] for i in rng.integers(0, 3, n)]
+    return counts, res
+
+
 def _c3_views(cg, n=256, seed=3):
     """256 scenes of spheres and boxes, log-uniform 500..20,000 triangles, one
     camera and a resolution from {320x184, 640x368, 1280x736} each, 4 spp."""
     from concurrent.futures import ThreadPoolExecutor
     from convector_gb300 import scenes
     rng = np.random.default_rng(seed)
-    counts = np.exp(rng.uniform(np.log(500), np.log(20000), n)).astype(int)
-    sizes = [(320, 184), (640, 368), (1280, 736)]
-    res = [sizes[i] for i in rng.integers(0, 3, n)]
+    counts, res = _c3_plan(rng, n)
     tri_arrays = [scenes.spheres_and_boxes(int(c), seed=seed * 100003 + i, obj=False)[0] for i, c in enumerate(counts)]
     with ThreadPoolExecutor(8) as ex:
         bvhs = list(ex.map(cg.Bvh.build, tri_arrays))

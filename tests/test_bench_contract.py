@@ -1,7 +1,8 @@
-"""bench.py's reference arm (the oracle's restatement of the reference's AVX
-packet traversal on the host cores) runs without a GPU: its JSON line carries
-the keys the benchmark contract asks for, and under several ranks only rank 0
-does work and prints."""
+"""bench.py on the CPU. The reference arm (the oracle's restatement of the
+reference's AVX packet traversal on the host cores) runs without a GPU: its
+JSON line carries the keys the benchmark contract asks for, and under several
+ranks only rank 0 does work and prints. The synthetic batch workload has the
+shape it is specified with."""
 
 import json
 import os
@@ -39,3 +40,22 @@ def test_reference_arm_json_line():
 
 def test_reference_arm_other_ranks_do_nothing():
     assert _run({"RANK": "1", "WORLD_SIZE": "2", "LOCAL_RANK": "1"}) == []
+
+
+def test_batched_workload_shape():
+    """The 256-scene batch: log-uniform 500..20,000 triangles (mean near
+    19,500 / ln 40 = 5,286) and all three resolutions; the spheres-and-boxes
+    generator lands within 2 % above each count."""
+    import math
+
+    import numpy as np
+
+    import bench
+    from convector_gb300 import scenes
+    counts, res = bench._c3_plan(np.random.default_rng(3), 256)
+    assert counts.min() >= 500 and counts.max() <= 20000
+    assert abs(counts.mean() - 19500 / math.log(40)) < 0.1 * 5286
+    assert set(res) == {(320, 184), (640, 368), (1280, 736)}
+    for n in (500, 1234, 5000, 20000):
+        t, _ = scenes.spheres_and_boxes(n, 3, obj=False)
+        assert n <= t.shape[0] <= 1.02 * n + 2
