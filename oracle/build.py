@@ -1,8 +1,10 @@
 """Builds liboracle.so, the CPU restatement used as the test oracle and as the
 timed CPU baseline. Test infrastructure only: the product never loads it.
 
-Portable C++ (no intrinsics); -ffp-contract=off keeps every float operation
-rounding where the reference's does. On x86-64 the FMA and AVX2 instruction
+Portable C++ (no intrinsics; the packet traversal uses the GCC/Clang 8-float
+vector extension, lowered to the target's own vector registers);
+-ffp-contract=off keeps every float operation rounding where the reference's
+does. On x86-64 the FMA and AVX2 instruction
 sets are enabled for speed only: results are the same without them.
 """
 

@@ -210,73 +210,149 @@ inline void tri_intersect(const Tri& tr, int32_t idx, const Ray& r, bool active,
 }
 
 // bvh.rs:589-657, the 8-ray packet traversal, with its debug counters.
-struct Entry {
-    const Node* node;
-    BoxHit b[8];
-};
-inline bool should_try_before(const BoxHit a[8], const BoxHit b[8]) {  // aabb.rs:180-182
-    for (int j = 0; j < 8; j++)
-        if (sneg(a[j].tmin - b[j].tmin)) return false;
-    return true;
+// The packet traversal works on all 8 lanes at once, in the shape of the
+// reference's Mf32: a GCC/Clang vector of 8 floats (one AVX register on
+// x86-64, two NEON registers on aarch64). Its operations are elementwise IEEE
+// operations, never fused or reordered (-ffp-contract=off), so every lane
+// rounds exactly as box_hit above does for one ray.
+typedef float F8 __attribute__((vector_size(32)));
+typedef int32_t I8 __attribute__((vector_size(32)));
+// Always inlined: where the target's registers are narrower than 8 floats,
+// an 8-float value passed to a call would go through memory.
+#define ORC_V8 inline __attribute__((always_inline))
+
+ORC_V8 F8 splat8(float x) { return F8{x, x, x, x, x, x, x, x}; }
+ORC_V8 F8 vmin8(F8 a, F8 b) { return a < b ? a : b; }  // xmin per lane
+ORC_V8 F8 vmax8(F8 a, F8 b) { return a > b ? a : b; }  // xmax per lane
+// sneg per lane (sign bit set, or NaN): all ones where it holds.
+ORC_V8 I8 vsneg8(F8 x) {
+    I8 bits;
+    std::memcpy(&bits, &x, sizeof bits);
+    return (bits < 0) | (x != x);
 }
-inline bool any_masked(const BoxHit b[8], const bool active[8]) {  // aabb.rs:155-166
+ORC_V8 bool any8(I8 m) {
     for (int j = 0; j < 8; j++)
-        if (b[j].mask && active[j] && !sneg(b[j].tmax)) return true;
+        if (m[j]) return true;
     return false;
 }
-inline bool further_away(const BoxHit b[8], const Isect is[8], const bool active[8]) {  // aabb.rs:171-177
-    for (int j = 0; j < 8; j++)
-        if (b[j].mask && !(geq(b[j].tmin, is[j].dist) || !active[j])) return false;
-    return true;
+
+ORC_V8 F8 fmadd8(F8 a, F8 b, F8 c) {  // fmadd per lane
+    F8 r;
+    for (int j = 0; j < 8; j++) r[j] = std::fma(a[j], b[j], c[j]);
+    return r;
+}
+ORC_V8 F8 fmsub8(F8 a, F8 b, F8 c) { return fmadd8(a, b, -c); }  // fmsub per lane
+
+struct Packet8 {  // origins, directions and reciprocal directions of the 8 rays
+    F8 ox, oy, oz, dx, dy, dz, ix, iy, iz;
+    I8 active;  // all ones where the lane is active
+};
+struct BoxHit8 {
+    F8 tmin, tmax;
+    I8 mask;  // geq(tmax, tmin) per lane
+};
+// Aabb::intersect (aabb.rs:105-141) for the 8 rays of a packet.
+ORC_V8 BoxHit8 box_hit8(const Node& n, const Packet8& p) {
+    F8 tx1 = (splat8(n.origin[0]) - p.ox) * p.ix, tx2 = (splat8(n.far_[0]) - p.ox) * p.ix;
+    F8 txmin = vmin8(tx1, tx2), txmax = vmax8(tx1, tx2);
+    F8 ty1 = (splat8(n.origin[1]) - p.oy) * p.iy, ty2 = (splat8(n.far_[1]) - p.oy) * p.iy;
+    F8 tymin = vmin8(ty1, ty2), tymax = vmax8(ty1, ty2);
+    F8 tz1 = (splat8(n.origin[2]) - p.oz) * p.iz, tz2 = (splat8(n.far_[2]) - p.oz) * p.iz;
+    F8 tzmin = vmin8(tz1, tz2), tzmax = vmax8(tz1, tz2);
+    BoxHit8 h;
+    h.tmin = vmax8(txmin, vmax8(tymin, tzmin));
+    h.tmax = vmin8(txmax, vmin8(tymax, tzmax));
+    h.mask = ~(h.tmax < h.tmin);
+    return h;
+}
+struct Entry {
+    const Node* node;
+    BoxHit8 b;
+};
+ORC_V8 bool should_try_before(const BoxHit8& a, const BoxHit8& b) {  // aabb.rs:180-182
+    return !any8(vsneg8(a.tmin - b.tmin));
+}
+ORC_V8 bool any_masked(const BoxHit8& b, const Packet8& p) {  // aabb.rs:155-166
+    return any8(b.mask & p.active & ~vsneg8(b.tmax));
+}
+ORC_V8 bool further_away(const BoxHit8& b, const Isect is[8], const Packet8& p) {  // aabb.rs:171-177
+    F8 dist;
+    for (int j = 0; j < 8; j++) dist[j] = is[j].dist;
+    return !any8(b.mask & (b.tmin < dist) & p.active);
+}
+
+// Triangle::intersect (triangle.rs:59-148) for the 8 rays of a packet: the
+// lane arithmetic of tri_intersect, with the triangle's edges and normal
+// computed once; the hit record of each lane that is not rejected is taken
+// as tri_intersect takes it.
+ORC_V8 void tri_intersect8(const Tri& tr, int32_t idx, const Packet8& p, const Ray r[8], Isect is[8]) {
+    V3 v0 = ld(tr.v0), v1 = ld(tr.v1), v2 = ld(tr.v2);
+    V3 e1 = v0 - v2, e2 = v1 - v0;
+    V3 n = cross(e1, e2);
+    F8 frx = splat8(v0.x) - p.ox, fry = splat8(v0.y) - p.oy, frz = splat8(v0.z) - p.oz;
+    F8 denom = splat8(1.0f) / (p.dx * n.x + p.dy * n.y + p.dz * n.z);
+    F8 t = (frx * n.x + fry * n.y + frz * n.z) * denom;
+    F8 cx = fmsub8(p.dy, frz, p.dz * fry), cy = fmsub8(p.dz, frx, p.dx * frz), cz = fmsub8(p.dx, fry, p.dy * frx);
+    F8 u = (cx * e2.x + cy * e2.y + cz * e2.z) * denom;
+    F8 v = (cx * e1.x + cy * e1.y + cz * e1.z) * denom;
+    F8 w = (splat8(1.0f) - u) - v;
+    F8 dist;
+    for (int j = 0; j < 8; j++) dist[j] = is[j].dist;
+    I8 keep = ~(vsneg8(t) | vsneg8(u) | vsneg8(v) | vsneg8(w)) & p.active & (t < dist);
+    if (!any8(keep)) return;
+    for (int j = 0; j < 8; j++) {
+        if (!keep[j]) continue;
+        Isect& h = is[j];
+        h.pos = vfma(r[j].d, t[j], r[j].o);
+        h.normal = normalized(n);
+        h.dist = t[j];
+        h.mat = tr.material;
+        h.tu = fmadd(tr.uv0[0], w[j], fmadd(tr.uv1[0], v[j], tr.uv2[0] * u[j]));
+        h.tv = fmadd(tr.uv0[1], w[j], fmadd(tr.uv1[1], v[j], tr.uv2[1] * u[j]));
+        h.tri = idx;
+    }
 }
 
 void packet_traverse(const Scene& s, const Ray r[8], const bool active[8], Isect is[8], uint32_t* numi_aabb,
                      uint32_t* numi_tri) {
-    V3 inv[8];
-    for (int j = 0; j < 8; j++) inv[j] = v3(rcp(r[j].d.x), rcp(r[j].d.y), rcp(r[j].d.z));
+    Packet8 p;
+    for (int j = 0; j < 8; j++) {
+        p.ox[j] = r[j].o.x;
+        p.oy[j] = r[j].o.y;
+        p.oz[j] = r[j].o.z;
+        p.dx[j] = r[j].d.x;
+        p.dy[j] = r[j].d.y;
+        p.dz[j] = r[j].d.z;
+        p.ix[j] = rcp(r[j].d.x);
+        p.iy[j] = rcp(r[j].d.y);
+        p.iz[j] = rcp(r[j].d.z);
+        p.active[j] = active[j] ? -1 : 0;
+    }
     std::vector<Entry> stack;
     stack.reserve(32);
     uint32_t na = 2, nt = 0;
-    const Node* n0 = &s.nodes[0];
-    const Node* n1 = &s.nodes[1];
-    Entry e0, e1;
-    e0.node = n0;
-    e1.node = n1;
-    for (int j = 0; j < 8; j++) {
-        e0.b[j] = box_hit(*n0, r[j].o, inv[j]);
-        e1.b[j] = box_hit(*n1, r[j].o, inv[j]);
-    }
-    if (should_try_before(e0.b, e1.b)) {
-        if (any_masked(e0.b, active)) stack.push_back(e0);
-        if (any_masked(e1.b, active)) stack.push_back(e1);
-    } else {
-        if (any_masked(e1.b, active)) stack.push_back(e1);
-        if (any_masked(e0.b, active)) stack.push_back(e0);
-    }
+    auto push_pair = [&](const Node* n0, const Node* n1) {
+        Entry e0{n0, box_hit8(*n0, p)}, e1{n1, box_hit8(*n1, p)};
+        if (should_try_before(e0.b, e1.b)) {
+            if (any_masked(e0.b, p)) stack.push_back(e0);
+            if (any_masked(e1.b, p)) stack.push_back(e1);
+        } else {
+            if (any_masked(e1.b, p)) stack.push_back(e1);
+            if (any_masked(e0.b, p)) stack.push_back(e0);
+        }
+    };
+    push_pair(&s.nodes[0], &s.nodes[1]);
     while (!stack.empty()) {
         Entry e = stack.back();
         stack.pop_back();
-        if (further_away(e.b, is, active)) continue;
+        if (further_away(e.b, is, p)) continue;
         const Node& nd = *e.node;
         if (nd.len == 0) {
             na += 2;
-            Entry c0, c1;
-            c0.node = &s.nodes[nd.index];
-            c1.node = &s.nodes[nd.index + 1];
-            for (int j = 0; j < 8; j++) {
-                c0.b[j] = box_hit(*c0.node, r[j].o, inv[j]);
-                c1.b[j] = box_hit(*c1.node, r[j].o, inv[j]);
-            }
-            if (should_try_before(c0.b, c1.b)) {
-                if (any_masked(c0.b, active)) stack.push_back(c0);
-                if (any_masked(c1.b, active)) stack.push_back(c1);
-            } else {
-                if (any_masked(c1.b, active)) stack.push_back(c1);
-                if (any_masked(c0.b, active)) stack.push_back(c0);
-            }
+            push_pair(&s.nodes[nd.index], &s.nodes[nd.index + 1]);
         } else {
             for (uint32_t i = nd.index; i < nd.index + nd.len; i++) {
-                for (int j = 0; j < 8; j++) tri_intersect(s.tris[i], (int32_t)i, r[j], active[j], is[j]);
+                tri_intersect8(s.tris[i], (int32_t)i, p, r, is);
                 nt++;
             }
         }
