@@ -496,17 +496,49 @@ inline DirectHit intersect_direct(const Tri& tr, const Ray& r) {
     return h;
 }
 
-// material.rs:281-320
-inline float pd_direct_sample(const Scene& s, const Ray& r) {
-    float pd_total = 0.0f;
-    for (uint32_t li : s.ds) {
-        DirectHit h = intersect_direct(s.tris[li], r);
-        float dsq = h.dist * h.dist;
-        float dot_em = fabs_bits(dot(h.normal, r.d)) + 0.0001f;
-        float pd = dsq * rcp(h.area * dot_em);
-        pd_total = h.miss ? pd_total : pd_total + pd;
+// pd_direct_sample (material.rs:281-320) for the 8 rays of a group at once:
+// per light, the lane arithmetic of intersect_direct above, with the light
+// triangle's edges, normal and area computed once.
+void pd_direct_sample8(const Scene& s, const Ray r[8], float out[8]) {
+    F8 ox, oy, oz, dx, dy, dz;
+    for (int j = 0; j < 8; j++) {
+        ox[j] = r[j].o.x;
+        oy[j] = r[j].o.y;
+        oz[j] = r[j].o.z;
+        dx[j] = r[j].d.x;
+        dy[j] = r[j].d.y;
+        dz[j] = r[j].d.z;
     }
-    return pd_total * (1.0f / (float)s.ds.size());
+    F8 pd_total = splat8(0.0f);
+    for (uint32_t li : s.ds) {
+        const Tri& tr = s.tris[li];
+        V3 v0 = ld(tr.v0), v1 = ld(tr.v1), v2 = ld(tr.v2);
+        V3 e1 = v0 - v2, e2 = v1 - v0;
+        V3 n = cross(e1, e2);
+        float rnorm = rsqrt(dot(n, n));
+        float area = 0.5f * rcp(rnorm);
+        V3 nn = scale(n, rnorm);
+        F8 frx = splat8(v0.x) - ox, fry = splat8(v0.y) - oy, frz = splat8(v0.z) - oz;
+        F8 denom = dx * n.x + dy * n.y + dz * n.z;
+        for (int j = 0; j < 8; j++) denom[j] = rcp(denom[j]);
+        F8 t = (frx * n.x + fry * n.y + frz * n.z) * denom;
+        F8 cx = fmsub8(dy, frz, dz * fry), cy = fmsub8(dz, frx, dx * frz), cz = fmsub8(dx, fry, dy * frx);
+        F8 u = (cx * e2.x + cy * e2.y + cz * e2.z) * denom;
+        F8 v = (cx * e1.x + cy * e1.y + cz * e1.z) * denom;
+        I8 miss = vsneg8(u) | vsneg8(v) | vsneg8(t) | ~((u + v) < splat8(1.0f));
+        F8 dsq = t * t;
+        F8 dn = splat8(nn.x) * dx + splat8(nn.y) * dy + splat8(nn.z) * dz;
+        I8 bits;
+        std::memcpy(&bits, &dn, sizeof bits);
+        bits &= 0x7fffffff;
+        std::memcpy(&dn, &bits, sizeof bits);
+        F8 q = splat8(area) * (dn + 0.0001f);
+        for (int j = 0; j < 8; j++) q[j] = rcp(q[j]);
+        F8 pd = dsq * q;
+        pd_total = miss ? pd_total : pd_total + pd;
+    }
+    const float k = 1.0f / (float)s.ds.size();
+    for (int j = 0; j < 8; j++) out[j] = pd_total[j] * k;
 }
 
 inline uint32_t light_pick(const Scene& s, uint32_t bits) {
@@ -532,9 +564,12 @@ void continue_path(const Scene& s, Ray ray[8], bool active[8], const Isect is[8]
     rng.next(du);
     rng.next(dv);
     rng.next(drr);
+    // First the next ray of every lane, then the 8 light PDFs together, then
+    // the rest of each lane.
+    Ray nrs[8];
+    bool picks[8];
     for (int j = 0; j < 8; j++) {
         const Isect& I = is[j];
-        bool inactive = !active[j] || (I.mat >> 31) != 0u;
         // BRDF sample
         V3 dir_b = rotate_hemisphere(hemisphere_from(dphi[j], dr[j]), I.normal);
         V3 org_b = vfma(dir_b, 1.0e-4f, I.pos);
@@ -555,11 +590,19 @@ void continue_path(const Scene& s, Ray ray[8], bool active[8], const Isect is[8]
         // one-sample MIS
         float rr = fmadd(I.normal.z, 0.8f, biunit_from(drr[j]));
         bool pick_direct = sneg(rr);
-        Ray nr;
-        nr.o = vpick(org_b, org_d, pick_direct);
-        nr.d = vpick(dir_b, dir_d, pick_direct);
+        picks[j] = pick_direct;
+        nrs[j].o = vpick(org_b, org_d, pick_direct);
+        nrs[j].d = vpick(dir_b, dir_d, pick_direct);
+    }
+    float pds[8];
+    pd_direct_sample8(s, nrs, pds);
+    for (int j = 0; j < 8; j++) {
+        const Isect& I = is[j];
+        bool inactive = !active[j] || (I.mat >> 31) != 0u;
+        const bool pick_direct = picks[j];
+        const Ray& nr = nrs[j];
         float pd_b = xmax(dot(I.normal, nr.d), 0.0f) * (1.0f / kPi);
-        float pd_d = pd_direct_sample(s, nr);
+        float pd_d = pds[j];
         float wden = pd_b + pd_d + 0.01f;
         float p_brdf = fmadd(I.normal.z, 0.4f, 0.5f);
         float p_direct = fnmadd(I.normal.z, 0.4f, 0.5f);
