@@ -210,11 +210,12 @@ inline void tri_intersect(const Tri& tr, int32_t idx, const Ray& r, bool active,
 }
 
 // bvh.rs:589-657, the 8-ray packet traversal, with its debug counters.
-// The packet traversal works on all 8 lanes at once, in the shape of the
-// reference's Mf32: a GCC/Clang vector of 8 floats (one AVX register on
-// x86-64, two NEON registers on aarch64). Its operations are elementwise IEEE
-// operations, never fused or reordered (-ffp-contract=off), so every lane
-// rounds exactly as box_hit above does for one ray.
+// The packet traversal and the light PDFs of a group work on all 8 lanes at
+// once, in the shape of the reference's Mf32: a GCC/Clang vector of 8 floats
+// (one AVX register on x86-64, two NEON registers on aarch64). Its operations
+// are elementwise IEEE operations, never fused or reordered
+// (-ffp-contract=off), so every lane rounds exactly as the one-ray functions
+// above (box_hit, tri_intersect, intersect_direct) do.
 typedef float F8 __attribute__((vector_size(32)));
 typedef int32_t I8 __attribute__((vector_size(32)));
 // Always inlined: where the target's registers are narrower than 8 floats,
