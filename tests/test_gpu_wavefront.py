@@ -198,3 +198,26 @@ def test_server_admission_cancel_timeout(two_scenes, gpu):
         srv.wait(123456)
     assert e.value.status == 10
     srv.close()
+
+
+def test_size_limits_refused_on_the_host(two_scenes, gpu):
+    """Image sides above 16384 pixels and larger patches are refused by the
+    renderer, the batch and the server before any device work."""
+    scs = [s for _, s, _ in two_scenes]
+    cam = scenes.default_camera(gpu.Camera())
+    with pytest.raises(gpu.CvxError) as e:
+        gpu.Renderer(scs[0], 16385, 16)
+    assert e.value.status == 1
+    r = gpu.Renderer(scs[0], 64, 32)
+    with pytest.raises(gpu.CvxError) as e:
+        r.render_patches_u8(16400, [(0, 0)], 1)
+    assert e.value.status == 1
+    batch = gpu.Batch(scs, max_groups=1 << 14, max_pixels=1 << 20)
+    with pytest.raises(gpu.CvxError) as e:
+        batch.render([gpu.View(0, 16400, 4, 1, 0, cam)], want_images=False)
+    assert e.value.status == 1
+    srv = gpu.Server(scs, framebuffer_bytes=64 << 20, max_groups=1 << 14)
+    with pytest.raises(gpu.CvxError) as e:
+        srv.submit(0, 16, 16400, 1, cam)
+    assert e.value.status == 1
+    srv.close()
