@@ -21,7 +21,7 @@ def _run(env_extra):
     return [ln for ln in p.stdout.splitlines() if ln.startswith("{")]
 
 
-def test_reference_arm_json_line():
+def test_reference_arm_json_line(cvx):  # cvx: the library is built
     lines = _run({"RANK": "0", "WORLD_SIZE": "1"})
     assert len(lines) == 1
     r = json.loads(lines[0])
@@ -38,11 +38,11 @@ def test_reference_arm_json_line():
     assert e["h2d_bytes_per_step"] == 0 and e["d2h_bytes_per_step"] == 0
 
 
-def test_reference_arm_other_ranks_do_nothing():
+def test_reference_arm_other_ranks_do_nothing(cvx):
     assert _run({"RANK": "1", "WORLD_SIZE": "2", "LOCAL_RANK": "1"}) == []
 
 
-def test_batched_workload_shape():
+def test_batched_workload_shape(cvx):
     """The 256-scene batch: log-uniform 500..20,000 triangles (mean near
     19,500 / ln 40 = 5,286) and all three resolutions; the spheres-and-boxes
     generator lands within 2 % above each count."""
