@@ -112,6 +112,8 @@ def lib(build=False):
         "cvx_camera_set_interactive": (None, [P, F32, F32]),
         "cvx_renderer_set_time": (I32, [P, F32, F32]),
         "cvx_renderer_update_scene": (I32, [P]),
+        "cvx_set_traversal_stack_limit": (I32, [U32]),
+        "cvx_inject_allocation_failure": (I32, [I32]),
         "cvx_scene_create": (I32, [P, U32, P, U32, P]),
         "cvx_scene_from_bvh": (I32, [P, P]),
         "cvx_scene_num_direct_samples": (U32, [P]),
@@ -164,6 +166,18 @@ def _check(status):
         buf = ctypes.create_string_buffer(1024)
         lib().cvx_last_error(buf, 1024)
         raise CvxError(status, buf.value.decode(errors="replace"))
+
+
+def set_traversal_stack_limit(entries):
+    """Lowers the traversal stack's capacity on the current device (0: the
+    default 128) so that tests can run the stack-overflow status path."""
+    _check(lib().cvx_set_traversal_stack_limit(int(entries)))
+
+
+def inject_allocation_failure(after):
+    """The library's next `after` device allocations succeed and the one after
+    them fails as out of memory (CVX_ERR_CAPACITY); negative cancels."""
+    _check(lib().cvx_inject_allocation_failure(int(after)))
 
 
 def _ptr(a):

@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstring>
 #include <memory>
@@ -59,10 +60,16 @@ int32_t ensure_device(int* dev_out) {
     return CVX_OK;
 }
 
+// Device allocations that succeed before an injected failure (-1: none
+// pending). Process-wide: the allocation helpers of every thread count down.
+std::atomic<int64_t> g_alloc_countdown{-1};
+
 template <class T>
 int32_t dalloc(T** p, size_t count, const char* what) {
     *p = nullptr;
     if (count == 0) count = 1;
+    if (injected_allocation_failure())
+        return set_error(CVX_ERR_CAPACITY, std::string("cudaMalloc ") + what + ": out of memory (injected)");
     cudaError_t e = cudaMalloc((void**)p, count * sizeof(T));
     if (e != cudaSuccess) {
         cudaGetLastError();
@@ -84,6 +91,13 @@ bool page_locked(const void* p) {
 }
 
 }  // namespace
+
+bool cvx::injected_allocation_failure() {
+    int64_t v = g_alloc_countdown.load();
+    while (v >= 0)
+        if (g_alloc_countdown.compare_exchange_weak(v, v - 1)) return v == 0;
+    return false;
+}
 
 struct cvx_scene {
     int device = 0;
@@ -151,6 +165,7 @@ cudaStream_t cvx::scene_stream(const cvx_scene* s) { return s->stream; }
 uint32_t cvx::scene_depth(const cvx_scene* s) { return s->depth; }
 uint32_t cvx::scene_num_lights(const cvx_scene* s) { return s->n_lights; }
 int cvx::scene_device(const cvx_scene* s) { return s->device; }
+uint32_t cvx::scene_query_blocks_per_sm(const cvx_scene* s) { return s->blocks_per_sm; }
 
 struct cvx_renderer {
     std::unique_ptr<WaveEngine> engine;  // wavefront mode
@@ -234,6 +249,23 @@ int32_t cvx_device_info(int32_t* ordinal, char* name, size_t name_len) {
     return CVX_OK;
 }
 
+int32_t cvx_set_traversal_stack_limit(uint32_t entries) {
+    if (entries == 0) entries = (uint32_t)kStackDepth;
+    if (entries < 2 || entries > (uint32_t)kStackDepth)
+        return set_error(CVX_ERR_INVALID, "the traversal stack limit must be 2.." + std::to_string(kStackDepth));
+    int dev = 0;
+    int32_t st = ensure_device(&dev);
+    if (st) return st;
+    CK(set_stack_limit((int)entries), "set the traversal stack limit");
+    CK(set_stack_limit_wave((int)entries), "set the traversal stack limit");
+    return CVX_OK;
+}
+
+int32_t cvx_inject_allocation_failure(int32_t after) {
+    g_alloc_countdown.store(after < 0 ? -1 : (int64_t)after);
+    return CVX_OK;
+}
+
 int32_t cvx_scene_create(const cvx_triangle* tris, uint32_t n_tris, const cvx_bvh_node* nodes, uint32_t n_nodes,
                          cvx_scene** out) {
     if (!tris || !nodes || !out || n_tris == 0) return set_error(CVX_ERR_INVALID, "null argument or empty scene");
@@ -267,6 +299,9 @@ int32_t cvx_scene_create(const cvx_triangle* tris, uint32_t n_tris, const cvx_bv
     s->n_lights = (uint32_t)ds.size();
     s->depth = depth;
     CK(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking), "cudaStreamCreate");
+    // The no-allocation query's static buffer is reserved here, where
+    // allocating is expected, not at that query's first call.
+    if ((st = noalloc_setup_device())) return st;
     if ((st = dalloc(&s->d_geom, (size_t)n_tris * 3, "triangles"))) return st;
     if ((st = dalloc(&s->d_shade, n_tris, "shading data"))) return st;
     if ((st = dalloc(&s->d_lights, (size_t)s->n_lights * 5, "lights"))) return st;

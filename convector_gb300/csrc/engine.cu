@@ -36,6 +36,8 @@ static int32_t cuda_err(cudaError_t e, const char* what) {
 template <class T>
 static int32_t alloc(T** p, size_t n, std::vector<void*>& owned) {
     *p = nullptr;
+    if (injected_allocation_failure())
+        return set_error(CVX_ERR_CAPACITY, "cudaMalloc for the wave buffers: out of memory (injected)");
     cudaError_t e = cudaMalloc((void**)p, (n ? n : 1) * sizeof(T));
     if (e != cudaSuccess) {
         cudaGetLastError();
@@ -834,10 +836,12 @@ extern "C" int32_t cvx_server_submit(cvx_server* s, const cvx_request* req, uint
     q->host_rgba = rgba;
     q->npx = (uint64_t)req->width * req->height;
     q->groups = groups_of(req->width, req->height);
-    if (q->npx > s->pool_px || (s->mode[req->scene] == 1 && q->groups > s->engine.max_groups()))
-        return set_error(CVX_ERR_CAPACITY, "request larger than the server's framebuffer or ray-queue budget");
     {
+        // The scene's mode is read under the lock: cvx_server_set_scene_mode
+        // writes it under the same lock.
         std::lock_guard<std::mutex> lk(s->mu);
+        if (q->npx > s->pool_px || (s->mode[req->scene] == 1 && q->groups > s->engine.max_groups()))
+            return set_error(CVX_ERR_CAPACITY, "request larger than the server's framebuffer or ray-queue budget");
         q->id = s->next_id++;
         q->res.submit_s = s->now();
         s->pending.push_back(q);

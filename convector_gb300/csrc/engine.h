@@ -15,6 +15,14 @@ cudaStream_t scene_stream(const cvx_scene* s);
 uint32_t scene_depth(const cvx_scene* s);
 uint32_t scene_num_lights(const cvx_scene* s);
 int scene_device(const cvx_scene* s);  // the device the scene was created on
+// Resident blocks per SM of the scene's nearest-hit queries (0: default;
+// cvx_scene_set_query_launch).
+uint32_t scene_query_blocks_per_sm(const cvx_scene* s);
+// Loads the module of cvx_intersect_nearest_noalloc's static scratch array on
+// the current device and caches its address (noalloc.cu); scene creation
+// calls it once per scene, so the no-allocation query loads and allocates
+// nothing itself.
+int32_t noalloc_setup_device();
 // Largest image width and height of a renderer, batch view or server request
 // (an image of 16384 x 16384 is 2^25 groups, so group and path indices of
 // one image stay far inside 32 bits).

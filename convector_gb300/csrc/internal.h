@@ -10,6 +10,11 @@ namespace cvx {
 
 int32_t set_error(int32_t status, const std::string& msg);
 
+// Allocation-failure injection (cvx_inject_allocation_failure): called by the
+// library's device-allocation helpers before each cudaMalloc; true when this
+// allocation is to fail as if the device were out of memory.
+bool injected_allocation_failure();
+
 // A node of the interim tree of the device BVH build (bvh.rs:52-62): its
 // exact bounding box, its triangles order[beg .. beg + cnt) and its children
 // (c0 == 0: a leaf; node 0 is the root and never a child).

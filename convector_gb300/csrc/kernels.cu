@@ -2,6 +2,8 @@
 // Compiled with -fmad=false (see x86sem.cuh).
 #include <cuda_runtime.h>
 
+#include <atomic>
+
 #include "kernels.h"
 #include "path_refill.cuh"
 #include "shade.cuh"
@@ -546,15 +548,34 @@ __global__ void k_resolve(const float* __restrict__ accum, uint32_t npx, float f
 // ---------------------------------------------------------------------------
 // Launchers
 
-static int g_num_sms = 0;
-static int num_sms() {
-    if (!g_num_sms) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev);
-        if (g_num_sms <= 0) g_num_sms = 1;
+// SM count of the calling thread's current device, looked up once per device.
+// Threads may call this concurrently and devices may differ in SM count, so
+// each device has its own atomic slot (a racing first lookup stores the same
+// value twice).
+constexpr int kMaxCachedDevices = 64;
+static std::atomic<int> g_sm_count[kMaxCachedDevices];
+int sm_count() {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) {
+        cudaGetLastError();
+        return 1;
     }
-    return g_num_sms;
+    if (dev >= 0 && dev < kMaxCachedDevices) {
+        const int v = g_sm_count[dev].load(std::memory_order_relaxed);
+        if (v > 0) return v;
+    }
+    int n = 0;
+    if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) {
+        cudaGetLastError();
+        return 1;
+    }
+    if (dev >= 0 && dev < kMaxCachedDevices) g_sm_count[dev].store(n, std::memory_order_relaxed);
+    return n;
+}
+static int num_sms() { return sm_count(); }
+
+cudaError_t set_stack_limit(int entries) {
+    return cudaMemcpyToSymbol(c_stack_limit, &entries, sizeof entries);
 }
 
 cudaError_t upload_tables(const uint16_t* rcp, const uint16_t* rsqrt) {

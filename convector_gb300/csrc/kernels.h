@@ -8,6 +8,12 @@
 
 namespace cvx {
 
+// SM count of the calling thread's current device (cached per device).
+int sm_count();
+// The traversal stack limit (traverse.cuh c_stack_limit) on the current
+// device, for the kernels of kernels.cu and of wavefront.cu.
+cudaError_t set_stack_limit(int entries);
+cudaError_t set_stack_limit_wave(int entries);
 cudaError_t upload_tables(const uint16_t* rcp, const uint16_t* rsqrt);
 cudaError_t upload_tables_wave(const uint16_t* rcp, const uint16_t* rsqrt);
 cudaError_t launch_prep_geom(const cvx_triangle* tris, uint32_t n, float4* geom, TriShade* shade, cudaStream_t st);

@@ -1,7 +1,10 @@
 // cvx_intersect_nearest_noalloc: the nearest-hit query of cvx_intersect_nearest
 // for callers that must not allocate device memory. Every byte it needs beyond
 // the scene and the caller's host buffers lives in one file-scope static
-// device array, reserved when the library is loaded onto a GPU.
+// device array. The array's module is loaded, and its device address looked
+// up, when the first scene is created on a device (cvx_scene_create calls
+// cvx::noalloc_setup_device, and scene creation allocates anyway), so the
+// query itself neither loads a module nor allocates.
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -51,6 +54,18 @@ int32_t scratch_address(unsigned char** out) {
     return CVX_OK;
 }
 
+}  // namespace
+
+// Looks up the scratch array's address on the current device (loading the
+// module that holds it, which reserves the array there) unless that was
+// done before. Called by cvx_scene_create with the scene's device current.
+int32_t cvx::noalloc_setup_device() {
+    unsigned char* p = nullptr;
+    return scratch_address(&p);
+}
+
+namespace {
+
 int32_t fail(cudaError_t e, const char* what) {
     return cvx::set_error(CVX_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
 }
@@ -72,7 +87,7 @@ extern "C" int32_t cvx_intersect_nearest_noalloc(cvx_scene* scene, const float* 
                                                    std::to_string(kNoAllocMaxRays) + " rays per call, got " +
                                                    std::to_string(n));
     unsigned char* base = nullptr;
-    int32_t st = scratch_address(&base);
+    int32_t st = scratch_address(&base);  // set up when the scene was created: a cached lookup
     if (st) return st;
     uint32_t* status = reinterpret_cast<uint32_t*>(base);  // [0] status, [1] ray counter
     float* rays = reinterpret_cast<float*>(base + kHeaderBytes);
@@ -90,8 +105,8 @@ extern "C" int32_t cvx_intersect_nearest_noalloc(cvx_scene* scene, const float* 
                                  stream)) != cudaSuccess)
             return fail(e, "copy rays");
     if ((e = cvx::launch_intersect(cvx::scene_view(scene), cvx::soa_cols(rays, n), n, far_dist,
-                                   traversal == CVX_TRAVERSE_PACKET, t_dev, tri_dev, nullptr, status, 0, 0,
-                                   stream)) != cudaSuccess)
+                                   traversal == CVX_TRAVERSE_PACKET, t_dev, tri_dev, nullptr, status, 0,
+                                   cvx::scene_query_blocks_per_sm(scene), stream)) != cudaSuccess)
         return fail(e, "intersect launch");
     if ((e = cudaMemcpyAsync(t_out, t_dev, (size_t)n * sizeof(float), cudaMemcpyDeviceToHost, stream)) != cudaSuccess)
         return fail(e, "copy distances");

@@ -20,6 +20,14 @@
 
 namespace cvx {
 
+// Stack entries a traversal may hold before it reports kErrStackOverflow:
+// kStackDepth, unless lowered to test that error path
+// (cvx_set_traversal_stack_limit). Every stack array keeps kStackDepth
+// entries, so any limit up to that keeps all accesses in bounds. Each
+// translation unit that traverses has its own copy; set_stack_limit (in
+// kernels.cu and wavefront.cu) writes each.
+static __constant__ int c_stack_limit = kStackDepth;
+
 struct Hit {
     float t, u, v;
     int32_t tri;
@@ -147,7 +155,7 @@ __device__ __forceinline__ bool traverse(const DeviceScene& s, F3 o, F3 d, bool 
         float c1 = b1.mask ? b1.tmin : __int_as_float(0x7f800000);
         const uint32_t r0 = __float_as_uint(q3.x), r1 = __float_as_uint(q3.y);
         int need = (int)hit0 + (int)hit1;
-        if (sp + need > kStackDepth) {
+        if (sp + need > c_stack_limit) {
             ok = false;
             break;
         }
@@ -318,7 +326,7 @@ struct RefillRay {
             bool hit_first = first0 ? hit0 : hit1, hit_second = first0 ? hit1 : hit0;
             uint32_t ref_first = first0 ? r0 : r1, ref_second = first0 ? r1 : r0;
             float t_first = first0 ? b0.tmin : b1.tmin, t_second = first0 ? b1.tmin : b0.tmin;
-            if (sp + (int)hit_first + (int)hit_second > kStackDepth) {
+            if (sp + (int)hit_first + (int)hit_second > c_stack_limit) {
                 overflow = true;
                 sp = 0;
                 cur = kNone;

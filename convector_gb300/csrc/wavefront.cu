@@ -321,15 +321,10 @@ __global__ void __launch_bounds__(128, 8) k_wf_shade(const Job* __restrict__ job
     if ((threadIdx.x & 31u) == 0u && v) atomicAdd(out.rays, v);
 }
 
-static int g_sms_wf = 0;
-static int sms() {
-    if (!g_sms_wf) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&g_sms_wf, cudaDevAttrMultiProcessorCount, dev);
-        if (g_sms_wf <= 0) g_sms_wf = 1;
-    }
-    return g_sms_wf;
+static int sms() { return sm_count(); }
+
+cudaError_t set_stack_limit_wave(int entries) {
+    return cudaMemcpyToSymbol(c_stack_limit, &entries, sizeof entries);
 }
 
 // The fused form over a wave: every octet renders whole groups of any job

@@ -121,6 +121,24 @@ void cvx_camera_set_fov(cvx_camera* cam, float fov);
  * lasting `time_delta` (motion blur over the frame). */
 void cvx_camera_set_interactive(cvx_camera* cam, float time, float time_delta);
 
+/* ---- diagnostics: error paths ------------------------------------------
+ * No counterpart in the reference, which panics where these calls make the
+ * library return a status (bvh.rs:594-600 on a stack overflow, main.rs:65-66
+ * on allocation). They exist so that tests can run the error paths. */
+
+/* Lowers the number of entries a traversal stack may hold (2 .. 128; 0
+ * restores the default of 128) on the calling thread's current device, for
+ * kernels launched after the call returns; call it while no kernel of this
+ * library runs there. A ray that would need more entries stops, the kernel
+ * sets its status word and the call that launched it returns CVX_ERR_DEVICE;
+ * every access stays inside the stacks' full size. */
+int32_t cvx_set_traversal_stack_limit(uint32_t entries);
+/* Makes the library's device allocations fail as if the device were out of
+ * memory (CVX_ERR_CAPACITY): the next `after` allocations succeed and the one
+ * after them fails, once; a negative value cancels a pending failure.
+ * Process-wide, on every device. */
+int32_t cvx_inject_allocation_failure(int32_t after);
+
 /* ---- device: scenes ------------------------------------------------------ */
 
 /* The device that handles created now by the calling thread would belong to:
@@ -184,14 +202,13 @@ int32_t cvx_intersect_nearest_device(cvx_scene* scene, const float* rays, uint32
  * own allocator and forbids plugins to call cudaMalloc, or a real-time loop in
  * which an allocation (which can synchronise the device and take an
  * unpredictable time) would break the frame budget. The scene must already
- * exist; this call allocates nothing. Rays and hits are staged through one
- * static device buffer of 16 MiB + 256 B that the library reserves on every
- * GPU it is loaded on, until the process exits: at most 524,288 rays per call
+ * exist; this call allocates nothing and loads nothing. Rays and hits are
+ * staged through one static device buffer of 16 MiB + 256 B, reserved on a
+ * device (and its address looked up) when the first scene is created there,
+ * and held until the process exits: at most 524,288 rays per call
  * (CVX_ERR_INVALID beyond). Every call shares that buffer: calls that overlap
  * on the GPU (from several threads or scenes at once) race on it and must be
- * serialised by the caller. The first call on each device looks up the
- * buffer's device address; make that first call before any stream capture.
- * No counterpart in the reference. */
+ * serialised by the caller. No counterpart in the reference. */
 int32_t cvx_intersect_nearest_noalloc(cvx_scene* scene, const float* ox, const float* oy, const float* oz,
                                       const float* dx, const float* dy, const float* dz, uint32_t n,
                                       float far_dist, uint32_t traversal, float* t_out, int32_t* tri_out);

@@ -411,6 +411,97 @@ void brute_force(const Scene& s, const Ray& r, Isect& is) {
     for (size_t i = 0; i < s.tris.size(); i++) tri_intersect(s.tris[i], (int32_t)i, r, true, is);
 }
 
+// Why two traversals of one ray can return different nearest hits, both
+// computed with the reference's arithmetic. Result classes:
+//   kSame     equal index and equal t bits;
+//   kTie      equal t bits, different indices, and each triangle tested alone
+//             gives that t: the traversals tested the two in different
+//             orders, and the first tested wins (triangle.rs:127 rejects
+//             t >= dist);
+//   kGrazing  the nearer hit's triangle lies under a box (the leaf holding it
+//             or an ancestor) that the reference's approximate-reciprocal slab
+//             test (aabb.rs:105-141) rejects for this ray at the farther hit's
+//             distance (mask false, exit behind the origin, or entry at or
+//             beyond that distance), while an exact slab test in double
+//             precision finds the ray inside that box at the nearer hit. A
+//             traversal rejects a box only on one of those three conditions,
+//             and its current distance never drops below its final one, so
+//             this is the box the traversal with the farther hit discarded;
+//   kUnclassified anything else (a wrong result), including a result that
+//             is not what its own triangle gives alone.
+enum { kSame = 0, kTie = 1, kGrazing = 2, kUnclassified = 3 };
+
+// Leaf of every triangle and parent of every node (roots 0 and 1 have none).
+struct TreeIndex {
+    std::vector<uint32_t> tri_leaf, parent;
+    explicit TreeIndex(const Scene& s) : tri_leaf(s.tris.size(), UINT32_MAX), parent(s.nodes.size(), UINT32_MAX) {
+        for (uint32_t k = 0; k < s.nodes.size(); k++) {
+            const Node& nd = s.nodes[k];
+            if (nd.len == 0) {
+                parent[nd.index] = k;
+                parent[nd.index + 1] = k;
+            } else {
+                for (uint32_t i = nd.index; i < nd.index + nd.len && i < tri_leaf.size(); i++) tri_leaf[i] = k;
+            }
+        }
+    }
+};
+
+// The ray is inside the box at distance t, by exact division in double
+// precision, within a slack of 1e-5 relative (the hit point's own rounding).
+inline bool exact_box_contains(const Node& n, const Ray& r, double t) {
+    const double o[3] = {r.o.x, r.o.y, r.o.z}, d[3] = {r.d.x, r.d.y, r.d.z};
+    const double eps = 1e-5 * (1.0 + std::fabs(t));
+    double tmin = -INFINITY, tmax = INFINITY;
+    for (int a = 0; a < 3; a++) {
+        if (d[a] == 0.0) {
+            if (o[a] < n.origin[a] - eps || o[a] > n.far_[a] + eps) return false;
+            continue;
+        }
+        double t1 = (n.origin[a] - o[a]) / d[a], t2 = (n.far_[a] - o[a]) / d[a];
+        tmin = std::max(tmin, std::min(t1, t2));
+        tmax = std::min(tmax, std::max(t1, t2));
+    }
+    return tmin <= t + eps && tmax >= t - eps;
+}
+
+inline float tri_alone_t(const Scene& s, int32_t i, const Ray& r, float far_dist) {
+    Isect is;
+    is.dist = far_dist;
+    is.tri = -1;
+    tri_intersect(s.tris[(size_t)i], i, r, true, is);
+    return is.tri == i ? is.dist : NAN;
+}
+
+int classify_pair(const Scene& s, const TreeIndex& ix, const Ray& r, float far_dist, float ta, int32_t ia,
+                  float tb, int32_t ib) {
+    if (ia == ib && fbits(ta) == fbits(tb)) return kSame;
+    const int32_t nt = (int32_t)s.tris.size();
+    if (ia < -1 || ia >= nt || ib < -1 || ib >= nt) return kUnclassified;
+    if (fbits(ta) == fbits(tb)) {
+        if (ia < 0 || ib < 0) return kUnclassified;
+        float a = tri_alone_t(s, ia, r, far_dist), b = tri_alone_t(s, ib, r, far_dist);
+        return fbits(a) == fbits(ta) && fbits(b) == fbits(tb) ? kTie : kUnclassified;
+    }
+    // The nearer hit must be a hit of its triangle alone.
+    const bool a_near = ta < tb;
+    const float t_near = a_near ? ta : tb, t_far = a_near ? tb : ta;
+    const int32_t i_near = a_near ? ia : ib, i_far = a_near ? ib : ia;
+    if (i_near < 0 || i_near == i_far || !(t_near < t_far)) return kUnclassified;
+    // Each result must be what its triangle gives alone (a miss: the far distance).
+    if (fbits(tri_alone_t(s, i_near, r, far_dist)) != fbits(t_near)) return kUnclassified;
+    if (i_far < 0 ? fbits(t_far) != fbits(far_dist) : fbits(tri_alone_t(s, i_far, r, far_dist)) != fbits(t_far))
+        return kUnclassified;
+    V3 inv = v3(rcp(r.d.x), rcp(r.d.y), rcp(r.d.z));
+    for (uint32_t k = ix.tri_leaf[(size_t)i_near]; k != UINT32_MAX; k = ix.parent[k]) {
+        const Node& nd = s.nodes[k];
+        BoxHit b = box_hit(nd, r.o, inv);
+        const bool rejected = !b.mask || sneg(b.tmax) || geq(b.tmin, t_far);
+        if (rejected && exact_box_contains(nd, r, (double)t_near)) return kGrazing;
+    }
+    return kUnclassified;
+}
+
 inline Isect far_isect(const Ray& r, float far_dist) {  // scene.rs:220-230
     Isect is;
     is.pos = vfma(r.d, far_dist, r.o);
@@ -977,6 +1068,24 @@ void orc_scene_free(void* s) { delete (Scene*)s; }
 // order; lanes past n are padded with inactive copies of the first ray.
 // mode 0: packet traversal (the reference); 1: single-ray traversal;
 // 2: brute force over all triangles.
+// Classes (kSame .. kUnclassified) of n rays' two results (ta, ia), (tb, ib).
+void orc_classify(void* sp, const float* ox, const float* oy, const float* oz, const float* dx, const float* dy,
+                  const float* dz, uint32_t n, float far_dist, const float* ta, const int32_t* ia, const float* tb,
+                  const int32_t* ib, uint8_t* cls, int nthreads) {
+    const Scene& s = *(const Scene*)sp;
+    const TreeIndex ix(s);
+    parallel_for(n, nthreads, [&](uint32_t i) {
+        if (ia[i] == ib[i] && fbits(ta[i]) == fbits(tb[i])) {
+            cls[i] = kSame;
+            return;
+        }
+        Ray r;
+        r.o = v3(ox[i], oy[i], oz[i]);
+        r.d = v3(dx[i], dy[i], dz[i]);
+        cls[i] = (uint8_t)classify_pair(s, ix, r, far_dist, ta[i], ia[i], tb[i], ib[i]);
+    });
+}
+
 void orc_intersect(void* sp, const float* ox, const float* oy, const float* oz, const float* dx, const float* dy,
                    const float* dz, uint32_t n, float far_dist, int mode, float* t_out, int32_t* tri_out,
                    float* u_out, float* v_out, uint32_t* numi_aabb, uint32_t* numi_tri, int nthreads) {

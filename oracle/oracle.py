@@ -17,6 +17,8 @@ _L = None
 P, U32, I32, F32, U64 = ctypes.c_void_p, ctypes.c_uint32, ctypes.c_int32, ctypes.c_float, ctypes.c_uint64
 
 RNG_PATCH, RNG_GROUP = 0, 1
+# classes of orc_classify: why two traversals' nearest hits of a ray differ
+SAME, TIE, GRAZING, UNCLASSIFIED = 0, 1, 2, 3
 TRAVERSE_PACKET, TRAVERSE_SINGLE, BRUTE_FORCE = 0, 1, 2
 
 
@@ -29,6 +31,7 @@ def lib():
             "orc_scene_new": (P, [P, U32, P, U32, P, U32, ctypes.c_int]),
             "orc_scene_free": (None, [P]),
             "orc_intersect": (None, [P, P, P, P, P, P, P, U32, F32, ctypes.c_int, P, P, P, P, P, P, ctypes.c_int]),
+            "orc_classify": (None, [P, P, P, P, P, P, P, U32, F32, P, P, P, P, P, ctypes.c_int]),
             "orc_render": (U64, [P, P, U32, U32, U32, ctypes.c_int, ctypes.c_int, P, P, P, P, ctypes.c_int,
                                  ctypes.c_int]),
             "orc_render_patches": (U64, [P, P, U32, U32, U32, ctypes.c_int, U32, P, U32, P, P, P, P,
@@ -104,6 +107,23 @@ class OracleScene:
         if counters:
             return t, tri, na, nt
         return t, tri
+
+    def classify(self, origins, directions, ta, ia, tb, ib, far=1.0e5, nthreads=None):
+        """Per ray, why the results (ta, ia) and (tb, ib) of two traversals
+        differ: SAME, TIE (equal t, the first tested triangle wins), GRAZING
+        (the approximate-reciprocal slab test rejects a box that holds the
+        nearer hit) or UNCLASSIFIED."""
+        o = np.asarray(origins, dtype=np.float32)
+        d = np.asarray(directions, dtype=np.float32)
+        n = o.shape[0]
+        cols = [np.ascontiguousarray(o[:, k]) for k in range(3)] + [np.ascontiguousarray(d[:, k]) for k in range(3)]
+        arrs = [np.ascontiguousarray(ta, dtype=np.float32), np.ascontiguousarray(ia, dtype=np.int32),
+                np.ascontiguousarray(tb, dtype=np.float32), np.ascontiguousarray(ib, dtype=np.int32)]
+        assert all(a.shape == (n,) for a in arrs)
+        cls = np.empty(n, np.uint8)
+        lib().orc_classify(self._h, *[_p(c) for c in cols], n, far, *[_p(a) for a in arrs], _p(cls),
+                           nthreads or default_threads())
+        return cls
 
     def render(self, camera, width, height, frame, rng_order=RNG_GROUP, traversal=TRAVERSE_PACKET, nthreads=None,
                color=True, accum=None, debug=False):

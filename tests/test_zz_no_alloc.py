@@ -47,3 +47,26 @@ def test_noalloc_rejects_more_than_its_buffer_holds(scene, gpu):
     t, tri = scene.intersect_nearest_noalloc(o, d)  # still usable afterwards
     rt, rtri = scene.intersect_nearest(o, d)
     assert (tri == rtri).all()
+
+
+def test_noalloc_leaves_device_memory_unchanged(gpu):
+    """A fresh scene's first no-allocation calls change no device memory.
+
+    The allocating query runs first with the same traversal, so the kernels'
+    first launches (module loads, local-memory reservation), which any query
+    pays once, happen before the measurement; the static buffer was reserved
+    when the scene was created. Free device memory is then read before and
+    after four no-allocation calls."""
+    import torch
+    text, mats = scenes.displaced_icosphere(subdivisions=3)
+    sc = gpu.Scene(gpu.Bvh.from_meshes([gpu.Mesh.parse(text, mats)]))
+    o, d = scenes.random_rays(20000, seed=23)
+    for trav in (0, 1):
+        sc.intersect_nearest(o, d, traversal=trav)
+    torch.cuda.synchronize()
+    free_before = torch.cuda.mem_get_info()[0]
+    for trav in (0, 1):
+        for _ in range(2):
+            sc.intersect_nearest_noalloc(o, d, traversal=trav)
+    torch.cuda.synchronize()
+    assert torch.cuda.mem_get_info()[0] == free_before
