@@ -163,33 +163,39 @@ def cpu_sample_rays_per_s(osc, o, d, target_s=10.0):
 
 def run_reference(args):
     """The reference's CPU path on the host cores: the oracle's C++ restatement
-    of the reference AVX packet traversal (the Rust original cannot be built)."""
+    of the reference AVX packet traversal (the Rust original cannot be built),
+    over the same 4,194,304 rays per step as the GPU arm. The scene's BVH is
+    built by the oracle's own restatement of Bvh::build (identical to the
+    product's build), so this process never loads the product library."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
+    from convector_gb300 import scenes
     from oracle import oracle as orc
-    bvh, o, d = build_c1()
-    osc = orc.OracleScene.from_bvh(bvh)
+    tris, _ = scenes.displaced_icosphere(obj=False)
+    obvh = orc.OracleBvh(tris)
+    osc = orc.OracleScene(obvh.triangles, obvh.nodes)
+    o, d = scenes.random_rays(N_RAYS, seed=7)
     threads = os.cpu_count() or 1
-    sample = 1 << 16
-    for s in range(args.warmup):
-        lo = (s * sample) % (N_RAYS - sample)
-        osc.intersect(o[lo:lo + sample], d[lo:lo + sample], nthreads=threads)
+    for _ in range(args.warmup):
+        osc.intersect(o, d, nthreads=threads)
     times = []
-    for s in range(args.steps):
-        lo = ((args.warmup + s) * sample) % (N_RAYS - sample)
+    for _ in range(args.steps):
         t0 = time.perf_counter()
-        osc.intersect(o[lo:lo + sample], d[lo:lo + sample], nthreads=threads)
+        osc.intersect(o, d, nthreads=threads)
         times.append(time.perf_counter() - t0)
     total = sum(times)
-    value = sample * args.steps / total / 1e6
+    value = N_RAYS * args.steps / total / 1e6
+    import convector_gb300
+    assert convector_gb300._LIB is None, "the reference arm must not load the product library"
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "Mrays/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "sample_rays_per_step": sample, "traversal": "reference 8-ray packets"},
+        "config": {"workload": WORKLOAD, "rays_per_step": N_RAYS, "triangles": int(tris.shape[0]),
+                   "traversal": "reference 8-ray packets", "bvh": "oracle restatement of Bvh::build"},
         "cpu_baseline": {"value": value, "unit": "Mrays/s", "cores": threads, "kind": "port",
-                         "sample": "%d rays per step of the same workload, %d steps" % (sample, args.steps)},
+                         "sample": "all %d rays of the workload per step, %d steps" % (N_RAYS, args.steps)},
         "e2e": {"value": value, "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))

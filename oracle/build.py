@@ -15,7 +15,7 @@ import subprocess
 HERE = os.path.dirname(os.path.abspath(__file__))
 TABLES = os.path.join(os.path.dirname(HERE), "convector_gb300", "csrc")
 LIB = os.path.join(HERE, "liboracle.so")
-SOURCES = ["convector_oracle.cpp", "x86sem.h"]
+SOURCES = ["convector_oracle.cpp", "bvh_oracle.cpp", "x86sem.h"]
 
 
 def build(force=False):
@@ -27,7 +27,8 @@ def build(force=False):
     if platform.machine() in ("x86_64", "AMD64"):
         flags += ["-mfma", "-mavx2"]
     cmd = [os.environ.get("CXX", "g++")] + flags + ["-I", TABLES, "-o", LIB + ".tmp",
-                                                    os.path.join(HERE, "convector_oracle.cpp")]
+                                                    os.path.join(HERE, "convector_oracle.cpp"),
+                                                    os.path.join(HERE, "bvh_oracle.cpp")]
     res = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
     if res.returncode != 0:
         raise RuntimeError("oracle build failed:\n" + res.stdout)

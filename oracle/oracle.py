@@ -32,6 +32,12 @@ def lib():
             "orc_scene_free": (None, [P]),
             "orc_intersect": (None, [P, P, P, P, P, P, P, U32, F32, ctypes.c_int, P, P, P, P, P, P, ctypes.c_int]),
             "orc_classify": (None, [P, P, P, P, P, P, P, U32, F32, P, P, P, P, P, ctypes.c_int]),
+            "orc_bvh_build": (P, [P, U32]),
+            "orc_bvh_num_nodes": (U32, [P]),
+            "orc_bvh_num_triangles": (U32, [P]),
+            "orc_bvh_copy": (None, [P, P, P, P]),
+            "orc_bvh_stats": (None, [P, P, P, P]),
+            "orc_bvh_free": (None, [P]),
             "orc_render": (U64, [P, P, U32, U32, U32, ctypes.c_int, ctypes.c_int, P, P, P, P, ctypes.c_int,
                                  ctypes.c_int]),
             "orc_render_patches": (U64, [P, P, U32, U32, U32, ctypes.c_int, U32, P, U32, P, P, P, P,
@@ -149,6 +155,29 @@ class OracleScene:
         if getattr(self, "_h", None) and _L is not None:
             _L.orc_scene_free(self._h)
             self._h = None
+
+
+class OracleBvh:
+    """Bvh::build (bvh.rs:488-545) restated in bvh_oracle.cpp: nodes (n x 8
+    words), BVH-order triangles (n x 16 words), the source index of each
+    BVH-order triangle, and the build statistics (bvh.rs:570-583) plus depth."""
+
+    def __init__(self, triangles):
+        tris = np.ascontiguousarray(np.asarray(triangles).view(np.uint32).reshape(-1, 16))
+        h = lib().orc_bvh_build(_p(tris), tris.shape[0])
+        if not h:
+            raise ValueError("the BVH root does not split (bvh.rs:512 asserts)")
+        try:
+            nn, nt = lib().orc_bvh_num_nodes(h), lib().orc_bvh_num_triangles(h)
+            self.nodes = np.zeros((nn, 8), np.uint32)
+            self.triangles = np.zeros((nt, 16), np.uint32)
+            self.source_index = np.zeros(nt, np.uint32)
+            lib().orc_bvh_copy(h, _p(self.nodes), _p(self.triangles), _p(self.source_index))
+            a, r, d = ctypes.c_float(), ctypes.c_float(), ctypes.c_uint32()
+            lib().orc_bvh_stats(h, ctypes.byref(a), ctypes.byref(r), ctypes.byref(d))
+            self.avg_tris_per_leaf, self.avg_area_ratio, self.depth = a.value, r.value, d.value
+        finally:
+            lib().orc_bvh_free(h)
 
 
 def resolve(accum, n):

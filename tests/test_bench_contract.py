@@ -31,6 +31,7 @@ def test_reference_arm_json_line(cvx):  # cvx: the library is built
     assert r["impl"] == "reference" and r["steps"] == 3 and r["warmup"] == 3 and r["n_gpus"] == 1
     assert r["value"] > 0 and r["unit"] == "Mrays/s" and r["higher_is_better"] is True
     assert "workload" in r["config"]
+    assert r["config"]["rays_per_step"] == 4194304  # the GPU arm's workload, every step
     cb = r["cpu_baseline"]
     assert cb["kind"] == "port" and cb["cores"] >= 1 and cb["value"] == r["value"] and cb["sample"]
     e = r["e2e"]

@@ -1,4 +1,5 @@
-"""Device BVH build against the host build (bvh.rs:488-545): identical node
+"""Device BVH build against the host build and the oracle's independent
+restatement (bvh.rs:488-545): identical node
 array, triangle order, source indices and statistics, on the procedural
 scenes and on inputs that reach every branch of the build (the uniform split
 of bvh.rs:176-201 for small nodes and as the crowded-bin fallback, ties in
@@ -31,8 +32,13 @@ def _random_tris(n, seed, spread=4.0, size=0.05):
 
 
 def _same(cvx, tris):
+    """Device build == host build == the oracle's independent restatement."""
+    from oracle import oracle as orc
     a = cvx.Bvh.build(tris)
     b = cvx.Bvh.build_device(tris)
+    c = orc.OracleBvh(tris)
+    assert np.array_equal(a.nodes, c.nodes) and np.array_equal(a.source_index, c.source_index)
+    assert (a.depth, np.float32(a.avg_area_ratio).tobytes()) == (c.depth, np.float32(c.avg_area_ratio).tobytes())
     assert a.nodes.shape == b.nodes.shape
     assert np.array_equal(a.nodes, b.nodes)
     assert np.array_equal(a.triangles, b.triangles)

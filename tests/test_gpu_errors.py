@@ -137,7 +137,7 @@ def _fail_each_allocation(gpu, create):
             try:
                 h = create()
             except gpu.CvxError as e:
-                assert e.value.status == CVX_ERR_CAPACITY and "injected" in str(e.value), str(e.value)
+                assert e.status == CVX_ERR_CAPACITY and "injected" in str(e), str(e)
                 failures += 1
                 continue
             gpu.inject_allocation_failure(-1)
