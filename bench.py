@@ -31,6 +31,9 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 N_RAYS = 4194304
+# The frame sections time the oracle's CPU frame path beside the GPU (rank 0,
+# one GPU); --no-cpu-frames leaves it out.
+CPU_BASELINE = True
 METRIC = "Mrays/s (nearest-hit rays per second)"
 WORKLOAD = "ray-cast isolation: displaced icosphere subdiv 6 (81,920 tris, seed 7) in a 10-tri box room, " \
            "4,194,304 rays uniform in the room / on S^2 (seed 7)"
@@ -43,6 +46,79 @@ def _peaks():
         return float(p["hbm_gbs"]), "measured"
     except Exception:
         return 6800.0, "fallback"
+
+
+_L2_PEAK = None
+
+
+def l2_peak():
+    """L2 read bandwidth of this GPU (GB/s), measured once by the package's
+    L2 probe (libconvector_l2probe.so): an L2-resident buffer read with
+    ld.global.cg by a grid filling the GPU, best of 5 launches, at 8, 32 and
+    64 MB; the peak is the largest."""
+    global _L2_PEAK
+    if _L2_PEAK is None:
+        import ctypes
+        from convector_gb300 import _build
+        L = ctypes.CDLL(_build.build_probe())
+        L.cvx_probe_l2_read_gbs.restype = ctypes.c_int32
+        L.cvx_probe_l2_read_gbs.argtypes = [ctypes.c_uint64, ctypes.c_uint32, ctypes.c_uint32,
+                                            ctypes.POINTER(ctypes.c_double)]
+        by_size = {}
+        for mb, passes in ((8, 400), (32, 100), (64, 50)):
+            g = ctypes.c_double()
+            rc = L.cvx_probe_l2_read_gbs(mb << 20, passes, 5, ctypes.byref(g))
+            if rc != 0:
+                raise RuntimeError("L2 probe failed (%d)" % rc)
+            by_size["%d MB" % mb] = g.value
+        _L2_PEAK = {"gbs": max(by_size.values()), "by_buffer_size": by_size,
+                    "how": "ld.global.cg reads of an L2-resident buffer, grid of 8 blocks x 256 threads per SM, "
+                           "best of 5 launches (CUDA events)"}
+    return _L2_PEAK
+
+
+def frame_roofline(work, n_lights, pixels, frame_ms, out_bytes_per_px, traffic_key=None):
+    """Memory roofline of one frame from its counted work (cvx_renderer_count_work):
+    algorithmic bytes = 32 per box tested + 36 per triangle tested (the
+    reference's node and vertex records) + 36 per light for every shading step
+    that evaluates the light PDFs + the frame's output bytes per pixel."""
+    b = 32 * work["boxes"] + 36 * work["triangles"] + 36 * n_lights * work["light_shades"] + \
+        out_bytes_per_px * pixels
+    achieved = b / (frame_ms * 1e-3) / 1e9
+    hbm, hbm_kind = _peaks()
+    l2 = l2_peak()["gbs"]
+    dram = _traffic(traffic_key) if traffic_key else None
+    lts = _traffic(traffic_key + ":lts_bytes") if traffic_key else None
+    return {"algorithmic_bytes": b, "bytes_per_ray": b / max(1, work["rays"]), "achieved_gbs": achieved,
+            "hbm_peak_gbs": hbm, "hbm_peak_kind": hbm_kind, "hbm_frac": achieved / hbm,
+            "l2_peak_gbs": l2, "l2_frac": achieved / l2, "work": work, "traffic": dram, "l2_traffic": lts,
+            "l2_frac_measured": None if lts is None else lts / (frame_ms * 1e-3) / 1e9 / l2,
+            "boxes_per_ray": work["boxes"] / max(1, work["rays"]),
+            "tris_per_ray": work["triangles"] / max(1, work["rays"])}
+
+
+def cpu_frame_baseline(bvh, camera, w, h, frame, accumulate=False, target_s=10.0, max_frames=10):
+    """The reference's frame path on all host cores: the oracle in the
+    reference's patch order (one generator per 32x32 patch, main.rs:174-214,
+    renderer.rs:306-327), x86 arithmetic, 8-ray packet traversal, patches
+    spread over the threads. Frames of the same workload until about
+    target_s."""
+    from oracle import oracle as orc
+    osc = orc.OracleScene.from_bvh(bvh)
+    threads = os.cpu_count() or 1
+    cam = camera.as_array()
+    acc = np.zeros((h, w, 3), np.float32) if accumulate else None
+    dt, frames, rays = 0.0, 0, 0
+    while frames < max_frames and (dt < target_s or frames == 0):
+        t0 = time.perf_counter()
+        rays += osc.render(cam, w, h, frame + frames, rng_order=orc.RNG_PATCH, traversal=orc.TRAVERSE_PACKET,
+                           nthreads=threads, color=False, accum=acc)[3]
+        dt += time.perf_counter() - t0
+        frames += 1
+    return {"value": 1e3 * dt / frames, "unit": "ms per frame", "mrays_per_s": rays / dt / 1e6,
+            "frames": frames, "cores": threads, "kind": "port",
+            "sample": "%d frame(s) of %dx%d, %s, patch order, 8-ray packets, %.1f s" % (
+                frames, w, h, "accumulated" if accumulate else "1 spp", dt)}
 
 
 def _traffic(kernel_key):
@@ -345,6 +421,19 @@ def run_ours(args):
         bytes_launch = algo[trav]["bytes"]
         achieved = bytes_launch / (ms_per_step * 1e-3) / 1e9
         kname = "k_intersect_packet" if trav == 0 else "k_intersect_refill"
+        # The scene is L2-resident: node and triangle fetches are served by
+        # L1 and L2, so the kernel is also set against the measured L2 read
+        # bandwidth, with its algorithmic bytes and with the L2 bytes ncu
+        # counted for one launch (lts__t_bytes.sum, profiles/traffic.json).
+        l2 = _guard(l2_peak)
+        l2_block = None
+        if "gbs" in l2:
+            lts = _traffic(kname + ":lts_bytes")
+            l2_block = {"peak_gbs": l2["gbs"], "peak_by_buffer_size": l2["by_buffer_size"], "peak_how": l2["how"],
+                        "frac_algorithmic": achieved / l2["gbs"], "traffic": lts,
+                        "frac_measured": None if lts is None else lts / (ms_per_step * 1e-3) / 1e9 / l2["gbs"]}
+        else:
+            l2_block = l2
         cpu = None
         if world == 1:
             from oracle import oracle as orc
@@ -366,7 +455,7 @@ def run_ours(args):
                          "peak_kind": peak_kind, "traffic": _traffic(kname),
                          "algorithmic_bytes_per_launch": bytes_launch,
                          "boxes_per_ray": algo[trav]["boxes_per_ray"], "tris_per_ray": algo[trav]["tris_per_ray"],
-                         "kernel": kname},
+                         "kernel": kname, "l2": l2_block},
             "cpu_baseline": cpu,
             "clocks": clocks.summary(),
             "gpu_launches": args.steps * launches_per_step,
@@ -431,10 +520,19 @@ def bench_render(cg):
         out[name] = _frames(r, 10 if order == cg.RNG_PATCH else 30)
     from convector_gb300 import autotune
     best, table = autotune.tune(scene, 1280, 736, use_cache=False)
-    res = _frames(cg.Renderer(scene, 1280, 736, **best), 30)
+    r = cg.Renderer(scene, 1280, 736, **best)
+    res = _frames(r, 30)
     res["config"] = best
     res["candidates_ms"] = {k: round(v, 4) for k, v in table.items()}
     out["autotuned"] = res
+    # Roofline of the single-ray frame (the work of frame 42, counted on the
+    # device; the same for every single-ray kernel form): RGBA and gbuffer out.
+    work = cg.Renderer(scene, 1280, 736, rng_order=cg.RNG_GROUP, traversal=cg.TRAVERSE_SINGLE).count_work(42)
+    out["roofline"] = frame_roofline(work, scene.direct_sample_num(), 1280 * 736, res["frame_ms_p50"], 8,
+                                     "k_render_refill@room")
+    out["roofline"]["frame_ms"] = res["frame_ms_p50"]
+    if CPU_BASELINE:
+        out["cpu_baseline"] = cpu_frame_baseline(bvh, scene.camera, 1280, 736, 42)
     return out
 
 
@@ -464,7 +562,40 @@ def bench_large(cg):
         if name == "autotuned":
             res["config"] = best
         out[name] = res
+    # Roofline of one accumulated sample (frame 42's work): the accumulator is
+    # read and written (24 bytes per pixel).
+    work = cg.Renderer(scene, 1280, 736, rng_order=cg.RNG_GROUP, traversal=cg.TRAVERSE_SINGLE).count_work(42)
+    ms = out["autotuned"]["frame_ms_p50"]
+    out["roofline"] = frame_roofline(work, scene.direct_sample_num(), 1280 * 736, ms, 24, "k_render_refill@tube")
+    out["roofline"]["frame_ms"] = ms
+    if CPU_BASELINE:
+        out["cpu_baseline"] = cpu_frame_baseline(bvh, scene.camera, 1280, 736, 42, accumulate=True, target_s=5.0,
+                                                 max_frames=2)
     return out
+
+
+def bench_frame_kernel(cg, which):
+    """A few frames of one single-ray frame kernel alone (paths per lane, the
+    autotuned form for both scenes), for profiling: `room` renders the
+    1280x736 interactive frame of the room-and-sphere scene, `tube` samples of
+    the 870k-triangle tube accumulated at 1280x736."""
+    from convector_gb300 import scenes
+    if which == "room":
+        bvh = build_c0()
+    else:
+        bvh = cg.Bvh.build(scenes.random_walk_tube(obj=False)[0])
+    scene = cg.Scene(bvh)
+    scenes.default_camera(scene.camera)
+    r = cg.Renderer(scene, 1280, 736, rng_order=cg.RNG_GROUP, traversal=cg.TRAVERSE_SINGLE,
+                    refill_mode=cg.REFILL_ALL)
+    ms = []
+    for f in range(4):
+        if which == "room":
+            r.render_frame_u8(42 + f, gbuffer=False)
+        else:
+            r.accumulate_frame_f32(42 + f)
+        ms.append(r.stats()[1])
+    return {"scene": which, "frame_ms": ms}
 
 
 def _c3_plan(rng, n):
@@ -688,19 +819,24 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-render", action="store_true")
+    ap.add_argument("--no-cpu-frames", action="store_true",
+                    help="leave out the oracle's CPU frame baselines of the render and large sections")
     ap.add_argument("--no-extra", action="store_true", help="skip the large, batched and served sections")
     ap.add_argument("--launch", help="query launch shape (packet8/0, single/8, single/10, single/12) instead of "
                                      "the fastest of a short timed trial")
-    ap.add_argument("--section", choices=["render", "large", "batched", "served", "bvh"],
+    ap.add_argument("--section", choices=["render", "large", "batched", "served", "bvh", "frame-room", "frame-tube"],
                     help="run one extra section alone and print its JSON (no headline line)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
+    global CPU_BASELINE
+    CPU_BASELINE = not args.no_cpu_frames
     if args.section:
         import convector_gb300 as cg
         cg.lib(build=True)
         fn = {"render": bench_render, "large": bench_large, "batched": bench_batched, "served": bench_served,
-              "bvh": bench_bvh_build}
+              "bvh": bench_bvh_build, "frame-room": lambda c: bench_frame_kernel(c, "room"),
+              "frame-tube": lambda c: bench_frame_kernel(c, "tube")}
         print(json.dumps({args.section: fn[args.section](cg)}))
         return
     if args.impl == "reference":

@@ -136,6 +136,7 @@ def lib(build=False):
         "cvx_clear_accumulator": (I32, [P]),
         "cvx_read_frame_f32": (I32, [P, P]),
         "cvx_renderer_stats": (I32, [P, P, P]),
+        "cvx_renderer_count_work": (I32, [P, U32, P]),
         "cvx_batch_create": (I32, [P, U32, U32, ctypes.c_uint64, P, P]),
         "cvx_batch_render": (I32, [P, P, U32, P, P, P]),
         "cvx_batch_destroy": (None, [P]),
@@ -547,6 +548,14 @@ class Renderer:
         rays, ms = ctypes.c_uint64(), ctypes.c_float()
         _check(lib().cvx_renderer_stats(self._h, ctypes.byref(rays), ctypes.byref(ms)))
         return rays.value, ms.value
+
+    def count_work(self, frame):
+        """The work of frame `frame` (cvx_renderer_count_work): rays traced,
+        boxes and triangles they tested, and shading steps that evaluated
+        every light's PDF."""
+        out = (ctypes.c_uint64 * 4)()
+        _check(lib().cvx_renderer_count_work(self._h, frame, out))
+        return {"rays": out[0], "boxes": out[1], "triangles": out[2], "light_shades": out[3]}
 
     def __del__(self):
         if getattr(self, "_h", None) and self._h.value and _LIB is not None:

@@ -17,6 +17,10 @@ CSRC = os.path.join(PKG, "csrc")
 INCLUDE = os.path.join(os.path.dirname(PKG), "include")
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "lib", "libconvector_gpu.so")
+# The L2 read-bandwidth probe (the traversal kernels' L2 roofline), a library
+# of its own: the render path never loads it.
+PROBE_SOURCE = "l2_probe.cu"
+PROBE_LIB = os.path.join(PKG, "lib", "libconvector_l2probe.so")
 
 CU_SOURCES = ["kernels.cu", "wavefront.cu", "engine.cu", "capi.cu", "noalloc.cu", "postprocess.cu", "bvh_build.cu"]
 CPP_SOURCES = ["host_scene.cpp"]
@@ -50,6 +54,18 @@ def _run(cmd):
     return res.stdout
 
 
+def build_probe(force=False):
+    """Compiles libconvector_l2probe.so if its source is newer; returns its path."""
+    src = os.path.join(CSRC, PROBE_SOURCE)
+    if not force and os.path.exists(PROBE_LIB) and os.path.getmtime(PROBE_LIB) >= _newest([src, __file__]):
+        return PROBE_LIB
+    os.makedirs(os.path.dirname(PROBE_LIB), exist_ok=True)
+    tmp = PROBE_LIB + ".tmp"
+    _run([_nvcc()] + NVCC_FLAGS + ["-shared", "-o", tmp, src])
+    os.replace(tmp, PROBE_LIB)
+    return PROBE_LIB
+
+
 def build(force=False, verbose=False, extra_nvcc=()):
     """Compiles the extension if any source is newer than the library; returns its path."""
     sources = [os.path.join(CSRC, s) for s in CU_SOURCES + CPP_SOURCES + HEADERS]
@@ -71,8 +87,10 @@ def build(force=False, verbose=False, extra_nvcc=()):
         obj = os.path.join(BUILD, s + ".o")
         objs.append(obj)
         jobs.append([cxx] + CXX_FLAGS + ["-I", INCLUDE, "-c", os.path.join(CSRC, s), "-o", obj])
-    with concurrent.futures.ThreadPoolExecutor(max_workers=len(jobs)) as ex:
+    with concurrent.futures.ThreadPoolExecutor(max_workers=len(jobs) + 1) as ex:
+        probe = ex.submit(build_probe, force)
         outs = list(ex.map(_run, jobs))
+        probe.result()
     if verbose:
         for o in outs:
             if o.strip():

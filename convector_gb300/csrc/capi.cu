@@ -189,7 +189,9 @@ struct cvx_renderer {
     uint32_t* d_patches = nullptr;  // patch origins of the patch entry points
     uint32_t patch_cap = 0;
     uint32_t* d_group_em = nullptr;  // per 8-pixel group: lanes that hit an emitter at bounce 0
+    unsigned long long* d_work = nullptr;  // cvx_renderer_count_work's counters (allocated at first use)
     ~cvx_renderer() {
+        cudaFree(d_work);
         cudaFree(d_group_em);
         cudaFree(d_patches);
         cudaFree(d_rgba);
@@ -635,6 +637,36 @@ static int32_t run_frame(cvx_renderer* r, uint32_t frame, bool accumulate, uint3
     cudaEventElapsedTime(&r->last_ms, r->e0, r->e1);
     r->last_rays = rays;
     if (err) return set_error(CVX_ERR_DEVICE, "traversal stack overflow reported by the kernel");
+    return CVX_OK;
+}
+
+int32_t cvx_renderer_count_work(cvx_renderer* r, uint32_t frame, uint64_t* out) {
+    if (!r || !out) return set_error(CVX_ERR_INVALID, "null argument");
+    CVX_ON_DEVICE(r->device);
+    if (r->cfg.traversal != CVX_TRAVERSE_SINGLE || r->cfg.rng_order != CVX_RNG_GROUP || r->debug)
+        return set_error(CVX_ERR_INVALID,
+                         "work counts are defined for single-ray frames in the per-group RNG order");
+    int32_t st = 0;
+    if (!r->d_work && (st = dalloc(&r->d_work, 3, "work counters"))) return st;
+    unsigned long long rays = 0, work[3] = {0, 0, 0};
+    uint32_t err = 0;
+    StreamSync sync(r->stream);
+    CK(cudaMemsetAsync(r->d_rays, 0, 8, r->stream), "reset counters");
+    CK(cudaMemsetAsync(r->d_err, 0, 8, r->stream), "reset status");
+    CK(cudaMemsetAsync(r->d_work, 0, 24, r->stream), "reset counters");
+    CK(launch_render(r->scene->view(), r->cam, r->w, r->h, frame, false, false, r->d_rgba, r->d_gbuf, r->d_color,
+                     nullptr, r->d_rays, r->d_err, r->cfg.block_size, false, r->stream, 32, nullptr, 0,
+                     r->d_group_em, r->d_work),
+       "render launch");
+    CK(cudaMemcpyAsync(&rays, r->d_rays, 8, cudaMemcpyDeviceToHost, r->stream), "copy counters");
+    CK(cudaMemcpyAsync(work, r->d_work, 24, cudaMemcpyDeviceToHost, r->stream), "copy counters");
+    CK(cudaMemcpyAsync(&err, r->d_err, 4, cudaMemcpyDeviceToHost, r->stream), "copy status");
+    CK(cudaStreamSynchronize(r->stream), "render");
+    if (err) return set_error(CVX_ERR_DEVICE, "traversal stack overflow reported by the kernel");
+    out[0] = rays;
+    out[1] = work[0];
+    out[2] = work[1];
+    out[3] = work[2];
     return CVX_OK;
 }
 

@@ -308,6 +308,9 @@ struct FrameArgs {
     // per-lane path refill (k_render_refill): one word per 8-pixel group,
     // zero at launch
     uint32_t* group_em;
+    // the counting form of k_render_refill: totals of boxes and triangles
+    // tested and of light-PDF shading steps (3 words, zero at launch)
+    unsigned long long* work;
 };
 
 // Screen x (or y) of lane k of group g of the 16x4 block at (xb, yb), before
@@ -452,6 +455,13 @@ struct FramePaths {
     }
     __device__ __forceinline__ void count_ray(const PathRef&) { rays++; }
     __device__ __forceinline__ void finish(const PathRef&) { flush_rays(a, rays); }
+    __device__ __forceinline__ void work(uint64_t boxes, uint64_t tris, uint64_t shades) {
+        unsigned long long v[3] = {boxes, tris, shades};
+        for (int k = 0; k < 3; k++) {
+            for (int off = 16; off > 0; off >>= 1) v[k] += __shfl_down_sync(0xffffffffu, v[k], off);
+            if ((threadIdx.x & 31u) == 0u && v[k]) atomicAdd(a.work + k, v[k]);
+        }
+    }
 };
 
 // Launch shape and loop form of the per-lane path refill, each measured on the
@@ -463,12 +473,14 @@ struct FramePaths {
 constexpr int kRefillFrameBlocksPerSm = 7;
 constexpr int kRefillFrameSteps = 2;
 
-template <int CLAIM_MIN>
+// COUNT: the same frame, also counting its work (FrameArgs::work); the
+// counters cost registers, so frames are rendered without them.
+template <int CLAIM_MIN, bool COUNT>
 __global__ void __launch_bounds__(128, kRefillFrameBlocksPerSm) k_render_refill(FrameArgs a) {
     __shared__ ApproxTables tab;
     load_tables(tab);
     FramePaths P{a, (a.w + 15u) / 16u, (a.h + 3u) / 4u, 0u};
-    if (!path_refill<CLAIM_MIN, kRefillFrameSteps>(P, tab)) atomicOr(a.err, kErrStackOverflow);
+    if (!path_refill<CLAIM_MIN, kRefillFrameSteps, COUNT>(P, tab)) atomicOr(a.err, kErrStackOverflow);
 }
 
 // After k_render_refill: a group whose 8 lanes all hit an emitter at bounce 0
@@ -651,10 +663,11 @@ cudaError_t launch_intersect(const DeviceScene& s, const RayCols& rays, uint32_t
 cudaError_t launch_render(const DeviceScene& s, const DeviceCamera& cam, uint32_t w, uint32_t h, uint32_t frame,
                           bool packet, bool patch_order, uint32_t* rgba, uint32_t* gbuf, float* color, float* accum,
                           unsigned long long* rays, uint32_t* err, uint32_t block, bool debug, cudaStream_t st,
-                          uint32_t patch, const uint32_t* patches, uint32_t n_patches, uint32_t* group_em) {
+                          uint32_t patch, const uint32_t* patches, uint32_t n_patches, uint32_t* group_em,
+                          unsigned long long* work) {
     if (patch == 0) patch = 32;
     FrameArgs a{s, cam, w, h, frame, rgba, gbuf, color, accum, rays, err, debug ? 1u : 0u, patch, patches, n_patches,
-                group_em};
+                group_em, work};
     if (block == 0) block = 128;
     if (group_em && !packet && !patch_order && !debug) {
         uint32_t ngroups = ((w + 15u) / 16u) * ((h + 3u) / 4u) * 8u;
@@ -662,8 +675,14 @@ cudaError_t launch_render(const DeviceScene& s, const DeviceCamera& cam, uint32_
         if (e != cudaSuccess) return e;
         uint32_t need = (ngroups * 8u + 127u) / 128u, blocks = (uint32_t)num_sms() * kRefillFrameBlocksPerSm;
         if (blocks > need) blocks = need;
-        if (s.depth > 40) k_render_refill<8><<<blocks, 128, 0, st>>>(a);
-        else k_render_refill<16><<<blocks, 128, 0, st>>>(a);
+        if (work) {
+            if (s.depth > 40) k_render_refill<8, true><<<blocks, 128, 0, st>>>(a);
+            else k_render_refill<16, true><<<blocks, 128, 0, st>>>(a);
+        } else if (s.depth > 40) {
+            k_render_refill<8, false><<<blocks, 128, 0, st>>>(a);
+        } else {
+            k_render_refill<16, false><<<blocks, 128, 0, st>>>(a);
+        }
         if (gbuf) {
             uint32_t fb = (ngroups + 255u) / 256u, cap = (uint32_t)num_sms() * 8u;
             k_emitter_groups<<<fb < cap ? fb : cap, 256, 0, st>>>(group_em, ngroups, w, h, gbuf);

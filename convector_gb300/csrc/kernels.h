@@ -57,11 +57,14 @@ inline bool path_refill_wave(uint32_t refill_mode, uint32_t deep_groups, uint32_
 
 // group_em: one word per 8-pixel group; given, a single-ray frame in the
 // per-group RNG order takes the per-lane path refill form (k_render_refill),
-// else one octet per group (k_render_group).
+// else one octet per group (k_render_group). work (3 words, zeroed by the
+// caller; needs group_em): the counting form of k_render_refill adds the
+// frame's boxes tested, triangles tested and light-PDF shading steps.
 cudaError_t launch_render(const DeviceScene& s, const DeviceCamera& cam, uint32_t w, uint32_t h, uint32_t frame,
                           bool packet, bool patch_order, uint32_t* rgba, uint32_t* gbuf, float* color, float* accum,
                           unsigned long long* rays, uint32_t* err, uint32_t block, bool debug, cudaStream_t st, uint32_t patch = 32,
-                          const uint32_t* patches = nullptr, uint32_t n_patches = 0, uint32_t* group_em = nullptr);
+                          const uint32_t* patches = nullptr, uint32_t n_patches = 0, uint32_t* group_em = nullptr,
+                          unsigned long long* work = nullptr);
 cudaError_t launch_resolve(const float* accum, uint32_t npx, float factor, uint32_t* rgba, cudaStream_t st);
 // refill_from: first bounce whose single-ray traversal uses ray refill (the
 // earlier ones traverse one octet per group); packet traversal ignores it.

@@ -33,13 +33,17 @@
 //   void gbuffer(const PathRef&, uint32_t word), void mark_emitter(const PathRef&)
 //   void store(const PathRef&, F3 colour)
 //   void count_ray(const PathRef&), void finish(const PathRef& last)  (finish: whole warp)
+//   COUNT only: void work(uint64_t boxes, uint64_t triangles, uint64_t shades)
+//       (whole warp): this lane's totals of the boxes and triangles its rays
+//       tested (bvh.rs:604-651 counters) and of the shading steps that
+//       evaluated every light's PDF (material.rs:281-320)
 #pragma once
 #include "shade.cuh"
 #include "traverse.cuh"
 
 namespace cvx {
 
-template <int CLAIM_MIN, int STEPS, class Paths>
+template <int CLAIM_MIN, int STEPS, bool COUNT = false, class Paths>
 __device__ __forceinline__ bool path_refill(Paths& P, const ApproxTables& tab) {
     typedef typename Paths::PathRef PathRef;
     const int lane = threadIdx.x & 31;
@@ -61,6 +65,7 @@ __device__ __forceinline__ bool path_refill(Paths& P, const ApproxTables& tab) {
     F3 color = f3(1.0f, 1.0f, 1.0f);
     uint32_t bounce = 0;
     bool tracing = false, has_path = false, done = false, overflow = false;
+    uint64_t work_boxes = 0, work_tris = 0, work_shades = 0;
     for (;;) {
         bool want = !tracing && !done;
         unsigned b = __ballot_sync(0xffffffffu, want);
@@ -68,6 +73,10 @@ __device__ __forceinline__ bool path_refill(Paths& P, const ApproxTables& tab) {
         want = want && b;
         if (want && has_path) {
             // Shade the finished ray of this bounce.
+            if constexpr (COUNT) {
+                work_boxes += ray.na;
+                work_tris += ray.nt;
+            }
             const DeviceScene s = P.scene(ref);
             Isect I = make_isect(s, ray.h, ray.o, ray.d, tab);
             const bool em = (I.mat >> 31) != 0u;
@@ -82,6 +91,7 @@ __device__ __forceinline__ bool path_refill(Paths& P, const ApproxTables& tab) {
                 F3 h;
                 if (bounce == 0u) fr = fresnel_term(n.d, ray.d, h, tab);
             } else if (!ends) {
+                if constexpr (COUNT) work_shades++;
                 F3 cm = path_modulation(s, I, n, ray.d, bounce == 0u, tab, fr);
                 color = f3(color.x * cm.x, color.y * cm.y, color.z * cm.z);
             }
@@ -133,8 +143,9 @@ __device__ __forceinline__ bool path_refill(Paths& P, const ApproxTables& tab) {
         }
         if (__all_sync(0xffffffffu, done)) break;
         for (int st = 0; st < STEPS && tracing; st++)
-            if (ray.step<false, true>(stack, overflow)) tracing = false;
+            if (ray.step<COUNT, true>(stack, overflow)) tracing = false;
     }
+    if constexpr (COUNT) P.work(work_boxes, work_tris, work_shades);
     P.finish(ref);
     return !overflow;
 }

@@ -302,6 +302,17 @@ int32_t cvx_read_frame_f32(cvx_renderer* r, float* out);
 /* Rays traced by the last frame (camera plus bounce rays, active lanes only)
  * and its device time. */
 int32_t cvx_renderer_stats(cvx_renderer* r, uint64_t* rays, float* ms);
+/* The work of one frame, for the memory roofline of the frame kernels:
+ * renders frame_number as cvx_render_frame_u8 does (the image stays on the
+ * device) with the per-lane path refill kernel in a counting form, and writes
+ * out[0] the rays traced (camera and bounce rays), out[1] the boxes and
+ * out[2] the triangles they tested (two boxes per internal node visited, the
+ * reference's counters of bvh.rs:604-651), out[3] the shading steps that
+ * evaluated every light's PDF (material.rs:281-320). A ray's counts do not
+ * depend on which kernel traces it, so they hold for every single-ray form
+ * of the frame. Single-ray traversal and per-group RNG order only
+ * (CVX_ERR_INVALID otherwise). No counterpart in the reference. */
+int32_t cvx_renderer_count_work(cvx_renderer* r, uint32_t frame_number, uint64_t* out);
 
 /* ---- device: batched rendering -----------------------------------------
  * Many images of many resident scenes in shared wavefronts: sample s of

@@ -150,6 +150,9 @@ struct Scene {
     std::vector<Node> nodes;
     std::vector<uint32_t> ds;  // direct-sample triangle indices (scene.rs:108-110)
     bool general_pick = true;
+    // Boxes and triangles tested by the single-ray traversals of the last
+    // orc_render (the reference's counters, bvh.rs:604-651), all threads.
+    mutable std::atomic<uint64_t> work_boxes{0}, work_tris{0};
 };
 
 struct Ray {
@@ -733,8 +736,16 @@ struct NearestFn {
         if (!single) {
             packet_traverse(*s, r, active, is, nullptr, nullptr);
         } else {
-            for (int j = 0; j < 8; j++)
-                if (active[j]) single_traverse(*s, r[j], is[j], nullptr, nullptr);
+            uint64_t boxes = 0, tris = 0;
+            for (int j = 0; j < 8; j++) {
+                if (!active[j]) continue;
+                uint32_t a = 0, b = 0;
+                single_traverse(*s, r[j], is[j], &a, &b);
+                boxes += a;
+                tris += b;
+            }
+            s->work_boxes += boxes;
+            s->work_tris += tris;
         }
     }
 };
@@ -1182,7 +1193,16 @@ uint64_t orc_render(void* sp, const float* cam, uint32_t w, uint32_t h, uint32_t
     f.color = color;
     f.accum = accum;
     f.debug = debug != 0;
+    f.s->work_boxes = 0;
+    f.s->work_tris = 0;
     return render_frame(f, rng_order, nthreads);
+}
+
+// Boxes and triangles the single-ray traversals of the last orc_render tested.
+void orc_scene_work(void* sp, uint64_t* out) {
+    const Scene& s = *(const Scene*)sp;
+    out[0] = s.work_boxes;
+    out[1] = s.work_tris;
 }
 
 void* orc_display_new(uint32_t w, uint32_t h, const uint8_t* t1, const uint8_t* t2, uint32_t tw, uint32_t th) {

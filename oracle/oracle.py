@@ -32,6 +32,7 @@ def lib():
             "orc_scene_free": (None, [P]),
             "orc_intersect": (None, [P, P, P, P, P, P, P, U32, F32, ctypes.c_int, P, P, P, P, P, P, ctypes.c_int]),
             "orc_classify": (None, [P, P, P, P, P, P, P, U32, F32, P, P, P, P, P, ctypes.c_int]),
+            "orc_scene_work": (None, [P, P]),
             "orc_bvh_build": (P, [P, U32]),
             "orc_bvh_num_nodes": (U32, [P]),
             "orc_bvh_num_triangles": (U32, [P]),
@@ -140,6 +141,12 @@ class OracleScene:
         rays = lib().orc_render(self._h, _p(cam), width, height, frame, rng_order, traversal, _p(rgba), _p(gbuf),
                                 _p(col), _p(accum), nthreads or default_threads(), int(debug))
         return rgba, gbuf, col, rays
+
+    def last_render_work(self):
+        """(boxes, triangles) the single-ray traversals of the last render tested."""
+        out = np.zeros(2, np.uint64)
+        lib().orc_scene_work(self._h, _p(out))
+        return int(out[0]), int(out[1])
 
     def render_patches(self, camera, width, height, frame, patch_width, origins, traversal=TRAVERSE_PACKET,
                        rgba=None, gbuf=None, accum=None, nthreads=None):
