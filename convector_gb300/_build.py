@@ -60,7 +60,7 @@ def build_probe(force=False):
     if not force and os.path.exists(PROBE_LIB) and os.path.getmtime(PROBE_LIB) >= _newest([src, __file__]):
         return PROBE_LIB
     os.makedirs(os.path.dirname(PROBE_LIB), exist_ok=True)
-    tmp = PROBE_LIB + ".tmp"
+    tmp = "%s.%d.tmp" % (PROBE_LIB, os.getpid())  # concurrent builds must not share it
     _run([_nvcc()] + NVCC_FLAGS + ["-shared", "-o", tmp, src])
     os.replace(tmp, PROBE_LIB)
     return PROBE_LIB
@@ -95,7 +95,7 @@ def build(force=False, verbose=False, extra_nvcc=()):
         for o in outs:
             if o.strip():
                 print(o)
-    tmp = LIB + ".tmp"
+    tmp = "%s.%d.tmp" % (LIB, os.getpid())
     _run([nvcc, "-shared", "-gencode", "arch=compute_103a,code=sm_103a", "-o", tmp] + objs
          + ["-lpthread", "-ldl", "-lrt"])
     os.replace(tmp, LIB)
