@@ -317,28 +317,16 @@ def run_ours(args):
     def step(trav):
         scene.intersect_nearest_device(rays, t_out, tri_out, traversal=trav, stream=stream)
 
-    # Pick the faster traversal variant and launch shape on a short untimed trial.
-    trial = {}
-    shapes = ((0, 0), (1, 8), (1, 10), (1, 12))
-    if args.launch:  # a fixed shape (reproducible profiles): no trial
-        shapes = tuple(x for x in shapes if "%s/%d" % ("packet8" if x[0] == 0 else "single", x[1]) == args.launch)
-        if not shapes:
-            raise SystemExit("--launch: one of packet8/0, single/8, single/10, single/12")
-    for trav, bps in shapes:
-        scene.set_query_launch(bps)
-        for _ in range(2):
-            step(trav)
-        torch.cuda.synchronize()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record()
-        for _ in range(3):
-            step(trav)
-        e1.record()
-        torch.cuda.synchronize()
-        trial["%s/%d" % ("packet8" if trav == 0 else "single", bps)] = e0.elapsed_time(e1) / 3
-    best = min(trial, key=trial.get)
-    trav = 0 if best.startswith("packet8") else 1
-    scene.set_query_launch(int(best.split("/")[1]))
+    # Pick the traversal variant, launch shape and stack depth on a short
+    # untimed trial (the query autotuner).
+    from convector_gb300 import autotune
+    shapes = None
+    if args.launch:  # a fixed configuration (reproducible profiles): no trial
+        shapes = [args.launch]
+        if not any(q[0] == args.launch for q in autotune.QUERY_SHAPES):
+            raise SystemExit("--launch: one of " + ", ".join(q[0] for q in autotune.QUERY_SHAPES))
+    best, trial = autotune.tune_query(scene, rays, t_out, tri_out, shapes=shapes)
+    trav = autotune.query_traversal(best)
     # Kernels per step: the single-ray query on a scene whose node bounds are
     # finite, ordered and free of -0 runs the select-form kernel and the pass
     # over the rays it deferred (the library's check at scene creation).
@@ -858,8 +846,8 @@ def main():
     ap.add_argument("--no-cpu-frames", action="store_true",
                     help="leave out the oracle's CPU frame baselines of the render and large sections")
     ap.add_argument("--no-extra", action="store_true", help="skip the large, batched and served sections")
-    ap.add_argument("--launch", help="query launch shape (packet8/0, single/8, single/10, single/12) instead of "
-                                     "the fastest of a short timed trial")
+    ap.add_argument("--launch", help="query configuration (packet8/0, single/8, single/8/s0, single/8/s4, "
+                                     "single/8/s12, single/10, single/12) instead of the fastest of a short trial")
     ap.add_argument("--section", choices=["render", "large", "batched", "served", "bvh", "frame-room", "frame-tube"],
                     help="run one extra section alone and print its JSON (no headline line)")
     args = ap.parse_args()

@@ -119,6 +119,7 @@ def lib(build=False):
         "cvx_scene_num_direct_samples": (U32, [P]),
         "cvx_scene_set_light_pick": (I32, [P, U32]),
         "cvx_scene_set_query_launch": (I32, [P, U32]),
+        "cvx_scene_set_query_stack": (I32, [P, U32]),
         "cvx_scene_set_host_access": (I32, [P, U32, P]),
         "cvx_scene_destroy": (None, [P]),
         "cvx_intersect_nearest": (I32, [P, P, P, P, P, P, P, U32, F32, U32, P, P]),
@@ -412,6 +413,11 @@ class Scene:
     def set_query_launch(self, blocks_per_sm):
         """Resident blocks per SM of the nearest-hit kernel (0: default)."""
         _check(lib().cvx_scene_set_query_launch(self._h, blocks_per_sm))
+
+    def set_query_stack(self, shared_entries):
+        """Stack entries per lane the single-ray query keeps in shared memory
+        (0, 4, 8 or 12; default 8)."""
+        _check(lib().cvx_scene_set_query_stack(self._h, shared_entries))
 
     def set_host_access(self, mode):
         """How intersect_nearest brings host rays to the device: HOST_ACCESS_AUTO

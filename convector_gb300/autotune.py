@@ -1,14 +1,18 @@
 """Autotuner for the render path: times candidate kernel organisations on the
 actual scene and frame size and keeps the fastest.
 
-Candidates (all give the same image for a given RNG order and traversal; the
-single-ray and packet traversals can differ only on t-ties and grazing rays):
-the fused megakernel at several block sizes with one octet per 8-pixel group,
-the fused megakernel with paths per lane and ray refill, and the wavefront form with
-CUDA-graph replay at several persistent grid sizes and ray-refill modes, each
-with the single-ray and the 8-ray packet traversal. The traversal stack holds
-128 entries; a scene needs BVH depth + 2 (checked at scene creation), so stack
-depth is not a tuning knob: untouched entries cost nothing.
+Frames (tune): candidates (all give the same image for a given RNG order and
+traversal; the single-ray and packet traversals can differ only on t-ties and
+grazing rays): the fused megakernel at several block sizes with one octet per
+8-pixel group, the fused megakernel with paths per lane and ray refill, and the
+wavefront form with CUDA-graph replay at several persistent grid sizes and
+ray-refill modes, each with the single-ray and the 8-ray packet traversal.
+
+Nearest-hit queries (tune_query): the packet traversal and the single-ray
+kernel at 8, 10 and 12 resident blocks per SM and, at 8 blocks, with 0, 4, 8
+or 12 of each lane's stack entries in shared memory (the stack depth knob: the
+rest of the 128-entry stack is local memory, and shared entries take shared
+memory from L1, so the best depth depends on the tree).
 
 Results are cached per (GPU model, library build, scene size, BVH depth, frame
 size, RNG order) in a JSON file (CONVECTOR_AUTOTUNE_CACHE, default
@@ -123,3 +127,46 @@ def tune_wavefront(scene, width, height, frames=5):
 def autotuned_renderer(scene, width, height, rng_order=RNG_GROUP, allow_packet=True):
     best, _ = tune(scene, width, height, rng_order=rng_order, allow_packet=allow_packet)
     return Renderer(scene, width, height, **best)
+
+
+# (name, traversal, blocks per SM, shared stack entries) of the query candidates
+QUERY_SHAPES = [("packet8/0", TRAVERSE_PACKET, 0, 8)] + [
+    ("single/%d%s" % (bps, "" if st == 8 else "/s%d" % st), TRAVERSE_SINGLE, bps, st)
+    for bps, st in ((8, 8), (8, 0), (8, 4), (8, 12), (10, 8), (12, 8))]
+
+
+def tune_query(scene, rays_soa, t_out, tri_out, shapes=None, repeats=3):
+    """Times the nearest-hit query configurations (QUERY_SHAPES, or the named
+    subset `shapes`) on these device rays (a (6, n) float32 CUDA tensor; t_out
+    and tri_out its output tensors) on the current CUDA stream, leaves the
+    scene set to the fastest and returns (its name, {name: ms per query})."""
+    import torch
+    stream = torch.cuda.current_stream()
+    table = {}
+    for name, trav, bps, stack in QUERY_SHAPES:
+        if shapes is not None and name not in shapes:
+            continue
+        scene.set_query_launch(bps)
+        scene.set_query_stack(stack)
+        for _ in range(2):
+            scene.intersect_nearest_device(rays_soa, t_out, tri_out, traversal=trav, stream=stream.cuda_stream)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(repeats):
+            scene.intersect_nearest_device(rays_soa, t_out, tri_out, traversal=trav, stream=stream.cuda_stream)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        table[name] = e0.elapsed_time(e1) / repeats
+    if not table:
+        raise ValueError("no query configuration named %s" % (shapes,))
+    best = min(table, key=table.get)
+    _, trav, bps, stack = next(q for q in QUERY_SHAPES if q[0] == best)
+    scene.set_query_launch(bps)
+    scene.set_query_stack(stack)
+    return best, table
+
+
+def query_traversal(name):
+    """The traversal (TRAVERSE_*) of a QUERY_SHAPES name."""
+    return next(q[1] for q in QUERY_SHAPES if q[0] == name)

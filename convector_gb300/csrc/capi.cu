@@ -110,6 +110,7 @@ struct cvx_scene {
     uint32_t n_nodes = 0, n_tris = 0, n_lights = 0, depth = 0;
     uint32_t general_pick = 1;
     uint32_t blocks_per_sm = 0;  // launch shape of the nearest-hit query (0: default)
+    uint32_t query_stack = 8;    // stack entries per lane in shared memory (cvx_scene_set_query_stack)
     // The device reads host memory through the host's page tables (address
     // translation over a coherent CPU-GPU link): the host-buffer query may
     // read the caller's ray arrays in place. host_access: CVX_HOST_ACCESS_*.
@@ -166,6 +167,7 @@ uint32_t cvx::scene_depth(const cvx_scene* s) { return s->depth; }
 uint32_t cvx::scene_num_lights(const cvx_scene* s) { return s->n_lights; }
 int cvx::scene_device(const cvx_scene* s) { return s->device; }
 uint32_t cvx::scene_query_blocks_per_sm(const cvx_scene* s) { return s->blocks_per_sm; }
+uint32_t cvx::scene_query_stack(const cvx_scene* s) { return s->query_stack; }
 
 struct cvx_renderer {
     std::unique_ptr<WaveEngine> engine;  // wavefront mode
@@ -397,6 +399,13 @@ int32_t cvx_scene_set_host_access(cvx_scene* s, uint32_t mode, uint32_t* in_plac
     return CVX_OK;
 }
 
+int32_t cvx_scene_set_query_stack(cvx_scene* s, uint32_t shared_entries) {
+    if (!s || (shared_entries != 0 && shared_entries != 4 && shared_entries != 8 && shared_entries != 12))
+        return set_error(CVX_ERR_INVALID, "shared stack entries must be 0, 4, 8 or 12");
+    s->query_stack = shared_entries;
+    return CVX_OK;
+}
+
 int32_t cvx_scene_set_query_launch(cvx_scene* s, uint32_t blocks_per_sm) {
     if (!s || blocks_per_sm > 32) return set_error(CVX_ERR_INVALID, "bad launch shape");
     s->blocks_per_sm = blocks_per_sm;
@@ -418,7 +427,7 @@ int32_t cvx_intersect_nearest_device(cvx_scene* s, const float* rays, uint32_t n
     CVX_ON_DEVICE(s->device);
     cudaStream_t st = (cudaStream_t)stream;
     CK(launch_intersect(s->view(), soa_cols(rays, n), n, far_dist, traversal == CVX_TRAVERSE_PACKET, t_out, tri_out,
-                        counters, s->d_err, 0, s->blocks_per_sm, st),
+                        counters, s->d_err, 0, s->blocks_per_sm, st, s->query_stack),
        "intersect launch");
     return CVX_OK;
 }
@@ -491,7 +500,7 @@ int32_t cvx_intersect_nearest(cvx_scene* s, const float* ox, const float* oy, co
         }
         CK(cudaMemsetAsync(s->d_qerr + 2 * c, 0, 8, q), "reset status");
         CK(launch_intersect(s->view(), cols, len, far_dist, traversal == CVX_TRAVERSE_PACKET, s->d_t + off,
-                            s->d_tri + off, nullptr, s->d_qerr + 2 * c, 0, s->blocks_per_sm, q),
+                            s->d_tri + off, nullptr, s->d_qerr + 2 * c, 0, s->blocks_per_sm, q, s->query_stack),
            "intersect launch");
         CK(cudaMemcpyAsync(t_out + off, s->d_t + off, (size_t)len * 4, cudaMemcpyDeviceToHost, q), "copy distances");
         CK(cudaMemcpyAsync(tri_out + off, s->d_tri + off, (size_t)len * 4, cudaMemcpyDeviceToHost, q),

@@ -18,6 +18,9 @@ int scene_device(const cvx_scene* s);  // the device the scene was created on
 // Resident blocks per SM of the scene's nearest-hit queries (0: default;
 // cvx_scene_set_query_launch).
 uint32_t scene_query_blocks_per_sm(const cvx_scene* s);
+// Stack entries per lane the nearest-hit query keeps in shared memory
+// (cvx_scene_set_query_stack).
+uint32_t scene_query_stack(const cvx_scene* s);
 // Loads the module of cvx_intersect_nearest_noalloc's static scratch array on
 // the current device and caches its address (noalloc.cu); scene creation
 // calls it once per scene, so the no-allocation query loads and allocates

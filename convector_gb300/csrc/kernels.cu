@@ -228,22 +228,25 @@ struct StagedSoaClaim {
 // shared, 0.890 with 4, 0.878 with 8, 0.883 with 12. (The wavefront and the
 // path-refill traversals, whose larger working sets need the L1 that the
 // carve-out takes, measured no gain or a loss.)
+// The default; a scene may choose 0, 4 or 12 instead (cvx_scene_set_query_stack,
+// which the query autotuner sets per scene).
 constexpr int kQueryStackShared = 8;
 
 // SELECT: the select-form slab test for the rays that meet its conditions
 // (on scenes that do); the others are marked kDeferredRay and traced by
 // k_intersect_deferred. Measured on 4M rays: 0.844 against 0.877 ms.
-template <int MINB, bool COUNT, int CLAIM, bool SELECT>
+// SHARED: stack entries of each lane in shared memory (the rest in local).
+template <int MINB, bool COUNT, int CLAIM, bool SELECT, int SHARED = kQueryStackShared>
 __global__ void __launch_bounds__(128, MINB) k_intersect_refill(SoaRays src, uint32_t* __restrict__ next_ray,
                                                                 uint32_t* __restrict__ err) {
     // The reciprocal table is read three times per ray: from global memory
     // (L1-resident), which leaves the shared-memory carve-out to L1.
     __shared__ float stage[4][2][6][32];
-    __shared__ uint2 sstack[4][kQueryStackShared][32];
+    __shared__ uint2 sstack[4][SHARED > 0 ? SHARED : 1][32];
     StagedSoaClaim claim{src, next_ray, stage[threadIdx.x >> 5], 0u, 0u, 0u, 0};
     claim.init(threadIdx.x & 31);
-    bool ok = traverse_refill<COUNT, false, CLAIM, kQueryStackShared, SELECT>(
-        src, claim, g_tables, &sstack[threadIdx.x >> 5][0][threadIdx.x & 31]);
+    bool ok = traverse_refill<COUNT, false, CLAIM, SHARED, SELECT>(src, claim, g_tables,
+                                                                   &sstack[threadIdx.x >> 5][0][threadIdx.x & 31]);
     if (!ok) atomicOr(err, kErrStackOverflow);
 }
 
@@ -616,9 +619,22 @@ cudaError_t launch_prep_lights(const cvx_triangle* tris, const uint32_t* ds, uin
     return cudaGetLastError();
 }
 
+// The select-form query with CLAIM at 8 blocks per SM and `shared` stack
+// entries in shared memory (0, 4, 8 or 12).
+template <int CLAIM>
+static void launch_select_stack(uint32_t shared, uint32_t blocks, const SoaRays& src, uint32_t* err,
+                                cudaStream_t st) {
+    switch (shared) {
+        case 0: k_intersect_refill<8, false, CLAIM, true, 0><<<blocks, 128, 0, st>>>(src, err + 1, err); break;
+        case 4: k_intersect_refill<8, false, CLAIM, true, 4><<<blocks, 128, 0, st>>>(src, err + 1, err); break;
+        case 12: k_intersect_refill<8, false, CLAIM, true, 12><<<blocks, 128, 0, st>>>(src, err + 1, err); break;
+        default: k_intersect_refill<8, false, CLAIM, true, 8><<<blocks, 128, 0, st>>>(src, err + 1, err); break;
+    }
+}
+
 cudaError_t launch_intersect(const DeviceScene& s, const RayCols& rays, uint32_t n, float far_dist, bool packet,
                              float* t_out, int32_t* tri_out, uint32_t* counters, uint32_t* err, uint32_t block,
-                             uint32_t blocks_per_sm, cudaStream_t st) {
+                             uint32_t blocks_per_sm, cudaStream_t st, uint32_t shared_stack) {
     if (!packet) {
         // persistent ray-refill kernel; err[1] is its ray counter
         cudaError_t e = cudaMemsetAsync(err + 1, 0, 4, st);
@@ -637,11 +653,11 @@ cudaError_t launch_intersect(const DeviceScene& s, const RayCols& rays, uint32_t
         } else if (deep) {
             if (bps >= 12) k_intersect_refill<12, false, 8, true><<<blocks, 128, 0, st>>>(src, err + 1, err);
             else if (bps >= 10) k_intersect_refill<10, false, 8, true><<<blocks, 128, 0, st>>>(src, err + 1, err);
-            else k_intersect_refill<8, false, 8, true><<<blocks, 128, 0, st>>>(src, err + 1, err);
+            else launch_select_stack<8>(shared_stack, blocks, src, err, st);
         } else {
             if (bps >= 12) k_intersect_refill<12, false, 16, true><<<blocks, 128, 0, st>>>(src, err + 1, err);
             else if (bps >= 10) k_intersect_refill<10, false, 16, true><<<blocks, 128, 0, st>>>(src, err + 1, err);
-            else k_intersect_refill<8, false, 16, true><<<blocks, 128, 0, st>>>(src, err + 1, err);
+            else launch_select_stack<16>(shared_stack, blocks, src, err, st);
         }
         if (sel) {
             const uint32_t per_block = 256u * kDeferredScan;

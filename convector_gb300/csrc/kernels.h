@@ -31,9 +31,12 @@ inline RayCols soa_cols(const float* rays, uint32_t n) {  // one (6, n) device a
     return r;
 }
 
+// shared_stack: stack entries of each lane kept in shared memory by the
+// select-form single-ray kernel at 8 blocks per SM (0, 4, 8 or 12; other
+// launch shapes keep 8).
 cudaError_t launch_intersect(const DeviceScene& s, const RayCols& rays, uint32_t n, float far_dist, bool packet,
                              float* t_out, int32_t* tri_out, uint32_t* counters, uint32_t* err, uint32_t block,
-                             uint32_t blocks_per_sm, cudaStream_t st);
+                             uint32_t blocks_per_sm, cudaStream_t st, uint32_t shared_stack = 8);
 // Single-launch form of single-ray frames and waves in the per-group RNG
 // order: paths per lane with ray refill (k_render_refill, k_wave_refill), or
 // one octet per 8-pixel group (k_render_group, k_wave_fused). CVX_REFILL_ALL

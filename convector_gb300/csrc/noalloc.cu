@@ -106,7 +106,8 @@ extern "C" int32_t cvx_intersect_nearest_noalloc(cvx_scene* scene, const float* 
             return fail(e, "copy rays");
     if ((e = cvx::launch_intersect(cvx::scene_view(scene), cvx::soa_cols(rays, n), n, far_dist,
                                    traversal == CVX_TRAVERSE_PACKET, t_dev, tri_dev, nullptr, status, 0,
-                                   cvx::scene_query_blocks_per_sm(scene), stream)) != cudaSuccess)
+                                   cvx::scene_query_blocks_per_sm(scene), stream, cvx::scene_query_stack(scene))) !=
+        cudaSuccess)
         return fail(e, "intersect launch");
     if ((e = cudaMemcpyAsync(t_out, t_dev, (size_t)n * sizeof(float), cudaMemcpyDeviceToHost, stream)) != cudaSuccess)
         return fail(e, "copy distances");

@@ -161,6 +161,14 @@ int32_t cvx_scene_set_light_pick(cvx_scene* scene, uint32_t light_pick);
  * blocks per SM (0: default 8; the single-ray kernel is built for 8, 10 and
  * 12, trading registers for occupancy). Results do not depend on it. */
 int32_t cvx_scene_set_query_launch(cvx_scene* scene, uint32_t blocks_per_sm);
+/* Stack depth of this scene's single-ray nearest-hit queries at the default
+ * launch shape: how many of each lane's traversal stack entries are kept in
+ * shared memory (0, 4, 8 or 12; default 8), the deeper ones in local memory.
+ * Shared entries never miss a cache, but take shared memory from L1; the
+ * best depth depends on the tree (convector_gb300.autotune.tune_query times
+ * them). Results do not depend on it. No counterpart in the reference, whose
+ * stack is a Vec (bvh.rs:594-600). */
+int32_t cvx_scene_set_query_stack(cvx_scene* scene, uint32_t shared_entries);
 /* How cvx_intersect_nearest brings the caller's host ray arrays to the device.
  * AUTO (default): where the device translates addresses through the host's
  * page tables (a coherent CPU-GPU link, as on Grace systems; pinned or pageable

@@ -214,6 +214,45 @@ def test_intersect_single_launch_shapes_bitexact(icosphere, orc, launch):
     assert (t.view(np.uint32) == ot.view(np.uint32)).all()
 
 
+@pytest.mark.parametrize("stack", [0, 4, 12])
+def test_intersect_single_stack_depths_bitexact(icosphere, orc, stack):
+    """Every shared-memory stack depth of the single-ray query (the query
+    autotuner's stack knob) returns the oracle's results."""
+    bvh, scene, osc = icosphere
+    o, d = scenes.random_rays((1 << 17) + 45, seed=23)
+    ot, otri = osc.intersect(o, d, mode=1)
+    scene.set_query_stack(stack)
+    try:
+        t, tri = scene.intersect_nearest(o, d, traversal=1)
+    finally:
+        scene.set_query_stack(8)
+    assert (tri == otri).all(), np.nonzero(tri != otri)[0][:10]
+    assert (t.view(np.uint32) == ot.view(np.uint32)).all()
+
+
+def test_query_autotuner_picks_and_keeps_a_configuration(icosphere, gpu):
+    import torch
+    from convector_gb300 import autotune
+    bvh, scene, osc = icosphere
+    o, d = scenes.random_rays(1 << 18, seed=29)
+    rays = torch.from_numpy(np.concatenate([o.T, d.T]).copy()).cuda()
+    t = torch.empty(o.shape[0], dtype=torch.float32, device="cuda")
+    tri = torch.empty(o.shape[0], dtype=torch.int32, device="cuda")
+    try:
+        best, table = autotune.tune_query(scene, rays, t, tri)
+        assert set(table) == {q[0] for q in autotune.QUERY_SHAPES} and best in table
+        assert all(ms > 0 for ms in table.values())
+        ref_t, ref_tri = scene.intersect_nearest(o, d, traversal=autotune.query_traversal(best))
+        scene.intersect_nearest_device(rays, t, tri, traversal=autotune.query_traversal(best))
+        torch.cuda.synchronize()
+        assert (tri.cpu().numpy() == ref_tri).all()
+        with pytest.raises(gpu.CvxError):
+            scene.set_query_stack(6)
+    finally:
+        scene.set_query_launch(0)
+        scene.set_query_stack(8)
+
+
 def test_intersect_deep_tree_bitexact(gpu, orc):
     """A 70-level tree (the 870k-triangle tube) takes the deep-tree launch of
     the single-ray query; results equal the oracle's on rays from the camera
