@@ -489,7 +489,7 @@ __global__ void __launch_bounds__(128, kRefillFrameBlocksPerSm) k_render_refill(
     __shared__ ApproxTables tab;
     load_tables(tab);
     FramePaths P{a, (a.w + 15u) / 16u, (a.h + 3u) / 4u, 0u};
-    if (!path_refill<CLAIM_MIN, kRefillFrameSteps, COUNT>(P, tab)) atomicOr(a.err, kErrStackOverflow);
+    if (!path_refill<CLAIM_MIN, kRefillFrameSteps, COUNT, true>(P, tab)) atomicOr(a.err, kErrStackOverflow);
 }
 
 // After k_render_refill: a group whose 8 lanes all hit an emitter at bounce 0
