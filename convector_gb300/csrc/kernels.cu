@@ -484,12 +484,31 @@ constexpr int kRefillFrameSteps = 2;
 
 // COUNT: the same frame, also counting its work (FrameArgs::work); the
 // counters cost registers, so frames are rendered without them.
+// Trees deeper than 40 levels (the CLAIM_MIN 8 instantiation) keep the first
+// 16 stack entries of each lane in shared memory and read the approximation
+// tables from global memory instead (the 16 KB of entries per block take the
+// room the tables would); shallower trees keep the whole stack local. Measured
+// on the 870k-triangle tube (70 levels), ms per 1280x736 sample: local stack
+// 3.07-3.11; 4, 8 entries 3.11, 3.03; 8, 12, 16 with the tables in global
+// memory 3.10, 3.04, 2.99 (20, 24, 32: 2.96, 3.00, 3.19). On the 19-level room
+// the same entries cost 3-4 %.
+constexpr int kDeepFrameStackShared = 16;
+
 template <int CLAIM_MIN, bool COUNT>
 __global__ void __launch_bounds__(128, kRefillFrameBlocksPerSm) k_render_refill(FrameArgs a) {
-    __shared__ ApproxTables tab;
-    load_tables(tab);
+    constexpr int kShared = CLAIM_MIN == 8 ? kDeepFrameStackShared : 0;
     FramePaths P{a, (a.w + 15u) / 16u, (a.h + 3u) / 4u, 0u};
-    if (!path_refill<CLAIM_MIN, kRefillFrameSteps, COUNT, true>(P, tab)) atomicOr(a.err, kErrStackOverflow);
+    bool ok;
+    if constexpr (kShared > 0) {
+        __shared__ uint2 sstack[4][kShared][32];
+        ok = path_refill<CLAIM_MIN, kRefillFrameSteps, COUNT, true, kShared>(
+            P, g_tables, &sstack[threadIdx.x >> 5][0][threadIdx.x & 31]);
+    } else {
+        __shared__ ApproxTables tab;
+        load_tables(tab);
+        ok = path_refill<CLAIM_MIN, kRefillFrameSteps, COUNT, true>(P, tab);
+    }
+    if (!ok) atomicOr(a.err, kErrStackOverflow);
 }
 
 // After k_render_refill: a group whose 8 lanes all hit an emitter at bounce 0

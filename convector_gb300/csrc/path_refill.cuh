@@ -49,14 +49,16 @@ namespace cvx {
 // for the frame kernel: 1280x736 tube 3.11 -> 3.08 ms, room 0.714 -> 0.704 ms,
 // icosphere 1.44 -> 1.42 ms (the wave kernel, whose scene table costs
 // registers, would spill 10 bytes more).
-template <int CLAIM_MIN, int STEPS, bool COUNT = false, bool SELECT_ROUNDS = false, class Paths>
-__device__ __forceinline__ bool path_refill(Paths& P, const ApproxTables& tab) {
+template <int CLAIM_MIN, int STEPS, bool COUNT = false, bool SELECT_ROUNDS = false, int SHARED_STACK = 0,
+          class Paths>
+__device__ __forceinline__ bool path_refill(Paths& P, const ApproxTables& tab, uint2* shared_stack = nullptr) {
     typedef typename Paths::PathRef PathRef;
     const int lane = threadIdx.x & 31;
     const uint32_t npaths = P.n_paths();
     RefillRay ray;
     uint2 local_stack[kStackDepth];
-    LocalStack stack{local_stack};
+    typename std::conditional<SHARED_STACK == 0, LocalStack, SharedLocalStack<SHARED_STACK>>::type stack =
+        make_stack<SHARED_STACK>(shared_stack, local_stack);
     ray.top = make_uint2(0u, 0u);
     ray.sp = 0;
     ray.cur = RefillRay::kNone;
