@@ -492,15 +492,29 @@ struct WavePaths {
 // 7 resident blocks per SM (72 registers and a small spill): 6 (80 registers,
 // no spill) served the 415-request mix at 2,014 against 2,083 Mrays/s.
 constexpr int kRefillWaveBlocksPerSm = 7;
+// As the frame kernel: waves whose trees are deeper than 40 levels keep the
+// first 16 stack entries of each lane in shared memory and read the tables
+// from global memory (4 tube views of 1280x736, 2 samples: 21.5 -> 20.3 ms;
+// 12 entries 20.5 ms).
+constexpr int kDeepWaveStackShared = 16;
 template <int CLAIM_MIN>
 __global__ void __launch_bounds__(128, kRefillWaveBlocksPerSm) k_wave_refill(const Job* __restrict__ jobs,
                                                                           const WaveHeader* __restrict__ hdr,
                                                                           const DeviceScene* __restrict__ scenes,
                                                                           WaveOutputs out) {
-    __shared__ ApproxTables tab;
-    load_tables_wf(tab);
+    constexpr int kShared = CLAIM_MIN == 8 ? kDeepWaveStackShared : 0;
     WavePaths P{jobs, scenes, out, hdr->n_jobs, hdr->n_groups, 0u, 0u};
-    if (!path_refill<CLAIM_MIN, 2>(P, tab)) atomicOr(out.err, kErrStackOverflow);
+    bool ok;
+    if constexpr (kShared > 0) {
+        __shared__ uint2 sstack[4][kShared][32];
+        ok = path_refill<CLAIM_MIN, 2, false, false, kShared>(P, g_tables_wf,
+                                                               &sstack[threadIdx.x >> 5][0][threadIdx.x & 31]);
+    } else {
+        __shared__ ApproxTables tab;
+        load_tables_wf(tab);
+        ok = path_refill<CLAIM_MIN, 2>(P, tab);
+    }
+    if (!ok) atomicOr(out.err, kErrStackOverflow);
 }
 
 // After k_wave_refill: the groups of the wave whose 8 lanes all hit an
