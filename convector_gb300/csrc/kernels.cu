@@ -494,19 +494,24 @@ constexpr int kRefillFrameSteps = 2;
 // the same entries cost 3-4 %.
 constexpr int kDeepFrameStackShared = 16;
 
-template <int CLAIM_MIN, bool COUNT>
+// Deep trees: claim threshold 8 and three traversal steps per round of votes
+// (tube, ms per sample: claim 6, 8, 10, 12 -> 3.01, 2.98, 2.97, 2.99 at two
+// steps; steps 1, 2, 3, 4 -> 3.15, 2.98, 2.93, 3.07 at claim 8).
+constexpr int kDeepFrameClaim = 8;
+constexpr int kDeepFrameSteps = 3;
+// DEEP: a tree deeper than 40 levels (shared stack entries, the constants above).
+template <bool DEEP, bool COUNT>
 __global__ void __launch_bounds__(128, kRefillFrameBlocksPerSm) k_render_refill(FrameArgs a) {
-    constexpr int kShared = CLAIM_MIN == 8 ? kDeepFrameStackShared : 0;
     FramePaths P{a, (a.w + 15u) / 16u, (a.h + 3u) / 4u, 0u};
     bool ok;
-    if constexpr (kShared > 0) {
-        __shared__ uint2 sstack[4][kShared][32];
-        ok = path_refill<CLAIM_MIN, kRefillFrameSteps, COUNT, true, kShared>(
+    if constexpr (DEEP) {
+        __shared__ uint2 sstack[4][kDeepFrameStackShared][32];
+        ok = path_refill<kDeepFrameClaim, kDeepFrameSteps, COUNT, true, kDeepFrameStackShared>(
             P, g_tables, &sstack[threadIdx.x >> 5][0][threadIdx.x & 31]);
     } else {
         __shared__ ApproxTables tab;
         load_tables(tab);
-        ok = path_refill<CLAIM_MIN, kRefillFrameSteps, COUNT, true>(P, tab);
+        ok = path_refill<16, kRefillFrameSteps, COUNT, true>(P, tab);
     }
     if (!ok) atomicOr(a.err, kErrStackOverflow);
 }
@@ -717,12 +722,12 @@ cudaError_t launch_render(const DeviceScene& s, const DeviceCamera& cam, uint32_
         uint32_t need = (ngroups * 8u + 127u) / 128u, blocks = (uint32_t)num_sms() * kRefillFrameBlocksPerSm;
         if (blocks > need) blocks = need;
         if (work) {
-            if (s.depth > 40) k_render_refill<8, true><<<blocks, 128, 0, st>>>(a);
-            else k_render_refill<16, true><<<blocks, 128, 0, st>>>(a);
+            if (s.depth > 40) k_render_refill<true, true><<<blocks, 128, 0, st>>>(a);
+            else k_render_refill<false, true><<<blocks, 128, 0, st>>>(a);
         } else if (s.depth > 40) {
-            k_render_refill<8, false><<<blocks, 128, 0, st>>>(a);
+            k_render_refill<true, false><<<blocks, 128, 0, st>>>(a);
         } else {
-            k_render_refill<16, false><<<blocks, 128, 0, st>>>(a);
+            k_render_refill<false, false><<<blocks, 128, 0, st>>>(a);
         }
         if (gbuf) {
             uint32_t fb = (ngroups + 255u) / 256u, cap = (uint32_t)num_sms() * 8u;

@@ -495,7 +495,7 @@ constexpr int kRefillWaveBlocksPerSm = 7;
 // As the frame kernel: waves whose trees are deeper than 40 levels keep the
 // first 16 stack entries of each lane in shared memory and read the tables
 // from global memory (4 tube views of 1280x736, 2 samples: 21.5 -> 20.3 ms;
-// 12 entries 20.5 ms).
+// 12 entries 20.5 ms; three or four steps per round 20.3, 22.5 ms).
 constexpr int kDeepWaveStackShared = 16;
 template <int CLAIM_MIN>
 __global__ void __launch_bounds__(128, kRefillWaveBlocksPerSm) k_wave_refill(const Job* __restrict__ jobs,
