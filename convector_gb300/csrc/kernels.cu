@@ -496,7 +496,9 @@ constexpr int kDeepFrameStackShared = 16;
 
 // Deep trees: claim threshold 8 and three traversal steps per round of votes
 // (tube, ms per sample: claim 6, 8, 10, 12 -> 3.01, 2.98, 2.97, 2.99 at two
-// steps; steps 1, 2, 3, 4 -> 3.15, 2.98, 2.93, 3.07 at claim 8).
+// steps; steps 1, 2, 3, 4 -> 3.15, 2.98, 2.93, 3.07 at claim 8; 6 and 8
+// resident blocks per SM instead of 7 -> 3.07 and 2.97, the latter with 64
+// registers and a 76-byte spill).
 constexpr int kDeepFrameClaim = 8;
 constexpr int kDeepFrameSteps = 3;
 // DEEP: a tree deeper than 40 levels (shared stack entries, the constants above).
