@@ -234,6 +234,11 @@ struct StagedSoaClaim {
 // shared, 0.890 with 4, 0.878 with 8, 0.883 with 12. (The wavefront and the
 // path-refill traversals, whose larger working sets need the L1 that the
 // carve-out takes, measured no gain or a loss.)
+// Traversal steps a lane takes per round of the warp's claim votes: 1, 3, 4
+// -> 0.798, 0.784, 0.777 ms per 4M rays of the 28-level icosphere (12 shared
+// stack entries) and 1.538, 1.503, 1.499 ms on the 70-level tube (medians of
+// three runs each).
+constexpr int kQuerySteps = 4;
 // The default; a scene may choose 0, 4 or 12 instead (cvx_scene_set_query_stack,
 // which the query autotuner sets per scene).
 constexpr int kQueryStackShared = 8;
@@ -251,8 +256,8 @@ __global__ void __launch_bounds__(128, MINB) k_intersect_refill(SoaRays src, uin
     __shared__ uint2 sstack[4][SHARED > 0 ? SHARED : 1][32];
     StagedSoaClaim claim{src, next_ray, stage[threadIdx.x >> 5], 0u, 0u, 0u, 0};
     claim.init(threadIdx.x & 31);
-    bool ok = traverse_refill<COUNT, false, CLAIM, SHARED, SELECT>(src, claim, g_tables,
-                                                                   &sstack[threadIdx.x >> 5][0][threadIdx.x & 31]);
+    bool ok = traverse_refill<COUNT, false, CLAIM, SHARED, SELECT, kQuerySteps>(
+        src, claim, g_tables, &sstack[threadIdx.x >> 5][0][threadIdx.x & 31]);
     if (!ok) atomicOr(err, kErrStackOverflow);
 }
 

@@ -384,9 +384,11 @@ __device__ __forceinline__ typename std::conditional<N == 0, LocalStack, SharedL
 // Returns false if a ray overflowed the stack (its hit is then incomplete).
 // SELECT: every ray whose reciprocals meet select_form_ray is traversed with
 // the select-form slab test; the others are handed to src.defer(r) untraced
-// (the caller traces them afterwards with the x86 form).
-template <bool COUNT, bool LEAF_AFTER_PAIR, int CLAIM_MIN, int SHARED_STACK = 0, bool SELECT = false, class Src,
-          class Claim>
+// (the caller traces them afterwards with the x86 form). STEPS: traversal
+// steps per round of the warp's votes (a lane whose ray ends within a round
+// waits for the next round's claim).
+template <bool COUNT, bool LEAF_AFTER_PAIR, int CLAIM_MIN, int SHARED_STACK = 0, bool SELECT = false, int STEPS = 1,
+          class Src, class Claim>
 __device__ __forceinline__ bool traverse_refill(const Src& src, Claim& claim, const ApproxTables& tab,
                                                 uint2* shared_stack = nullptr) {
     const int lane = threadIdx.x & 31;
@@ -432,10 +434,11 @@ __device__ __forceinline__ bool traverse_refill(const Src& src, Claim& claim, co
             }
         }
         if (__all_sync(0xffffffffu, done)) break;
-        if (!have) continue;
-        if (ray.step<COUNT, LEAF_AFTER_PAIR, SELECT>(stack, overflow)) {
-            src.store(r_id, ray.h, ray.na, ray.nt);
-            have = false;
+        for (int st = 0; st < STEPS && have; st++) {
+            if (ray.step<COUNT, LEAF_AFTER_PAIR, SELECT>(stack, overflow)) {
+                src.store(r_id, ray.h, ray.na, ray.nt);
+                have = false;
+            }
         }
     }
     return !overflow;
