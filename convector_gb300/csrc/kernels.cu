@@ -482,11 +482,14 @@ struct FramePaths {
 // Launch shape and loop form of the per-lane path refill, each measured on the
 // room (5k triangles), the 82k-triangle icosphere and the 870k-triangle tube at
 // 1280x736: 7 resident blocks per SM (72 registers, no spill; 8 blocks spill
-// and lose 2-7 %), two traversal steps per round of votes (1 and 3 are 3-8 %
-// slower), and a leaf reached from a pair tested in the same step. Claim
-// threshold: 16 lanes up to 40 levels, 8 beyond (measured 4 to 24).
+// and lose 2-7 %), and a leaf reached from a pair tested in the same step.
+// Trees up to 40 levels: claim threshold 16 and three traversal steps per
+// round of votes, swept with the select-form rounds in place (room 0.711 ->
+// 0.701-0.704 ms, icosphere 1.42 -> 1.40-1.41 ms against two steps; four
+// steps 0.733 and 1.46; claim 12 or 20 at three steps: room 0.751 or 0.694,
+// icosphere 1.412 or 1.432). Deeper trees: below (kDeepFrame*).
 constexpr int kRefillFrameBlocksPerSm = 7;
-constexpr int kRefillFrameSteps = 2;
+constexpr int kRefillFrameSteps = 3;
 
 // COUNT: the same frame, also counting its work (FrameArgs::work); the
 // counters cost registers, so frames are rendered without them.
