@@ -237,8 +237,10 @@ struct StagedSoaClaim {
 // Traversal steps a lane takes per round of the warp's claim votes: 1, 3, 4
 // -> 0.798, 0.784, 0.777 ms per 4M rays of the 28-level icosphere (12 shared
 // stack entries) and 1.538, 1.503, 1.499 ms on the 70-level tube (medians of
-// three runs each). The claim threshold, swept again at four steps (12, 16,
-// 20 on the icosphere: 0.774-0.780, 0.776-0.778, 0.792-0.796 ms), stays at 16.
+// three runs each; six steps: 0.774-0.778 and 1.474-1.482, within noise). The
+// claim thresholds, swept again at four steps, stay at 16 (12, 16, 20 on the
+// icosphere: 0.774-0.780, 0.776-0.778, 0.792-0.796 ms) and 8 for trees deeper
+// than 40 levels (6, 8, 12 on the tube: 1.499, 1.489-1.513, 1.493 ms).
 constexpr int kQuerySteps = 4;
 // The default; a scene may choose 0, 4 or 12 instead (cvx_scene_set_query_stack,
 // which the query autotuner sets per scene).

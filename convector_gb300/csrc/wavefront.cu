@@ -516,7 +516,7 @@ __global__ void __launch_bounds__(128, kRefillWaveBlocksPerSm) k_wave_refill(con
     } else {
         __shared__ ApproxTables tab;
         load_tables_wf(tab);
-        ok = path_refill<CLAIM_MIN, 2>(P, tab);
+        ok = path_refill<CLAIM_MIN, 2>(P, tab);  // three steps: room waves 5.24 -> 5.34 ms
     }
     if (!ok) atomicOr(out.err, kErrStackOverflow);
 }
