@@ -240,7 +240,9 @@ struct StagedSoaClaim {
 // three runs each; six steps: 0.774-0.778 and 1.474-1.482, within noise). The
 // claim thresholds, swept again at four steps, stay at 16 (12, 16, 20 on the
 // icosphere: 0.774-0.780, 0.776-0.778, 0.792-0.796 ms) and 8 for trees deeper
-// than 40 levels (6, 8, 12 on the tube: 1.499, 1.489-1.513, 1.493 ms).
+// than 40 levels (6, 8, 12 on the tube: 1.499, 1.489-1.513, 1.493 ms). A leaf
+// reached from a pair tested in the same step (the frame kernels' form) is
+// slower here at 2, 3 and 4 steps: 0.84, 0.82-0.84, 0.82 ms on the icosphere.
 constexpr int kQuerySteps = 4;
 // The default; a scene may choose 0, 4 or 12 instead (cvx_scene_set_query_stack,
 // which the query autotuner sets per scene).
