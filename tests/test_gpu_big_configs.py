@@ -87,3 +87,29 @@ def test_batch_of_256_scenes_equals_views_alone(gpu):
             r.accumulate_frame_f32(v.frame_base + s)
         alone = r.resolve_u8(v.spp)
         assert (imgs[i] == alone).all(), i
+
+
+def test_large_mesh_full_frame_bitexact_against_oracle(gpu, orc):
+    """The deep-tree path-refill kernel (shared stack entries, select-form
+    rounds) on the benchmark's own frame: 1280x736 of the 870k-triangle tube,
+    frame 42, per-group RNG order, bit-exact RGBA, gbuffer, linear colour and
+    ray count against the oracle; then two accumulated samples, bit-exact."""
+    tris, _ = scenes.random_walk_tube(obj=False)
+    bvh = gpu.Bvh.build(tris)
+    scene = gpu.Scene(bvh)
+    scenes.default_camera(scene.camera)
+    osc = orc.OracleScene.from_bvh(bvh)
+    w, h = 1280, 736
+    r = gpu.Renderer(scene, w, h, rng_order=gpu.RNG_GROUP, traversal=gpu.TRAVERSE_SINGLE,
+                     refill_mode=gpu.REFILL_ALL)
+    rgba, gb = r.render_frame_u8(42)
+    col = r.read_frame_f32()
+    orgba, ogb, ocol, orays = osc.render(scene.camera.as_array(), w, h, 42, rng_order=orc.RNG_GROUP, traversal=1)
+    assert (rgba == orgba).all() and (gb == ogb).all()
+    assert (col.view(np.uint32) == ocol.view(np.uint32)).all()
+    assert r.stats()[0] == orays
+    acc = np.zeros((h, w, 3), np.float32)
+    for f in (43, 44):
+        r.accumulate_frame_f32(f)
+        osc.render(scene.camera.as_array(), w, h, f, rng_order=orc.RNG_GROUP, traversal=1, color=False, accum=acc)
+    assert (r.read_accumulator().view(np.uint32) == acc.view(np.uint32)).all()

@@ -49,3 +49,18 @@ def test_raycast_kernel_against_reference_packet_traversal(gpu, orc):
     g = cls == orc.GRAZING
     print("grazing rays where the reference's hit is the nearer: %d of %d" % (int((t_ref[g] < t[g]).sum()),
                                                                            int(g.sum())))
+
+
+def test_packet_query_equals_reference_traversal_on_every_ray(gpu, orc):
+    """The packet variant takes the reference's decisions (bvh.rs:589-657:
+    an octet is the 8-ray packet): on all 4,194,304 rays of the workload its
+    index and t bits equal the oracle's packet traversal, with no exception."""
+    text, mats = scenes.displaced_icosphere()
+    bvh = gpu.Bvh.from_meshes([gpu.Mesh.parse(text, mats)])
+    scene = gpu.Scene(bvh)
+    osc = orc.OracleScene.from_bvh(bvh)
+    o, d = scenes.random_rays(N_RAYS, seed=7)
+    t, tri = scene.intersect_nearest(o, d, traversal=gpu.TRAVERSE_PACKET)
+    t_ref, tri_ref = osc.intersect(o, d, mode=orc.TRAVERSE_PACKET)
+    assert (tri == tri_ref).all(), np.nonzero(tri != tri_ref)[0][:10]
+    assert (t.view(np.uint32) == t_ref.view(np.uint32)).all()
