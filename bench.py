@@ -550,12 +550,28 @@ def bench_large(cg):
         if name == "autotuned":
             res["config"] = best
         out[name] = res
+    # The 64 samples in one call (cvx_accumulate_frames_f32): in the
+    # path-refill form 32 samples share a launch, so the launch's drain is paid
+    # once per 32 samples; same accumulator bits as 64 one-sample calls.
+    r = cg.Renderer(scene, 1280, 736, **dict(best, rng_order=cg.RNG_GROUP))
+    r.accumulate_frames_f32(0, 16)
+    ms_calls, rays = [], 0
+    for c in range(5):
+        r.accumulate_frames_f32(42 + 64 * c, 64)
+        nr, m = r.stats()
+        ms_calls.append(m)
+        rays += nr
+    per = float(np.percentile(ms_calls, 50)) / 64.0
+    out["in_one_call"] = {"sample_ms_p50": per, "call_ms": [round(m, 3) for m in ms_calls], "spp": 64,
+                          "frames_per_launch": 32, "mrays_per_s": rays / (sum(ms_calls) * 1e-3) / 1e6,
+                          "mpaths_per_s": 1280 * 736 * 64 * 5 / (sum(ms_calls) * 1e-3) / 1e6, "config": best}
     # Roofline of one accumulated sample (frame 42's work): the accumulator is
     # read and written (24 bytes per pixel).
     work = cg.Renderer(scene, 1280, 736, rng_order=cg.RNG_GROUP, traversal=cg.TRAVERSE_SINGLE).count_work(42)
     ms = out["autotuned"]["frame_ms_p50"]
     out["roofline"] = frame_roofline(work, scene.direct_sample_num(), 1280 * 736, ms, 24, "k_render_refill@tube")
     out["roofline"]["frame_ms"] = ms
+    out["in_one_call"]["roofline"] = frame_roofline(work, scene.direct_sample_num(), 1280 * 736, per, 24)
     if CPU_BASELINE:
         out["cpu_baseline"] = cpu_frame_baseline(bvh, scene.camera, 1280, 736, 42, accumulate=True, target_s=5.0,
                                                  max_frames=2)
@@ -566,7 +582,8 @@ def bench_frame_kernel(cg, which):
     """A few frames of one single-ray frame kernel alone (paths per lane, the
     autotuned form for both scenes), for profiling: `room` renders the
     1280x736 interactive frame of the room-and-sphere scene, `tube` samples of
-    the 870k-triangle tube accumulated at 1280x736."""
+    the 870k-triangle tube accumulated at 1280x736, `tube-multi` two
+    accumulate_frames_f32 calls of 32 tube samples (one launch each)."""
     from convector_gb300 import scenes
     if which == "room":
         bvh = build_c0()
@@ -577,9 +594,11 @@ def bench_frame_kernel(cg, which):
     r = cg.Renderer(scene, 1280, 736, rng_order=cg.RNG_GROUP, traversal=cg.TRAVERSE_SINGLE,
                     refill_mode=cg.REFILL_ALL)
     ms = []
-    for f in range(4):
+    for f in range(2 if which == "tube-multi" else 4):
         if which == "room":
             r.render_frame_u8(42 + f, gbuffer=False)
+        elif which == "tube-multi":
+            r.accumulate_frames_f32(42 + 32 * f, 32)
         else:
             r.accumulate_frame_f32(42 + f)
         ms.append(r.stats()[1])
@@ -672,10 +691,11 @@ def _served_run(cg, scs, reqs, sequential, engine=None):
             "wavefront_busy_s": st["wavefront_busy_s"]}
 
 
-def _plain_renderer_run(cg, scs, bvhs, reqs, modes=None):
+def _plain_renderer_run(cg, scs, bvhs, reqs, modes=None, one_call=False):
     """The plain method: the drop-in Renderer API, one request at a time in
     arrival order. Each request gets a Renderer at its resolution, spp
-    accumulate_frame_f32 calls and a resolve_u8 read back to the host; the
+    accumulate_frame_f32 calls (the reference's per-frame loop; one_call: a
+    single accumulate_frames_f32 call) and a resolve_u8 read back to the host; the
     scene's kernel form is the server's default rule (wavefront for BVHs
     deeper than 40 or above 200k triangles, else the single-launch form)
     unless `modes` gives one per scene. The time of the requests is broken
@@ -693,9 +713,12 @@ def _plain_renderer_run(cg, scs, bvhs, reqs, modes=None):
         r.set_camera(cam)
         t1 = time.perf_counter()
         n, dev = 0, 0.0
-        for s in range(spp):
-            r.accumulate_frame_f32(base + s)
-            nr, ms = r.stats()  # rays and device time of the last frame
+        for s in range(1 if one_call else spp):
+            if one_call:
+                r.accumulate_frames_f32(base, spp)
+            else:
+                r.accumulate_frame_f32(base + s)
+            nr, ms = r.stats()  # rays and device time of the last call
             n += nr
             dev += ms * 1e-3
         t2 = time.perf_counter()
@@ -793,6 +816,10 @@ def bench_served(cg, duration=2.0, rate=200.0, seed=4):
     # scene in the wavefront form (the server's default rule for its engines).
     plain = _plain_renderer_run(cg, scs, bvhs, reqs, modes=[cg.MODE_MEGAKERNEL] * len(scs))
     plain_wf = _plain_renderer_run(cg, scs, bvhs, reqs)
+    # The same plain path with each request's samples in one
+    # accumulate_frames_f32 call (up to 32 samples per launch in the
+    # path-refill form).
+    plain_one = _plain_renderer_run(cg, scs, bvhs, reqs, modes=[cg.MODE_MEGAKERNEL] * len(scs), one_call=True)
     # Below saturation: half the arrival rate.
     low_rate = rate / 2
     reqs_low = _served_requests(cg, scenes, low_rate, duration, seed + 1)
@@ -802,6 +829,8 @@ def bench_served(cg, duration=2.0, rate=200.0, seed=4):
             "served_wavefront_engines": served_wf, "served_wavefront_engine_config": wf_engine,
             "served_default_engine": served_default, "plain_renderer": plain,
             "plain_renderer_wavefront_for_deep": plain_wf,
+            "plain_renderer_frames_in_one_call": plain_one,
+            "throughput_ratio_vs_plain_frames_in_one_call": served["mrays_per_s"] / plain_one["mrays_per_s"],
             "throughput_ratio_vs_plain_wavefront_for_deep": served["mrays_per_s"] / plain_wf["mrays_per_s"],
             "server_one_at_a_time": sequential,
             "throughput_ratio": served["mrays_per_s"] / plain["mrays_per_s"],
@@ -848,7 +877,8 @@ def main():
     ap.add_argument("--no-extra", action="store_true", help="skip the large, batched and served sections")
     ap.add_argument("--launch", help="query configuration (packet8/0, single/8, single/8/s0, single/8/s4, "
                                      "single/8/s12, single/10, single/12) instead of the fastest of a short trial")
-    ap.add_argument("--section", choices=["render", "large", "batched", "served", "bvh", "frame-room", "frame-tube"],
+    ap.add_argument("--section", choices=["render", "large", "batched", "served", "bvh", "frame-room", "frame-tube",
+                                          "frame-tube-multi"],
                     help="run one extra section alone and print its JSON (no headline line)")
     args = ap.parse_args()
     if args.warmup < 3:
@@ -860,7 +890,8 @@ def main():
         cg.lib(build=True)
         fn = {"render": bench_render, "large": bench_large, "batched": bench_batched, "served": bench_served,
               "bvh": bench_bvh_build, "frame-room": lambda c: bench_frame_kernel(c, "room"),
-              "frame-tube": lambda c: bench_frame_kernel(c, "tube")}
+              "frame-tube": lambda c: bench_frame_kernel(c, "tube"),
+              "frame-tube-multi": lambda c: bench_frame_kernel(c, "tube-multi")}
         print(json.dumps({args.section: fn[args.section](cg)}))
         return
     if args.impl == "reference":

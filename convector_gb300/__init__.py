@@ -132,6 +132,7 @@ def lib(build=False):
         "cvx_render_patches_u8": (I32, [P, U32, P, U32, U32, P, P]),
         "cvx_accumulate_patches_f32": (I32, [P, U32, P, U32, U32, P]),
         "cvx_accumulate_frame_f32": (I32, [P, U32, P]),
+        "cvx_accumulate_frames_f32": (I32, [P, U32, U32, P]),
         "cvx_resolve_u8": (I32, [P, U32, P]),
         "cvx_read_accumulator": (I32, [P, P]),
         "cvx_clear_accumulator": (I32, [P]),
@@ -530,6 +531,14 @@ class Renderer:
     def accumulate_frame_f32(self, frame_number, gbuffer=False):
         gb = np.empty((self.height, self.width), dtype=np.uint32) if gbuffer else None
         _check(lib().cvx_accumulate_frame_f32(self._h, frame_number, _ptr(gb)))
+        return gb
+
+    def accumulate_frames_f32(self, first_frame, n_frames, gbuffer=False):
+        """accumulate_frame_f32 for frames first_frame .. first_frame +
+        n_frames - 1 in one call (cvx_accumulate_frames_f32): the same bits,
+        with up to 32 frames per launch in the path-refill form."""
+        gb = np.empty((self.height, self.width), dtype=np.uint32) if gbuffer else None
+        _check(lib().cvx_accumulate_frames_f32(self._h, first_frame, n_frames, _ptr(gb)))
         return gb
 
     def resolve_u8(self, num_samples):

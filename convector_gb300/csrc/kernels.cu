@@ -2,6 +2,7 @@
 // Compiled with -fmad=false (see x86sem.cuh).
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <atomic>
 
 #include "kernels.h"
@@ -330,6 +331,13 @@ struct FrameArgs {
     // the counting form of k_render_refill: totals of boxes and triangles
     // tested and of light-PDF shading steps (3 words, zero at launch)
     unsigned long long* work;
+    // k_render_refill: samples rendered by the launch (frames frame ..
+    // frame + samples - 1, their paths claimed sample after sample). The last
+    // sample writes the frame buffers as a one-sample launch does (without the
+    // accumulator); sample s < samples - 1 writes its linear colour to
+    // sample_color + 3 * w * h * s, for k_accumulate_samples.
+    uint32_t samples;
+    float* sample_color;
 };
 
 // Screen x (or y) of lane k of group g of the 16x4 block at (xb, yb), before
@@ -420,46 +428,70 @@ __device__ __forceinline__ void path_pixel(uint32_t p, uint32_t bw, uint32_t& gx
     py = gy + (k >> 2);
 }
 
-// The paths of one frame for path_refill (path p: lane p & 7 of group p >> 3,
-// groups numbered as in k_render_group).
+// The paths of a launch for path_refill. One sample (MULTI false): path p is
+// lane p & 7 of group p >> 3, groups numbered as in k_render_group. MULTI:
+// a.samples samples, claimed one after the other: claim number p is path
+// p mod per of sample p / per, per being the paths of one sample (a multiple
+// of 64, so both numbers share their lane and group-in-block bits). The two
+// forms are separate instantiations: the sample logic in the one-sample
+// kernel's loop slowed it by 6-7 % (tube 2.945 -> 3.12 ms, room 0.705 ->
+// 0.759 ms). The reference keeps the sample, so that only the path's start
+// divides (tube 2.356 -> 2.248 ms per sample with 16 per launch, room 0.620 ->
+// 0.588 ms).
+template <bool MULTI>
 struct FramePaths {
     struct PathRef {
-        uint32_t path;
+        uint32_t path;  // within its sample
+        uint32_t smp;
     };
     const FrameArgs& a;
     uint32_t bw, bh, rays;
 
-    __device__ __forceinline__ uint32_t n_paths() const { return bw * bh * 64u; }
+    __device__ __forceinline__ uint32_t per() const { return bw * bh * 64u; }
+    __device__ __forceinline__ uint32_t n_paths() const { return MULTI ? per() * a.samples : per(); }
     __device__ __forceinline__ uint32_t claim(uint32_t n) { return atomicAdd(a.err + 1, n); }
     __device__ __forceinline__ bool begin(uint32_t p, PathRef& r, F3& o, F3& d, LaneRng& rng,
                                           const ApproxTables& tab) {
+        const uint32_t smp = MULTI ? p / per() : 0u;
+        p -= smp * per();
         uint32_t gx, gy, px, py;
         path_pixel(p, bw, gx, gy, px, py);
         if (gx >= a.w || gy >= a.h) return false;
         r.path = p;
+        r.smp = smp;
         const int k = (int)(p & 7u);
         float x, y, scale;
         block_coord(a.w, a.h, gx & ~15u, gy & ~3u, (int)((p >> 3) & 7u), k, &x, &y, &scale);
-        rng.seed(gx, gy, a.frame, k);
+        rng.seed(gx, gy, a.frame + smp, k);
         x = fmaf(unit_from(rng.next()), scale, x);
         y = fmaf(unit_from(rng.next()), scale, y);
         camera_ray(a.cam, x, y, unit_from(rng.next()), tab, o, d);
         return true;
     }
     __device__ __forceinline__ DeviceScene scene(const PathRef&) const { return a.s; }
+    __device__ __forceinline__ bool last(const PathRef& r) const { return !MULTI || r.smp + 1u == a.samples; }
     __device__ __forceinline__ void gbuffer(const PathRef& r, uint32_t word) {
+        if (!a.gbuf || !last(r)) return;
         uint32_t gx, gy, px, py;
         path_pixel(r.path, bw, gx, gy, px, py);
-        if (a.gbuf && px < a.w && py < a.h) a.gbuf[(size_t)py * a.w + px] = word;
+        if (px < a.w && py < a.h) a.gbuf[(size_t)py * a.w + px] = word;
     }
     __device__ __forceinline__ void mark_emitter(const PathRef& r) {
-        if (a.gbuf) atomicOr(a.group_em + (r.path >> 3), 1u << (r.path & 7u));
+        if (!a.gbuf || !last(r)) return;
+        atomicOr(a.group_em + (r.path >> 3), 1u << (r.path & 7u));
     }
     __device__ __forceinline__ void store(const PathRef& r, F3 c) {
         uint32_t gx, gy, px, py;
         path_pixel(r.path, bw, gx, gy, px, py);
         if (px >= a.w || py >= a.h) return;
         const size_t idx = (size_t)py * a.w + px;
+        if (!last(r)) {
+            float* out = a.sample_color + (size_t)3 * a.w * a.h * r.smp + 3 * idx;
+            out[0] = c.x;
+            out[1] = c.y;
+            out[2] = c.z;
+            return;
+        }
         if (a.rgba) a.rgba[idx] = pack_color(c);
         if (a.color) {
             a.color[3 * idx] = c.x;
@@ -515,9 +547,10 @@ constexpr int kDeepFrameStackShared = 16;
 constexpr int kDeepFrameClaim = 8;
 constexpr int kDeepFrameSteps = 3;
 // DEEP: a tree deeper than 40 levels (shared stack entries, the constants above).
-template <bool DEEP, bool COUNT>
+// MULTI: a.samples samples in one launch (FramePaths<true>).
+template <bool DEEP, bool COUNT, bool MULTI = false>
 __global__ void __launch_bounds__(128, kRefillFrameBlocksPerSm) k_render_refill(FrameArgs a) {
-    FramePaths P{a, (a.w + 15u) / 16u, (a.h + 3u) / 4u, 0u};
+    FramePaths<MULTI> P{a, (a.w + 15u) / 16u, (a.h + 3u) / 4u, 0u};
     bool ok;
     if constexpr (DEEP) {
         __shared__ uint2 sstack[4][kDeepFrameStackShared][32];
@@ -545,6 +578,21 @@ __global__ void __launch_bounds__(256) k_emitter_groups(const uint32_t* __restri
             uint32_t qx = gx + (q & 3u), qy = gy + (q >> 2);
             if (qx < w && qy < h) gbuf[(size_t)qy * w + qx] = 0u;
         }
+    }
+}
+
+// After a k_render_refill launch of n > 1 samples: adds each pixel's sample
+// colours to the accumulator in sample order (samples 0 .. n - 2 from
+// `samples`, the last from the frame's colour buffer). These are the additions
+// one launch per frame makes (renderer.rs:339-410 accumulates a frame at a
+// time), in the same order, so the accumulator gets the same bits.
+__global__ void __launch_bounds__(256) k_accumulate_samples(float* __restrict__ accum,
+                                                           const float* __restrict__ samples,
+                                                           const float* __restrict__ last, size_t nf, uint32_t n) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < nf; i += (size_t)gridDim.x * blockDim.x) {
+        float v = accum[i];
+        for (uint32_t s = 0; s + 1u < n; s++) v += __ldg(samples + (size_t)s * nf + i);
+        accum[i] = v + last[i];
     }
 }
 
@@ -725,20 +773,27 @@ cudaError_t launch_render(const DeviceScene& s, const DeviceCamera& cam, uint32_
                           bool packet, bool patch_order, uint32_t* rgba, uint32_t* gbuf, float* color, float* accum,
                           unsigned long long* rays, uint32_t* err, uint32_t block, bool debug, cudaStream_t st,
                           uint32_t patch, const uint32_t* patches, uint32_t n_patches, uint32_t* group_em,
-                          unsigned long long* work) {
+                          unsigned long long* work, uint32_t samples, float* sample_color) {
     if (patch == 0) patch = 32;
-    FrameArgs a{s, cam, w, h, frame, rgba, gbuf, color, accum, rays, err, debug ? 1u : 0u, patch, patches, n_patches,
-                group_em, work};
+    if (samples == 0) samples = 1;
+    if (samples > 1 && (!accum || !color || !sample_color)) return cudaErrorInvalidValue;
+    FrameArgs a{s,      cam,     w,         h,       frame, rgba, gbuf, color, samples > 1 ? nullptr : accum,
+                rays,   err,     debug ? 1u : 0u, patch, patches, n_patches, group_em, work, samples, sample_color};
     if (block == 0) block = 128;
     if (group_em && !packet && !patch_order && !debug) {
         uint32_t ngroups = ((w + 15u) / 16u) * ((h + 3u) / 4u) * 8u;
         cudaError_t e = cudaMemsetAsync(group_em, 0, (size_t)ngroups * 4u, st);
         if (e != cudaSuccess) return e;
-        uint32_t need = (ngroups * 8u + 127u) / 128u, blocks = (uint32_t)num_sms() * kRefillFrameBlocksPerSm;
+        uint32_t need = (uint32_t)(((uint64_t)ngroups * 8u * samples + 127u) / 128u),
+                 blocks = (uint32_t)num_sms() * kRefillFrameBlocksPerSm;
         if (blocks > need) blocks = need;
         if (work) {
+            if (samples > 1) return cudaErrorInvalidValue;
             if (s.depth > 40) k_render_refill<true, true><<<blocks, 128, 0, st>>>(a);
             else k_render_refill<false, true><<<blocks, 128, 0, st>>>(a);
+        } else if (samples > 1) {
+            if (s.depth > 40) k_render_refill<true, false, true><<<blocks, 128, 0, st>>>(a);
+            else k_render_refill<false, false, true><<<blocks, 128, 0, st>>>(a);
         } else if (s.depth > 40) {
             k_render_refill<true, false><<<blocks, 128, 0, st>>>(a);
         } else {
@@ -748,8 +803,15 @@ cudaError_t launch_render(const DeviceScene& s, const DeviceCamera& cam, uint32_
             uint32_t fb = (ngroups + 255u) / 256u, cap = (uint32_t)num_sms() * 8u;
             k_emitter_groups<<<fb < cap ? fb : cap, 256, 0, st>>>(group_em, ngroups, w, h, gbuf);
         }
+        if (samples > 1 && accum) {
+            const size_t nf = (size_t)3 * w * h;
+            const uint32_t cap = (uint32_t)num_sms() * 8u;
+            const uint32_t fb = (uint32_t)std::min<size_t>((nf + 255u) / 256u, cap);
+            k_accumulate_samples<<<fb, 256, 0, st>>>(accum, sample_color, color, nf, samples);
+        }
         return cudaGetLastError();
     }
+    if (samples != 1) return cudaErrorInvalidValue;
     if (patch_order) {
         uint32_t units = patches ? n_patches : ((w + patch - 1) / patch) * ((h + patch - 1) / patch);
         uint32_t blocks = (units * 32 + block - 1) / block;  // one warp per patch

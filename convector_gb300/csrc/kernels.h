@@ -67,7 +67,13 @@ cudaError_t launch_render(const DeviceScene& s, const DeviceCamera& cam, uint32_
                           bool packet, bool patch_order, uint32_t* rgba, uint32_t* gbuf, float* color, float* accum,
                           unsigned long long* rays, uint32_t* err, uint32_t block, bool debug, cudaStream_t st, uint32_t patch = 32,
                           const uint32_t* patches = nullptr, uint32_t n_patches = 0, uint32_t* group_em = nullptr,
-                          unsigned long long* work = nullptr);
+                          unsigned long long* work = nullptr, uint32_t samples = 1, float* sample_color = nullptr);
+// Frames with the per-lane path refill (group_em set, single-ray traversal,
+// per-group RNG order) may render `samples` > 1 frames, frame .. frame +
+// samples - 1, in one launch, accumulating them into `accum` in frame order
+// (bit-identical to one launch per frame); color and gbuf then hold the last
+// frame's values, and sample_color holds 3 * w * h * (samples - 1) floats.
+// Other forms take samples == 1 only.
 cudaError_t launch_resolve(const float* accum, uint32_t npx, float factor, uint32_t* rgba, cudaStream_t st);
 // refill_from: first bounce whose single-ray traversal uses ray refill (the
 // earlier ones traverse one octet per group); packet traversal ignores it.

@@ -283,6 +283,18 @@ int32_t cvx_render_frame_u8(cvx_renderer* r, uint32_t frame_number, uint32_t* rg
 /* Renderer::accumulate_patch_f32 (renderer.rs:339-362) over the frame: adds
  * this frame's colour to the device accumulator; gbuffer may be NULL. */
 int32_t cvx_accumulate_frame_f32(cvx_renderer* r, uint32_t frame_number, uint32_t* gbuffer);
+/* The accumulation loop of main.rs (one accumulate_patch_f32 pass per frame,
+ * renderer.rs:339-362) over frames first_frame .. first_frame + n_frames - 1
+ * in one call: the accumulator, the frame buffer (cvx_read_frame_f32) and the
+ * gbuffer (may be NULL) end with the same bits as after n_frames calls of
+ * cvx_accumulate_frame_f32 in frame order, and cvx_renderer_stats reports
+ * their total rays and time. A single-launch renderer with the single-ray
+ * traversal and the per-group RNG order renders up to 32 frames per launch
+ * with the per-lane path refill (whatever its refill_mode: the frames' bits
+ * are the same), each pixel's frames being added in frame order afterwards;
+ * this takes up to 512 MiB of device memory for their colours, allocated at
+ * the first call. Other forms take one launch per frame. */
+int32_t cvx_accumulate_frames_f32(cvx_renderer* r, uint32_t first_frame, uint32_t n_frames, uint32_t* gbuffer);
 /* Renderer::render_patch_u8 (renderer.rs:306-327) for a list of patches in
  * one call: origins holds n_patches (x, y) pairs, each patch patch_width
  * pixels square (a multiple of 16, at most CVX_MAX_IMAGE_SIDE; pixels of a
