@@ -661,14 +661,18 @@ def bench_batched(cg):
             "speedup_wall": wall_p / wall_b}
 
 
-def _served_run(cg, scs, reqs, sequential, engine=None):
+def _served_run(cg, scs, reqs, sequential, engine=None, burst=False):
+    """The requests through a Server, each submitted at its arrival time
+    (burst: all at once, which measures the throughput the server sustains)."""
     engine = engine or {}
     srv = cg.Server(scs, framebuffer_bytes=24 << 30, max_groups=1 << 21, traversal=cg.TRAVERSE_SINGLE,
                     sequential=sequential, blocks_per_sm=engine.get("blocks_per_sm", 0),
                     refill_mode=engine.get("refill_mode", cg.REFILL_AFTER_CAMERA),
                     fused_blocks_per_sm=engine.get("fused_blocks_per_sm", 0),
                     wavefront_streams=engine.get("wavefront_streams", 1),
-                    deep_single_launch=engine.get("deep_single_launch", 0))
+                    deep_single_launch=engine.get("deep_single_launch", 0),
+                    max_inflight_pixels=engine.get("max_inflight_pixels", 0),
+                    samples_per_wave=engine.get("samples_per_wave", 1))
     # warm-up: one small request per scene
     for k in range(len(scs)):
         srv.wait(srv.submit(k, 64, 64, 1, reqs[0][5]))
@@ -676,10 +680,14 @@ def _served_run(cg, scs, reqs, sequential, engine=None):
     t0 = time.perf_counter()
     for at, sc, w, h, spp, cam in reqs:
         dt = t0 + at - time.perf_counter()
-        if dt > 0:
+        if dt > 0 and not burst:
             time.sleep(dt)
         ids.append(srv.submit(sc, w, h, spp, cam, frame_base=len(ids) * 16))
-    res = [srv.wait(i, 600000)[2] for i in ids]
+    done = [srv.wait(i, 600000) for i in ids]
+    failed = sum(1 for st, _, _ in done if st != 0)
+    if failed:
+        raise RuntimeError("%d of %d served requests failed" % (failed, len(ids)))
+    res = [r for _, _, r in done]
     lat = np.array([r["done_s"] - r["submit_s"] for r in res]) * 1e3
     rays = sum(r["rays"] for r in res)
     span = max(r["done_s"] for r in res) - min(r["submit_s"] for r in res)
@@ -691,7 +699,7 @@ def _served_run(cg, scs, reqs, sequential, engine=None):
             "wavefront_busy_s": st["wavefront_busy_s"]}
 
 
-def _plain_renderer_run(cg, scs, bvhs, reqs, modes=None, one_call=False):
+def _plain_renderer_run(cg, scs, bvhs, reqs, modes=None, one_call=False, burst=False):
     """The plain method: the drop-in Renderer API, one request at a time in
     arrival order. Each request gets a Renderer at its resolution, spp
     accumulate_frame_f32 calls (the reference's per-frame loop; one_call: a
@@ -738,14 +746,14 @@ def _plain_renderer_run(cg, scs, bvhs, reqs, modes=None, one_call=False):
     first = last = None
     for i, (at, sc, w, h, spp, cam) in enumerate(reqs):
         dt = t0 + at - time.perf_counter()
-        if dt > 0:
+        if dt > 0 and not burst:
             time.sleep(dt)
         start = time.perf_counter()
         first = start if first is None else first
         rays += run(sc, w, h, spp, cam, i * 16, True)
         last = time.perf_counter()
-        lat.append((last - (t0 + at)) * 1e3)
-    span = last - min(t0 + reqs[0][0], first)
+        lat.append((last - (t0 if burst else t0 + at)) * 1e3)
+    span = last - (t0 if burst else min(t0 + reqs[0][0], first))
     lat = np.array(lat)
     busy = parts["create_s"] + parts["samples_s"] + parts["resolve_s"]
     parts["sample_overhead_s"] = parts["samples_s"] - parts["device_s"]
@@ -797,7 +805,14 @@ def bench_served(cg, duration=2.0, rate=200.0, seed=4):
     # for two wavefront engines with the autotuner's configuration, p99 1.38
     # against 1.61 s). The tuned wavefront engines and the server's defaults are
     # measured beside it.
-    engine = {"refill_mode": cg.REFILL_ALL, "deep_single_launch": 1, "wavefront_streams": 1}
+    # Up to 16 samples of a request per wave, admission capped at 8M pixels
+    # (measured at 200 req/s: 2,158 Mrays/s, p50 369 / p99 791 ms, against
+    # 2,140 and 369 / 1,189 ms uncapped, 2,153 and 526 / 1,191 ms with one
+    # sample per wave; two deep engines 2,128 and 416 / 838 ms).
+    engine = {"refill_mode": cg.REFILL_ALL, "deep_single_launch": 1, "wavefront_streams": 1,
+              "samples_per_wave": 16, "max_inflight_pixels": 8 << 20}
+    # One sample of each request per wave, no cap (the server before sample slots).
+    engine_one = dict(engine, samples_per_wave=1, max_inflight_pixels=0)
     from convector_gb300 import autotune
     wf = [k for k, b in enumerate(bvhs) if b.depth > 40 or b.triangles.shape[0] > 200000]
     wf_engine = {}
@@ -807,6 +822,7 @@ def bench_served(cg, duration=2.0, rate=200.0, seed=4):
         wf_engine = {"blocks_per_sm": best["blocks_per_sm"], "refill_mode": best["refill_mode"],
                      "wavefront_streams": 2}
     served = _served_run(cg, scs, reqs, sequential=False, engine=engine)
+    served_one = _served_run(cg, scs, reqs, sequential=False, engine=engine_one)
     served_wf = _served_run(cg, scs, reqs, sequential=False, engine=wf_engine)
     served_default = _served_run(cg, scs, reqs, sequential=False)
     sequential = _served_run(cg, scs, reqs, sequential=True, engine=engine)
@@ -820,12 +836,24 @@ def bench_served(cg, duration=2.0, rate=200.0, seed=4):
     # accumulate_frames_f32 call (up to 32 samples per launch in the
     # path-refill form).
     plain_one = _plain_renderer_run(cg, scs, bvhs, reqs, modes=[cg.MODE_MEGAKERNEL] * len(scs), one_call=True)
+    # Sustained throughput: the same requests all submitted at once.
+    burst = {"served": _served_run(cg, scs, reqs, sequential=False, engine=engine, burst=True),
+             "plain_renderer": _plain_renderer_run(cg, scs, bvhs, reqs, modes=[cg.MODE_MEGAKERNEL] * len(scs),
+                                                   burst=True),
+             "plain_renderer_frames_in_one_call": _plain_renderer_run(
+                 cg, scs, bvhs, reqs, modes=[cg.MODE_MEGAKERNEL] * len(scs), one_call=True, burst=True)}
+    burst["throughput_ratio"] = burst["served"]["mrays_per_s"] / burst["plain_renderer"]["mrays_per_s"]
+    burst["throughput_ratio_vs_plain_frames_in_one_call"] = \
+        burst["served"]["mrays_per_s"] / burst["plain_renderer_frames_in_one_call"]["mrays_per_s"]
     # Below saturation: half the arrival rate.
     low_rate = rate / 2
     reqs_low = _served_requests(cg, scenes, low_rate, duration, seed + 1)
     served_low = _served_run(cg, scs, reqs_low, sequential=False, engine=engine)
     plain_low = _plain_renderer_run(cg, scs, bvhs, reqs_low, modes=[cg.MODE_MEGAKERNEL] * len(scs))
+    plain_one_low = _plain_renderer_run(cg, scs, bvhs, reqs_low, modes=[cg.MODE_MEGAKERNEL] * len(scs),
+                                        one_call=True)
     return {"rate_per_s": rate, "duration_s": duration, "served": served, "served_engine": engine,
+            "served_one_sample_per_wave": served_one, "all_at_once": burst,
             "served_wavefront_engines": served_wf, "served_wavefront_engine_config": wf_engine,
             "served_default_engine": served_default, "plain_renderer": plain,
             "plain_renderer_wavefront_for_deep": plain_wf,
@@ -838,6 +866,7 @@ def bench_served(cg, duration=2.0, rate=200.0, seed=4):
             "throughput_ratio_default_engine": served_default["mrays_per_s"] / plain["mrays_per_s"],
             "throughput_ratio_vs_server_one_at_a_time": served["mrays_per_s"] / sequential["mrays_per_s"],
             "below_saturation": {"rate_per_s": low_rate, "served": served_low, "plain_renderer": plain_low,
+                                 "plain_renderer_frames_in_one_call": plain_one_low,
                                  "latency_p99_ratio_plain_over_served":
                                      plain_low["latency_ms_p99"] / served_low["latency_ms_p99"]}}
 

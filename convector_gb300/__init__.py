@@ -59,7 +59,9 @@ class _ServerConfig(ctypes.Structure):
                 ("traversal", ctypes.c_uint32), ("use_graph", ctypes.c_uint32), ("sequential", ctypes.c_uint32),
                 ("blocks_per_sm", ctypes.c_uint32), ("refill_mode", ctypes.c_uint32),
                 ("kernel_mode", ctypes.c_uint32), ("fused_blocks_per_sm", ctypes.c_uint32),
-                ("wavefront_streams", ctypes.c_uint32), ("deep_single_launch", ctypes.c_uint32)]
+                ("wavefront_streams", ctypes.c_uint32), ("deep_single_launch", ctypes.c_uint32),
+                ("max_inflight_pixels", ctypes.c_uint64), ("samples_per_wave", ctypes.c_uint32),
+                ("sample_buffer_bytes", ctypes.c_uint64)]
 
 
 class _Request(ctypes.Structure):
@@ -653,11 +655,13 @@ class Server:
 
     def __init__(self, scenes, framebuffer_bytes=4 << 30, max_groups=1 << 21, traversal=TRAVERSE_SINGLE,
                  use_graph=1, sequential=False, blocks_per_sm=0, refill_mode=REFILL_AFTER_CAMERA, kernel_mode=0,
-                 fused_blocks_per_sm=0, wavefront_streams=1, deep_single_launch=0):
+                 fused_blocks_per_sm=0, wavefront_streams=1, deep_single_launch=0, max_inflight_pixels=0,
+                 samples_per_wave=1, sample_buffer_bytes=0):
         self.scenes = list(scenes)
         arr = (ctypes.c_void_p * len(self.scenes))(*[s._h.value for s in self.scenes])
         cfg = _ServerConfig(framebuffer_bytes, max_groups, traversal, use_graph, int(sequential), blocks_per_sm,
-                            refill_mode, kernel_mode, fused_blocks_per_sm, wavefront_streams, deep_single_launch)
+                            refill_mode, kernel_mode, fused_blocks_per_sm, wavefront_streams, deep_single_launch,
+                            max_inflight_pixels, samples_per_wave, sample_buffer_bytes)
         out = ctypes.c_void_p()
         _check(lib().cvx_server_create(arr, len(self.scenes), ctypes.byref(cfg), ctypes.byref(out)))
         self._h = out

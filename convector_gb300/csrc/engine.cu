@@ -215,6 +215,7 @@ int32_t WaveEngine::submit(const std::vector<Job>& jobs_in, WaveOutputs out, cud
         out.group_em = d_group_em_;
         ECK(cudaMemsetAsync(d_group_em_, 0, (size_t)groups * 4, stream), "reset group counters");
     }
+    if (out.samples && !out.group_em) return set_error(CVX_ERR_INVALID, "sample slots need a path-refill wave");
     ECK(cudaMemcpyAsync(d_jobs_, h_jobs_, jobs_in.size() * sizeof(Job), cudaMemcpyHostToDevice, stream),
         "upload jobs");
     ECK(cudaMemcpyAsync(d_hdr_, h_hdr_, sizeof(WaveHeader), cudaMemcpyHostToDevice, stream), "upload jobs");
@@ -459,6 +460,7 @@ struct Request {
     uint32_t groups = 0;
     uint64_t offset = 0;  // pixel offset in the framebuffer pool
     uint32_t next_sample = 0;
+    uint32_t wave_k = 1, wave_job = 0;  // samples in its current wave, and the first one's job index
     int eng = -1;            // engine it is rendered on: 0 single-launch, 1 and 2 wavefront
     bool in_flight = false;  // a sample of it is on the GPU
     bool admitted = false, finished = false, cancelled = false;
@@ -516,6 +518,12 @@ struct cvx_server {
     float* d_accum = nullptr;
     uint32_t* d_rgba = nullptr;
     ResolveItem* d_items = nullptr;
+    // cfg.samples_per_wave > 1: colour slots of the samples after a request's
+    // first in a wave, one region of slot_region_px pixels per engine (an
+    // engine has one wave on the GPU at a time), and their reduction lists
+    float* d_samples = nullptr;
+    uint64_t slot_region_px = 0;
+    SlotItem* d_slot_items = nullptr;
     uint64_t pool_px = 0;
     RangeAlloc pool;
     cudaStream_t stream = nullptr;
@@ -527,6 +535,7 @@ struct cvx_server {
     uint64_t next_id = 1;
     uint32_t eng_groups[kMaxEngines] = {};  // ray-queue groups admitted per engine
     uint32_t eng_jobs[kMaxEngines] = {};
+    uint64_t admitted_px = 0;  // pixels of the admitted requests (cfg.max_inflight_pixels)
     uint64_t arrivals = 0;  // bumped by submissions, cancellations and finished waves
     bool stop = false;
     std::thread worker;
@@ -545,6 +554,7 @@ struct cvx_server {
         q->res.done_s = now();
         if (q->admitted) {
             pool.give(q->offset, q->npx);
+            admitted_px -= q->npx;
             eng_groups[q->eng] -= q->groups;
             eng_jobs[q->eng]--;
             q->admitted = false;
@@ -562,6 +572,11 @@ struct cvx_server {
         while (!pending.empty()) {
             auto& q = pending.front();
             if (cfg.sequential && !admitted.empty()) break;
+            // Pixel cap: in overload, requests then finish in arrival order
+            // instead of all advancing together; the oldest pending request
+            // is admitted whenever none is.
+            if (cfg.max_inflight_pixels && !admitted.empty() && admitted_px + q->npx > cfg.max_inflight_pixels)
+                break;
             int e = 0;
             if (mode[q->r.scene] != 0) {  // the wavefront engine with the fewest admitted groups
                 e = 1;
@@ -575,6 +590,7 @@ struct cvx_server {
                 break;
             q->offset = off;
             q->admitted = true;
+            admitted_px += q->npx;
             q->eng = e;
             q->res.start_s = now();
             q->groups = qg;
@@ -585,26 +601,70 @@ struct cvx_server {
         }
     }
 
-    // Queues the next sample of each request in `reqs` as one wave on engine e.
+    // Queues the next sample of each request in `reqs` as one wave on engine
+    // e; with cfg.samples_per_wave > 1 and an engine that takes sample slots,
+    // up to that many of its next samples, while the engine's jobs, its slot
+    // region and the wave's path numbers last. The first adds to the
+    // accumulator in the wave, the others write slots that
+    // k_accumulate_slots adds after it, in sample order.
     int32_t submit_wave(int e, const std::vector<std::shared_ptr<Request>>& reqs) {
         std::vector<Job> jobs;
+        std::vector<SlotItem> items;
         jobs.reserve(reqs.size());
         cudaStream_t st = stream_of(e);
-        for (auto& q : reqs) {
-            Job j{};
-            std::memcpy(&j.cam, &q->r.camera, sizeof(cvx_camera));
-            j.scene = q->r.scene;
-            j.w = q->r.width;
-            j.h = q->r.height;
-            j.frame = q->r.frame_base + q->next_sample;
-            j.out_offset = q->offset;
-            jobs.push_back(j);
+        WaveEngine* eng = eng_of(e);
+        const uint64_t region = slot_region_px * (uint64_t)e;
+        uint64_t used = 0, groups = 0;
+        for (auto& q : reqs) groups += groups_of(q->r.width, q->r.height);
+        // The wave's groups stay within the engine's ray-queue capacity (which
+        // admission checked for one sample of each request) and below
+        // kMaxRefillGroups (from there a wave takes the octet form).
+        const uint64_t max_groups = std::min<uint64_t>(eng->max_groups(), kMaxRefillGroups - 1);
+        const bool slots = cfg.samples_per_wave > 1 && d_samples && eng->takes_sample_slots() &&
+                           groups <= max_groups;
+        for (size_t i = 0; i < reqs.size(); i++) {
+            auto& q = reqs[i];
+            uint32_t k = 1;
+            if (slots) {
+                const uint32_t g = groups_of(q->r.width, q->r.height);
+                uint64_t fit = std::min<uint64_t>(q->r.spp - q->next_sample, cfg.samples_per_wave);
+                // every later request keeps its first sample's job
+                fit = std::min<uint64_t>(fit, 1 + (eng->max_jobs() - jobs.size() - (reqs.size() - i)));
+                fit = std::min<uint64_t>(fit, 1 + (slot_region_px - used) / q->npx);
+                fit = std::min<uint64_t>(fit, 1 + (max_groups - groups) / g);
+                k = (uint32_t)fit;
+                groups += (uint64_t)(k - 1) * g;
+            }
+            q->wave_job = (uint32_t)jobs.size();
+            q->wave_k = k;
+            for (uint32_t smp = 0; smp < k; smp++) {
+                Job j{};
+                std::memcpy(&j.cam, &q->r.camera, sizeof(cvx_camera));
+                j.scene = q->r.scene;
+                j.w = q->r.width;
+                j.h = q->r.height;
+                j.frame = q->r.frame_base + q->next_sample + smp;
+                j.out_offset = q->offset;
+                j.slot = smp == 0 ? kNoSlot : region + used + (uint64_t)(smp - 1) * q->npx;
+                jobs.push_back(j);
+            }
+            if (k > 1) {
+                items.push_back(SlotItem{q->offset, region + used, (uint32_t)q->npx, k - 1});
+                used += (uint64_t)(k - 1) * q->npx;
+            }
             // a request's accumulator starts at zero with its first sample
             if (q->next_sample == 0) cudaMemsetAsync(d_accum + 3 * q->offset, 0, q->npx * 12, st);
         }
         WaveOutputs out{};
         out.accum = d_accum;
-        return eng_of(e)->submit(jobs, out, st, true);
+        if (!items.empty()) out.samples = d_samples;
+        int32_t r = eng->submit(jobs, out, st, true);
+        if (r || items.empty()) return r;
+        SlotItem* di = d_slot_items + 1024 * e;
+        ECK(cudaMemcpyAsync(di, items.data(), items.size() * sizeof(SlotItem), cudaMemcpyHostToDevice, st),
+            "upload slot list");
+        ECK(launch_accumulate_slots(di, (uint32_t)items.size(), d_accum, d_samples, st), "add sample slots");
+        return CVX_OK;
     }
 
     // Engine e's wave over `reqs` has ended with status st: account for it,
@@ -632,8 +692,9 @@ struct cvx_server {
                     }
                     continue;
                 }
-                q->res.rays += i < jr.size() ? jr[i] : 0;
-                q->next_sample++;
+                for (uint32_t k = 0; k < q->wave_k; k++)
+                    q->res.rays += q->wave_job + k < jr.size() ? jr[q->wave_job + k] : 0;
+                q->next_sample += q->wave_k;
                 if (q->next_sample == q->r.spp && !q->cancelled) {
                     done.push_back(q);
                     items.push_back(ResolveItem{q->offset, (uint32_t)q->npx, 1.0f / (float)q->r.spp});
@@ -764,6 +825,8 @@ struct cvx_server {
         cudaFree(d_accum);
         cudaFree(d_rgba);
         cudaFree(d_items);
+        cudaFree(d_samples);
+        cudaFree(d_slot_items);
         if (stream) cudaStreamDestroy(stream);
         if (stream2) cudaStreamDestroy(stream2);
         for (cudaStream_t x : extra_stream)
@@ -820,6 +883,13 @@ extern "C" int32_t cvx_server_create(cvx_scene* const* scenes, uint32_t n_scenes
     if ((st = alloc(&s->d_accum, s->pool_px * 3, owned))) return st;
     if ((st = alloc(&s->d_rgba, s->pool_px, owned))) return st;
     if ((st = alloc(&s->d_items, (size_t)cvx_server::kMaxEngines * 1024, owned))) return st;
+    if (cfg->samples_per_wave > 1) {
+        const uint64_t bytes = cfg->sample_buffer_bytes ? cfg->sample_buffer_bytes : cfg->framebuffer_bytes;
+        s->slot_region_px = bytes / 12 / (uint64_t)(s->n_wf + 1);
+        if (s->slot_region_px == 0) return set_error(CVX_ERR_INVALID, "sample buffer too small");
+        if ((st = alloc(&s->d_samples, s->slot_region_px * 3 * (uint64_t)(s->n_wf + 1), owned))) return st;
+        if ((st = alloc(&s->d_slot_items, (size_t)cvx_server::kMaxEngines * 1024, owned))) return st;
+    }
     s->pool.init(s->pool_px);
     s->worker = std::thread([p = s.get()] { p->loop(); });
     *out = s.release();

@@ -59,6 +59,9 @@ class WaveEngine {
     uint32_t max_groups() const { return max_groups_; }
     uint32_t max_jobs() const { return max_jobs_; }
     bool fused() const { return fused_; }
+    // Its waves take paths per lane whatever their scenes, so they accept
+    // sample slots (Job::slot, WaveOutputs::samples).
+    bool takes_sample_slots() const { return fused_ && !packet_ && refill_mode_ == CVX_REFILL_ALL; }
 
    private:
     int32_t launch(const WaveOutputs& out, bool deep, cudaStream_t stream);

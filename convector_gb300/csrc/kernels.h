@@ -87,5 +87,9 @@ cudaError_t launch_wave_fused(const Job* jobs, const WaveHeader* hdr, const Devi
                               cudaStream_t stream);
 cudaError_t launch_resolve_multi(const ResolveItem* items, uint32_t n_items, const float* accum, uint32_t* rgba,
                                  cudaStream_t stream);
+// After a wave with sample slots (WaveOutputs::samples): adds each item's
+// slots to its accumulator pixels in sample order.
+cudaError_t launch_accumulate_slots(const SlotItem* items, uint32_t n_items, float* accum, const float* samples,
+                                    cudaStream_t stream);
 
 }  // namespace cvx

@@ -401,7 +401,10 @@ __global__ void __launch_bounds__(128, 8) k_wave_fused(const Job* __restrict__ j
 // p >> 3, which belongs to the job whose group range holds it. Ray counts per
 // job are kept per lane for the job of its current path (the path reference's
 // job) and added to the job's total when the lane moves to another job, and at
-// the end.
+// the end. SLOTS: the wave carries sample slots (WaveOutputs::samples), and a
+// job with one writes its colours there (a separate instantiation, so that
+// waves without slots run the loop they ran before).
+template <bool SLOTS>
 struct WavePaths {
     struct PathRef {
         uint32_t path, job;
@@ -466,6 +469,16 @@ struct WavePaths {
         uint32_t gx, gy, px, py;
         origin(r, j, gx, gy, px, py);
         if (px >= j.w || py >= j.h) return;
+        if (SLOTS) {
+            const uint64_t slot = j.slot;
+            if (slot != kNoSlot) {
+                float* o = out.samples + 3 * (slot + (size_t)py * j.w + px);
+                o[0] = c.x;
+                o[1] = c.y;
+                o[2] = c.z;
+                return;
+            }
+        }
         const size_t idx = (size_t)j.out_offset + (size_t)py * j.w + px;
         if (out.rgba) out.rgba[idx] = pack_color(c);
         if (out.color) {
@@ -501,13 +514,13 @@ constexpr int kRefillWaveBlocksPerSm = 7;
 // from global memory (4 tube views of 1280x736, 2 samples: 21.5 -> 20.3 ms;
 // 12 entries 20.5 ms; three or four steps per round 20.3, 22.5 ms).
 constexpr int kDeepWaveStackShared = 16;
-template <int CLAIM_MIN>
+template <int CLAIM_MIN, bool SLOTS = false>
 __global__ void __launch_bounds__(128, kRefillWaveBlocksPerSm) k_wave_refill(const Job* __restrict__ jobs,
                                                                           const WaveHeader* __restrict__ hdr,
                                                                           const DeviceScene* __restrict__ scenes,
                                                                           WaveOutputs out) {
     constexpr int kShared = CLAIM_MIN == 8 ? kDeepWaveStackShared : 0;
-    WavePaths P{jobs, scenes, out, hdr->n_jobs, hdr->n_groups, 0u, 0u};
+    WavePaths<SLOTS> P{jobs, scenes, out, hdr->n_jobs, hdr->n_groups, 0u, 0u};
     bool ok;
     if constexpr (kShared > 0) {
         __shared__ uint2 sstack[4][kShared][32];
@@ -544,11 +557,18 @@ cudaError_t launch_wave_fused(const Job* jobs, const WaveHeader* hdr, const Devi
                               cudaStream_t stream) {
     if (!packet && out.group_em) {
         uint32_t grid = (uint32_t)sms() * kRefillWaveBlocksPerSm;
+        if (out.samples) {  // sample slots: no gbuffer (several samples of an image share the wave)
+            if (out.gbuf) return cudaErrorInvalidValue;
+            if (deep) k_wave_refill<8, true><<<grid, 128, 0, stream>>>(jobs, hdr, scenes, out);
+            else k_wave_refill<16, true><<<grid, 128, 0, stream>>>(jobs, hdr, scenes, out);
+            return cudaGetLastError();
+        }
         if (deep) k_wave_refill<8><<<grid, 128, 0, stream>>>(jobs, hdr, scenes, out);
         else k_wave_refill<16><<<grid, 128, 0, stream>>>(jobs, hdr, scenes, out);
         if (out.gbuf) k_wave_emitter_groups<<<(uint32_t)sms() * 4u, 256, 0, stream>>>(jobs, hdr, out);
         return cudaGetLastError();
     }
+    if (out.samples) return cudaErrorInvalidValue;  // slots need the path-refill wave
     if (blocks_per_sm == 0) blocks_per_sm = 16;
     uint32_t grid = (uint32_t)sms() * blocks_per_sm;
     if (packet) k_wave_fused<true><<<grid, 128, 0, stream>>>(jobs, hdr, scenes, out);
@@ -566,6 +586,30 @@ __global__ void k_resolve_multi(const ResolveItem* __restrict__ items, uint32_t 
             rgba[p] = pack_color(c);
         }
     }
+}
+
+// After a wave with sample slots: each item's slots added to its accumulator
+// in sample order, after the sample the wave added directly. These are the
+// additions one wave per sample makes, in the same order.
+__global__ void k_accumulate_slots(const SlotItem* __restrict__ items, uint32_t n_items, float* __restrict__ accum,
+                                   const float* __restrict__ samples) {
+    for (uint32_t it = blockIdx.y; it < n_items; it += gridDim.y) {
+        const SlotItem r = items[it];
+        const size_t nf = (size_t)3 * r.npx;
+        for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < nf; i += (size_t)gridDim.x * blockDim.x) {
+            float v = accum[3 * r.accum_offset + i];
+            for (uint32_t k = 0; k < r.count; k++) v += __ldg(samples + 3 * r.slot + (size_t)k * nf + i);
+            accum[3 * r.accum_offset + i] = v;
+        }
+    }
+}
+
+cudaError_t launch_accumulate_slots(const SlotItem* items, uint32_t n_items, float* accum, const float* samples,
+                                    cudaStream_t stream) {
+    if (n_items == 0) return cudaSuccess;
+    dim3 grid(64, n_items < 1024 ? n_items : 1024);
+    k_accumulate_slots<<<grid, 256, 0, stream>>>(items, n_items, accum, samples);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_resolve_multi(const ResolveItem* items, uint32_t n_items, const float* accum, uint32_t* rgba,

@@ -20,6 +20,22 @@ struct Job {
     uint32_t group_base;  // first wave-global group index of this job
     uint32_t n_groups;    // 8 * ceil(w/16) * ceil(h/4)
     uint64_t out_offset;  // first pixel of this image in the output buffers
+    // Waves with WaveOutputs::samples (path refill only): kNoSlot, or the
+    // first pixel of this job's colour slot there; the job then writes its
+    // colours to the slot instead of the outputs, and a pass after the wave
+    // adds the slots to the accumulator in sample order (several samples of
+    // one image in one wave).
+    uint64_t slot;
+};
+constexpr uint64_t kNoSlot = ~0ull;
+
+// A request's samples 1 .. count of one wave, added after it: accum pixels
+// from accum_offset, count slots of npx pixels each from slot.
+struct SlotItem {
+    uint64_t accum_offset;
+    uint64_t slot;
+    uint32_t npx;
+    uint32_t count;
 };
 
 struct WaveHeader {
@@ -53,6 +69,8 @@ struct WaveOutputs {
     // one word per group of the wave, zero at launch: given, a single-ray
     // fused wave takes paths per lane (k_wave_refill)
     uint32_t* group_em;
+    // colour slots of the jobs' Job::slot (3 floats per pixel), or null
+    float* samples;
 };
 
 // One image to resolve from the accumulator (renderer.rs:378-410).

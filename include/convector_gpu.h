@@ -387,6 +387,18 @@ typedef struct cvx_server_config {
     uint32_t deep_single_launch; /* 1: the engines of the deep scenes (those in wavefront mode)
                                     run their waves as single launches instead of the wavefront
                                     kernels, keeping their streams and priority */
+    uint64_t max_inflight_pixels; /* 0: admit while framebuffer memory lasts; else admitted
+                                     requests hold at most this many pixels (the oldest queued
+                                     request is admitted whenever none is), so that in overload
+                                     requests finish in arrival order instead of all together */
+    uint32_t samples_per_wave;    /* 0, 1: a wave takes the next sample of each admitted request;
+                                     n > 1: up to n of its next samples, on the single-launch
+                                     engines that take paths per lane (CVX_REFILL_ALL, single-ray
+                                     traversal; the others take one). The samples are added to the
+                                     request's accumulator in sample order, so its image is the
+                                     same either way */
+    uint64_t sample_buffer_bytes; /* device memory for those samples' colours (0: as much as
+                                     framebuffer_bytes), shared among the engines */
 } cvx_server_config;
 
 typedef struct cvx_request {

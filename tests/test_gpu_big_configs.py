@@ -115,12 +115,10 @@ def test_large_mesh_full_frame_bitexact_against_oracle(gpu, orc):
     assert (r.read_accumulator().view(np.uint32) == acc.view(np.uint32)).all()
 
 
-def test_served_benchmark_requests_equal_alone(gpu):
-    """24 requests of the served workload's own stream (3 resident scenes,
-    Poisson arrivals, poses on a radius-3 sphere, 320x184 to 1920x1080, 1 to
-    16 spp), served with the benchmark's engine configuration (the tube on a
-    single-launch deep engine, paths per lane) and all submitted at once, so
-    that they share waves: each image equals the request rendered alone."""
+@pytest.fixture(scope="module")
+def served_stream(gpu):
+    """24 requests of the served workload's own stream and each one's image
+    rendered alone (one accumulate_frame_f32 call per sample)."""
     import bench
     scs = []
     for gen in (scenes.room_sphere, lambda obj: scenes.displaced_icosphere(obj=obj, light=True),
@@ -128,16 +126,31 @@ def test_served_benchmark_requests_equal_alone(gpu):
         scs.append(gpu.Scene(gpu.Bvh.build(gen(obj=False)[0])))
     reqs = bench._served_requests(gpu, scenes, 200.0, 2.0, 4)[:24]
     assert {sc for _, sc, *_ in reqs} == {0, 1, 2}
-    srv = gpu.Server(scs, framebuffer_bytes=4 << 30, max_groups=1 << 21, refill_mode=gpu.REFILL_ALL,
-                     deep_single_launch=1)
-    ids = [srv.submit(sc, w, h, spp, cam, frame_base=16 * i) for i, (_, sc, w, h, spp, cam) in enumerate(reqs)]
-    for i, rid in enumerate(ids):
-        st, img, _ = srv.wait(rid, 600000)
-        assert st == 0
-        _, sc, w, h, spp, cam = reqs[i]
+    alone = []
+    for i, (_, sc, w, h, spp, cam) in enumerate(reqs):
         r = gpu.Renderer(scs[sc], w, h, rng_order=gpu.RNG_GROUP, traversal=gpu.TRAVERSE_SINGLE)
         r.set_camera(cam)
         for s in range(spp):
             r.accumulate_frame_f32(16 * i + s)
-        assert (img == r.resolve_u8(spp)).all(), i
+        alone.append(r.resolve_u8(spp))
+    return scs, reqs, alone
+
+
+@pytest.mark.parametrize("extra", [{}, {"samples_per_wave": 16}, {"samples_per_wave": 16, "max_inflight_pixels": 4 << 20}])
+def test_served_benchmark_requests_equal_alone(gpu, served_stream, extra):
+    """24 requests of the served workload's own stream (3 resident scenes,
+    Poisson arrivals, poses on a radius-3 sphere, 320x184 to 1920x1080, 1 to
+    16 spp), served with the benchmark's engine configuration (the tube on a
+    single-launch deep engine, paths per lane; one sample per request per
+    wave, or up to 16, with admission capped by pixels or not) and all
+    submitted at once, so that they share waves: each image equals the request
+    rendered alone."""
+    scs, reqs, alone = served_stream
+    srv = gpu.Server(scs, framebuffer_bytes=4 << 30, max_groups=1 << 21, refill_mode=gpu.REFILL_ALL,
+                     deep_single_launch=1, **extra)
+    ids = [srv.submit(sc, w, h, spp, cam, frame_base=16 * i) for i, (_, sc, w, h, spp, cam) in enumerate(reqs)]
+    for i, rid in enumerate(ids):
+        st, img, _ = srv.wait(rid, 600000)
+        assert st == 0
+        assert (img == alone[i]).all(), i
     srv.close()

@@ -173,6 +173,47 @@ def test_server_two_engines_concurrent_equal_alone(two_scenes, gpu, wavefront_st
     srv.close()
 
 
+@pytest.mark.parametrize("samples_per_wave,slot_bytes,cap,two_engines,max_groups", [
+    (16, 0, 0, False, 1 << 14),
+    (4, 100 * 96 * 12 * 2, 0, False, 1 << 14),  # slots for two extra samples of the largest request per wave
+    (16, 0, 64 * 50, False, 1 << 14),           # at most one 64x50 image admitted at a time
+    (8, 0, 0, True, 1 << 14),                   # scene 1 on the deep-scene engine (single launch)
+    (8, 0, 0, True, 1500),                      # its waves limited to 1500 groups (a 100x96 image: 1344)
+])
+def test_server_samples_per_wave_equal_alone(two_scenes, gpu, samples_per_wave, slot_bytes, cap, two_engines,
+                                             max_groups):
+    """Several samples of a request in one wave: the first adds to the
+    accumulator in the wave, the others are written to slots and added after
+    it in sample order, so every image and ray count equals the request
+    rendered alone, with too little slot memory for all samples at once, with
+    admission capped by pixels and with a deep-scene engine whose ray-queue
+    capacity bounds its waves; and the requests take fewer waves than
+    samples."""
+    scs = [s for _, s, _ in two_scenes]
+    srv = gpu.Server(scs, framebuffer_bytes=64 << 20, max_groups=max_groups, refill_mode=gpu.REFILL_ALL,
+                     kernel_mode=1, deep_single_launch=1, samples_per_wave=samples_per_wave,
+                     sample_buffer_bytes=slot_bytes, max_inflight_pixels=cap)
+    if two_engines:
+        srv.set_scene_mode(1, gpu.MODE_WAVEFRONT)
+    rng = np.random.default_rng(12)
+    reqs, ids = [], []
+    for k in range(12):
+        cam = gpu.Camera()
+        scenes.default_camera(cam, eye=(rng.uniform(-1, 1), 1.2, 1.6))
+        reqs.append((k % 2, int(rng.choice([64, 100])), int(rng.choice([50, 96])), int(rng.integers(1, 9)), cam))
+    for i, (sc, w, h, spp, cam) in enumerate(reqs):
+        ids.append(srv.submit(sc, w, h, spp, cam, frame_base=9 * i))
+    for i, rid in enumerate(ids):
+        st, img, info = srv.wait(rid)
+        sc, w, h, spp, cam = reqs[i]
+        assert st == 0
+        rays = []
+        assert (img == _alone(gpu, scs[sc], gpu.View(sc, w, h, spp, 9 * i, cam), rays)).all(), i
+        assert info["rays"] == rays[0]
+    assert srv.stats()["waves"] < sum(r[3] for r in reqs)
+    srv.close()
+
+
 def test_server_admission_cancel_timeout(two_scenes, gpu):
     scs = [s for _, s, _ in two_scenes]
     cam = scenes.default_camera(gpu.Camera())
