@@ -665,7 +665,8 @@ def _served_run(cg, scs, reqs, sequential, engine=None, burst=False):
     """The requests through a Server, each submitted at its arrival time
     (burst: all at once, which measures the throughput the server sustains)."""
     engine = engine or {}
-    srv = cg.Server(scs, framebuffer_bytes=24 << 30, max_groups=1 << 21, traversal=cg.TRAVERSE_SINGLE,
+    srv = cg.Server(scs, framebuffer_bytes=24 << 30, max_groups=engine.get("max_groups", 1 << 21),
+                    traversal=cg.TRAVERSE_SINGLE,
                     sequential=sequential, blocks_per_sm=engine.get("blocks_per_sm", 0),
                     refill_mode=engine.get("refill_mode", cg.REFILL_AFTER_CAMERA),
                     fused_blocks_per_sm=engine.get("fused_blocks_per_sm", 0),
