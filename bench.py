@@ -571,7 +571,8 @@ def bench_large(cg):
     ms = out["autotuned"]["frame_ms_p50"]
     out["roofline"] = frame_roofline(work, scene.direct_sample_num(), 1280 * 736, ms, 24, "k_render_refill@tube")
     out["roofline"]["frame_ms"] = ms
-    out["in_one_call"]["roofline"] = frame_roofline(work, scene.direct_sample_num(), 1280 * 736, per, 24)
+    out["in_one_call"]["roofline"] = frame_roofline(work, scene.direct_sample_num(), 1280 * 736, per, 24,
+                                                    "k_render_refill@tube-32")
     if CPU_BASELINE:
         out["cpu_baseline"] = cpu_frame_baseline(bvh, scene.camera, 1280, 736, 42, accumulate=True, target_s=5.0,
                                                  max_frames=2)
