@@ -11,9 +11,10 @@ arrays' full size, so nothing faults and the context stays usable. After the
 error the same handle must give the results of a handle that never failed.
 
 Allocation failures are injected on the host (cvx_inject_allocation_failure)
-at every allocation of scene, renderer, batch and server creation in turn:
-each must return CVX_ERR_CAPACITY, hand out no handle and leak no device
-memory.
+at every allocation of scene, renderer, batch and server creation in turn
+(a server with sample slots among them): each must return CVX_ERR_CAPACITY,
+hand out no handle and leak no device memory; a renderer whose sample buffers
+fail to allocate at its first multi-frame call stays usable.
 """
 
 import contextlib
@@ -89,6 +90,23 @@ def test_frame_reports_stack_overflow(room, gpu, form):
     assert (rgba == rgba_ref).all() and (gb == gb_ref).all()
 
 
+@pytest.mark.parametrize("kw", [dict(rng_order=1, traversal=1, refill_mode=1), dict(rng_order=1, traversal=0)],
+                         ids=["shared_launches", "launch_per_frame"])
+def test_multi_frame_accumulation_reports_stack_overflow(room, gpu, kw):
+    """cvx_accumulate_frames_f32 returns the kernel's status; after a clear
+    the same renderer accumulates what a fresh one does."""
+    ref = gpu.Renderer(room, 96, 64, **kw)
+    ref.accumulate_frames_f32(3, 5)
+    r = gpu.Renderer(room, 96, 64, **kw)
+    with stack_limit(gpu, 2):
+        with pytest.raises(gpu.CvxError) as e:
+            r.accumulate_frames_f32(3, 5)
+    assert e.value.status == CVX_ERR_DEVICE
+    r.clear_accumulator()
+    r.accumulate_frames_f32(3, 5)
+    assert (r.read_accumulator().view(np.uint32) == ref.read_accumulator().view(np.uint32)).all()
+
+
 @pytest.mark.parametrize("mode,refill", [(0, 2), (0, 1), (1, 0)])
 def test_batch_reports_stack_overflow(room, gpu, mode, refill):
     """Single-launch waves with one octet per group (k_wave_fused), with paths
@@ -106,10 +124,10 @@ def test_batch_reports_stack_overflow(room, gpu, mode, refill):
         assert (a == b).all()
 
 
-@pytest.mark.parametrize("kernel_mode,refill", [(1, 1), (2, 0)])
-def test_server_request_reports_stack_overflow(room, gpu, kernel_mode, refill):
+@pytest.mark.parametrize("kernel_mode,refill,samples_per_wave", [(1, 1, 1), (2, 0, 1), (1, 1, 4)])
+def test_server_request_reports_stack_overflow(room, gpu, kernel_mode, refill, samples_per_wave):
     srv = gpu.Server([room], framebuffer_bytes=16 << 20, max_groups=1 << 14, kernel_mode=kernel_mode,
-                     refill_mode=refill)
+                     refill_mode=refill, samples_per_wave=samples_per_wave)
     cam = scenes.default_camera(gpu.Camera())
     st, ref, _ = srv.wait(srv.submit(0, 64, 48, 2, cam, frame_base=5))
     assert st == 0
@@ -161,11 +179,28 @@ def test_allocation_failures_at_creation(room, gpu):
         "batch": _fail_each_allocation(gpu, lambda: gpu.Batch([room], max_groups=1 << 20, max_pixels=1 << 22)),
         "server": _fail_each_allocation(gpu, lambda: gpu.Server([room], framebuffer_bytes=256 << 20,
                                                                 max_groups=1 << 20)),
+        "server with sample slots": _fail_each_allocation(
+            gpu, lambda: gpu.Server([room], framebuffer_bytes=256 << 20, max_groups=1 << 20,
+                                    refill_mode=gpu.REFILL_ALL, samples_per_wave=8)),
     }
     for what, n in counts.items():
         assert n >= 3, (what, n)
     # every partial creation released what it had allocated
     assert abs(_free_bytes() - free0) < (32 << 20), counts
+    # the renderer's sample buffers, allocated at its first multi-frame call
+    r = gpu.Renderer(room, 256, 128, rng_order=1, traversal=1, refill_mode=1)
+    gpu.inject_allocation_failure(0)
+    try:
+        with pytest.raises(gpu.CvxError) as e:
+            r.accumulate_frames_f32(0, 4)
+    finally:
+        gpu.inject_allocation_failure(-1)
+    assert e.value.status == CVX_ERR_CAPACITY
+    r.accumulate_frames_f32(0, 4)
+    ref = gpu.Renderer(room, 256, 128, rng_order=1, traversal=1, refill_mode=1)
+    for f in range(4):
+        ref.accumulate_frame_f32(f)
+    assert (r.read_accumulator().view(np.uint32) == ref.read_accumulator().view(np.uint32)).all()
     # and the library still works
     o, d = scenes.random_rays(1000, seed=5)
     t, tri = room.intersect_nearest(o, d, traversal=1)
