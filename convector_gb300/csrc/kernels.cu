@@ -596,8 +596,16 @@ __global__ void __launch_bounds__(256) k_accumulate_samples(float* __restrict__ 
     }
 }
 
+// One resident block per SM is all the launch bound asks: the frame's few
+// hundred chains leave most warp slots empty, so registers are free, and with
+// the bound of 128 threads alone the compiler capped the kernel at 64
+// registers and spilled 48 bytes (packet 32) on the chains' critical path.
+// Without the cap (118 and 100 registers, no spill): room frame 17.49 ->
+// 17.01 ms, icosphere 26.52 -> 26.00 ms. (The packet traversal's stack top
+// held in registers, as in the refill step, measured slower: packet query
+// 2.92 -> 3.03 ms, packet frame 1.21 -> 1.32 ms.)
 template <bool PACKET>
-__global__ void __launch_bounds__(128) k_render_patch(FrameArgs a) {
+__global__ void __launch_bounds__(128, 1) k_render_patch(FrameArgs a) {
     __shared__ ApproxTables tab;
     load_tables(tab);
     const int k = threadIdx.x & 7;
