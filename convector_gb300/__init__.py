@@ -538,7 +538,8 @@ class Renderer:
     def accumulate_frames_f32(self, first_frame, n_frames, gbuffer=False):
         """accumulate_frame_f32 for frames first_frame .. first_frame +
         n_frames - 1 in one call (cvx_accumulate_frames_f32): the same bits,
-        with up to 32 frames per launch in the path-refill form."""
+        with up to 32 frames per path-refill launch for a single-launch,
+        single-ray renderer in the per-group RNG order."""
         gb = np.empty((self.height, self.width), dtype=np.uint32) if gbuffer else None
         _check(lib().cvx_accumulate_frames_f32(self._h, first_frame, n_frames, _ptr(gb)))
         return gb
