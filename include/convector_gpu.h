@@ -368,9 +368,10 @@ void cvx_batch_destroy(cvx_batch* b);
 /* ---- device: request server ----------------------------------------------
  * A request loop on its own host thread over resident scenes: submitted
  * requests wait in FIFO order and are admitted while their framebuffer and
- * ray-queue memory fit the budget; every wave renders the next sample of
- * every admitted request, so requests that arrive while others are on the
- * GPU join the next wave (continuous batching). No reference counterpart. */
+ * ray-queue memory fit the budget; every wave renders the next sample (or,
+ * with samples_per_wave, the next samples) of every admitted request, so
+ * requests that arrive while others are on the GPU join the next wave
+ * (continuous batching). No reference counterpart. */
 typedef struct cvx_server_config {
     uint64_t framebuffer_bytes; /* device memory for admitted requests' images */
     uint32_t max_groups;        /* ray-queue capacity of one wave, in 8-pixel groups */

@@ -10,6 +10,10 @@
   3 sigma (renderer.rs:339-410 accumulates and resolves the samples).
 * The 256-scene batch (500..20,000 triangles each, 4 spp): 16 of its views,
   drawn across the three resolutions, equal the same views rendered alone.
+* The tube's full frame from the deep-tree path-refill kernel, bit-exact
+  against the oracle, and 24 requests of the served benchmark's stream, each
+  equal to the request rendered alone, served with one sample per wave, with
+  up to 16, and with admission capped by pixels.
 """
 
 import numpy as np
