@@ -60,3 +60,32 @@ def test_batched_workload_shape(cvx):
     for n in (500, 1234, 5000, 20000):
         t, _ = scenes.spheres_and_boxes(n, 3, obj=False)
         assert n <= t.shape[0] <= 1.02 * n + 2
+
+
+def test_served_workload_shape(cvx):
+    """The served stream: Poisson arrivals at 200/s over 2 s (415 requests
+    with the benchmark's seed), widths log-uniform from 320 to 1920 at the
+    320x184 aspect up to a height of 1080, 1..16 spp, all three scenes,
+    cameras on the radius-3 sphere around the room centre."""
+    import numpy as np
+
+    import bench
+    from convector_gb300 import scenes
+    reqs = bench._served_requests(cvx, scenes, 200.0, 2.0, 4)
+    assert len(reqs) == 415
+    at = np.array([r[0] for r in reqs])
+    assert (np.diff(at) > 0).all() and 0.0 < at[0] and at[-1] <= 2.0
+    assert {r[1] for r in reqs} == {0, 1, 2}
+    w = np.array([r[2] for r in reqs])
+    h = np.array([r[3] for r in reqs])
+    assert w.min() >= 320 and w.max() <= 1920 and h.min() >= 184 and h.max() <= 1080
+    # the 320x184 aspect, the height clamped to 1080 (1920 x 184 / 320 is 1104)
+    assert (h == np.minimum(1080, np.maximum(184, np.round(w * 184 / 320)))).all()
+    # log-uniform: the median width near sqrt(320 * 1920) = 784
+    assert 650 < np.median(w) < 950
+    spp = np.array([r[4] for r in reqs])
+    assert spp.min() == 1 and spp.max() == 16
+    center = np.array([0.0, 1.25, -2.0])
+    for r in reqs[:20]:
+        eye = np.array(r[5].as_array()[:3], dtype=np.float64)
+        assert abs(np.linalg.norm(eye - center) - 3.0) < 1e-4
