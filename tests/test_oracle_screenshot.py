@@ -1,6 +1,8 @@
-"""The oracle's frame path against the reference's own output: the
-accumulative-mode screenshot the reference ships (screenshots/accumulative.png,
-1280x736, its indoor scene after a few minutes of accumulation).
+"""The oracle's frame path against the reference's own output: the two
+screenshots the reference ships, of its indoor scene at 1280x736. The
+accumulative one (screenshots/accumulative.png) after a few minutes of
+accumulation; the interactive one (screenshots/interactive.png, last test
+below) in real-time mode, with the camera moving.
 
 The reference renders that view in accumulative mode at a fixed time, with
 the camera on its interactive path: angle alpha = 0.1 - 0.02 t
@@ -124,3 +126,55 @@ def test_accumulated_frame_matches_the_screenshot(cvx, orc, indoor):
     flipped = displayed(floor[::-1].copy(), wood[::-1].copy())
     for k in (1, 2):
         assert diff(flipped, k)[2].mean() > diff(ours, k)[2].mean() + 2.0
+
+
+# The interactive screenshot (screenshots/interactive.png): the reference in
+# its real-time mode, each frame one sample with the camera moving over the
+# frame (scene.rs:81-88: every ray at its own time within the frame), the
+# display blending the last 8 frames and taking the median (ui.rs:313-364).
+# Fitted on the camera path: the last frame at alpha = -0.989 and a frame time
+# of 0.14 s (the reference measured about 10 fps on its author's machine).
+INTERACTIVE = os.path.join(REFERENCE, "screenshots", "interactive.png")
+ALPHA_LAST, FRAME_TIME = -0.989, 0.14
+
+
+def _interactive(cvx, orc, indoor, textures, w, h, seed, frame_time=FRAME_TIME):
+    disp = orc.OracleDisplay(w, h, *textures)
+    t_last = (0.1 - ALPHA_LAST) / 0.02
+    for k in range(8):  # main.rs:124-153: set_time(time, time_delta), update_scene, one frame
+        cam = cvx.Camera()
+        cam.set_interactive(t_last - (7 - k) * frame_time, frame_time)
+        rgba, gbuf, _, _ = indoor.render(cam.as_array(), w, h, 5000 + 17 * seed + k, rng_order=orc.RNG_PATCH,
+                                         traversal=orc.TRAVERSE_PACKET, color=False)
+        out = disp.frame(rgba, gbuf, blend=True, median=True)
+    return np.stack([(out >> (8 * j)) & 255 for j in range(3)], axis=2).astype(np.float64)[::-1]
+
+
+@pytest.mark.skipif(not os.path.isfile(INTERACTIVE), reason="no interactive screenshot")
+def test_interactive_frames_match_the_screenshot(cvx, orc, indoor):
+    """Two independent draws of the oracle's interactive pipeline differ from
+    each other exactly as they differ from the screenshot: the same mean
+    (within a level) and the same spread per pixel and over 16x16 blocks
+    (measured: std 19.45 / 17.85 / 16.96 against 19.41 / 17.81 / 16.91, block
+    MAE 1.99 against 1.97 in R). The comparison sees the motion: without it
+    the block MAE doubles (3.9 in R), as it does with the camera 0.01 rad away
+    or twice the frame time; half the frame time gives 1.5 times."""
+    textures = [read_jpeg_rgb(f) for f in TEXTURES]
+    shot = read_png_rgb(INTERACTIVE).astype(np.float64)
+    a, b, c = (_interactive(cvx, orc, indoor, textures, W, H, s) for s in range(3))
+    keep = ~((shot >= 250).all(axis=2) | (a >= 250).all(axis=2) | (b >= 250).all(axis=2))
+
+    def blocks(img):
+        return img.reshape(H // 16, 16, W // 16, 16, 3).mean(axis=(1, 3))
+
+    keep_blocks = blocks(keep[..., None].repeat(3, axis=2).astype(np.float64))[..., 0] == 1.0
+    to_shot, to_self = (a - shot)[keep], (b - c)[keep]
+    print("interactive: mean %s / %s, std %s / %s" % (to_shot.mean(axis=0).round(2), to_self.mean(axis=0).round(2),
+                                                      to_shot.std(axis=0).round(2), to_self.std(axis=0).round(2)))
+    assert (np.abs(to_shot.mean(axis=0)) <= 1.0).all()
+    assert (np.abs(to_shot.std(axis=0) / to_self.std(axis=0) - 1.0) <= 0.03).all()
+    mae_shot = np.abs(blocks(a) - blocks(shot))[keep_blocks].mean(axis=0)
+    mae_self = np.abs(blocks(b) - blocks(c))[keep_blocks].mean(axis=0)
+    assert (mae_shot <= 1.1 * mae_self).all(), (mae_shot, mae_self)
+    still = _interactive(cvx, orc, indoor, textures, W, H, 0, frame_time=0.0)
+    assert (np.abs(blocks(still) - blocks(shot))[keep_blocks].mean(axis=0) >= 1.6 * mae_self).all()
