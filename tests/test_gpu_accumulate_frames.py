@@ -7,8 +7,8 @@ the accumulator, the last frame's colour buffer and gbuffer, and the ray count
 must equal those of one cvx_accumulate_frame_f32 call per frame, bit for bit:
 on the deep-tree kernel (the 870k-triangle tube), the shallow one (room, paths
 per lane, and a renderer set to one octet per group), the packet, wavefront
-and patch-order forms, at ragged frame sizes, and across launch boundaries (33
-and 40 frames: 32 + 1 and 32 + 8)."""
+and patch-order forms, a moving camera and the debug view, at ragged frame
+sizes, and across launch boundaries (33 and 40 frames: 32 + 1 and 32 + 8)."""
 
 import numpy as np
 import pytest
@@ -81,6 +81,32 @@ def test_other_forms(gpu, room, form):
           "wavefront": dict(rng_order=1, traversal=1, mode=1, use_graph=1),
           "patch_order": dict(rng_order=0, traversal=0)}[form]
     _same(_one_by_one(gpu, room, 200, 120, kw, 3, 4), _in_one_call(gpu, room, 200, 120, kw, 3, 4))
+
+
+def test_moving_camera_and_debug_view(gpu, room):
+    """A camera moving over each frame (Renderer::set_time with a time step,
+    then update_scene) takes shared launches too; the debug view takes a
+    launch per frame. Both equal one call per frame."""
+    def moving(r):
+        r.set_time(3.5, 0.1)
+        r.update_scene()
+
+    def debug(r):
+        r.toggle_debug_view(True)
+
+    for prepare in (moving, debug):
+        a = gpu.Renderer(room, 200, 120, **REFILL)
+        b = gpu.Renderer(room, 200, 120, **REFILL)
+        prepare(a)
+        prepare(b)
+        rays = 0
+        for f in range(5, 11):
+            a.accumulate_frame_f32(f)
+            rays += a.stats()[0]
+        b.accumulate_frames_f32(5, 6)
+        assert (a.read_accumulator().view(np.uint32) == b.read_accumulator().view(np.uint32)).all()
+        assert (a.read_frame_f32().view(np.uint32) == b.read_frame_f32().view(np.uint32)).all()
+        assert rays == b.stats()[0]
 
 
 def test_accumulation_equals_oracle(gpu, orc, room):
